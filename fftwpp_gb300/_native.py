@@ -1,0 +1,116 @@
+"""ctypes binding of lib_fftwpp.so (the C ABI of include/cfftw++.h and
+include/fftwpp_gb300.h).
+
+Loading fails loudly when the library is missing: there is no CPU fallback
+anywhere in this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib_fftwpp.so")
+
+PAD, CENTERED, HERMITIAN, REAL = 0, 1, 2, 3
+F64, F32 = 0, 1
+MULT = {"none": 0, "binary": 1, "realbinary": 2, "correlation": 3,
+        "realjacobian": 4, "jacobian": 5, "realjacadj": 6, "dot": 7}
+
+_lib = None
+
+
+class NativeLibraryMissing(RuntimeError):
+    pass
+
+
+def load():
+    """Load lib_fftwpp.so and declare every prototype."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise NativeLibraryMissing(
+            f"{LIB_PATH} is missing; build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'` "
+            "(the GPU path has no fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    sz = ctypes.c_size_t
+    vp = ctypes.c_void_p
+    P = ctypes.POINTER
+
+    lib.fgb_create.restype = vp
+    lib.fgb_create.argtypes = [ctypes.c_int, P(ctypes.c_int), P(sz), P(sz),
+                               P(sz), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_int, sz]
+    lib.fgb_convolve_device.restype = ctypes.c_int
+    lib.fgb_convolve_device.argtypes = [vp, P(vp), P(vp), vp]
+    lib.fgb_convolve_host.restype = ctypes.c_int
+    lib.fgb_convolve_host.argtypes = [vp, P(vp), P(vp)]
+    lib.fgb_info.restype = ctypes.c_int
+    lib.fgb_info.argtypes = [vp, P(ctypes.c_long)]
+    lib.fgb_destroy.restype = None
+    lib.fgb_destroy.argtypes = [vp]
+    lib.fgb_last_error.restype = ctypes.c_char_p
+    lib.fgb_last_error.argtypes = []
+    lib.fgb_parameters.restype = None
+    lib.fgb_parameters.argtypes = [sz, sz, sz, ctypes.c_int, P(sz), P(sz), P(sz)]
+    lib.fgb_nextfftsize.restype = sz
+    lib.fgb_nextfftsize.argtypes = [sz]
+    lib.fgb_index.restype = sz
+    lib.fgb_index.argtypes = [ctypes.c_int, sz, sz, sz, sz, sz, sz, sz]
+    lib.fgb_hermitian_symmetrize_x_device.restype = ctypes.c_int
+    lib.fgb_hermitian_symmetrize_x_device.argtypes = [sz, sz, sz, vp,
+                                                      ctypes.c_int, vp]
+
+    # FFTW++-compatible entry points (wrappers/cfftw++.h).
+    for name in ("conv1d", "hconv1d", "conv2d", "hconv2d", "conv3d",
+                 "hconv3d"):
+        create = getattr(lib, f"fftwpp_create_{name}")
+        create.restype = vp
+        dims = {"1d": 1, "2d": 2, "3d": 3}[name[-2:]]
+        create.argtypes = [sz] * dims
+        conv = getattr(lib, f"fftwpp_{name}_convolve")
+        conv.restype = None
+        conv.argtypes = [vp, vp, vp]
+        delete = getattr(lib, f"fftwpp_{name}_delete")
+        delete.restype = None
+        delete.argtypes = [vp]
+    lib.fftwpp_HermitianSymmetrize.argtypes = [vp]
+    lib.fftwpp_HermitianSymmetrizeX.argtypes = [sz, sz, sz, vp]
+    lib.fftwpp_HermitianSymmetrizeXY.argtypes = [sz, sz, sz, sz, sz, vp]
+    lib.create_complexAlign.restype = vp
+    lib.create_complexAlign.argtypes = [sz]
+    lib.delete_complexAlign.argtypes = [vp]
+    lib.create_doubleAlign.restype = vp
+    lib.create_doubleAlign.argtypes = [sz]
+    lib.delete_doubleAlign.argtypes = [vp]
+    lib.get_fftwpp_maxthreads.restype = sz
+    lib.set_fftwpp_maxthreads.argtypes = [sz]
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    return load().fgb_last_error().decode(errors="replace")
+
+
+def header_symbols() -> list[str]:
+    """Every function declared in include/*.h (for the export check)."""
+    import re
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    names = []
+    for fn in sorted(os.listdir(inc)):
+        if not fn.endswith(".h"):
+            continue
+        text = open(os.path.join(inc, fn)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"([A-Za-z_][A-Za-z_0-9]*)\s*\(", text):
+            name = m.group(1)
+            if name in ("if", "for", "while", "sizeof", "return", "defined"):
+                continue
+            if name.startswith(("fftwpp_", "fgb_", "create_", "delete_",
+                                "get_fftwpp", "set_fftwpp")):
+                names.append(name)
+    return sorted(set(names))

@@ -1,0 +1,447 @@
+// capi.cu -- C ABI of lib_fftwpp.so: the FFTW++-compatible entry points of
+// include/cfftw++.h and the device-pointer API of include/fftwpp_gb300.h.
+#include "engine.h"
+#include "kernels.cuh"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <vector>
+
+using namespace fgb;
+
+struct fgb_conv {
+  std::unique_ptr<Conv> conv;
+  cudaStream_t stream;
+};
+
+namespace {
+
+size_t maxthreads=1;
+
+// Host allocations handed out by create_*Align: page-locked when a GPU is
+// present, else posix_memalign; remembered so delete_* frees correctly.
+std::mutex allocMutex;
+std::map<void *,bool> allocPinned;
+
+void *alignedAlloc(size_t bytes)
+{
+  if(bytes == 0) bytes=16;
+  void *p=NULL;
+  bool pinned=cudaMallocHost(&p,bytes) == cudaSuccess;
+  if(!pinned) {
+    cudaGetLastError();
+    p=NULL;
+    if(posix_memalign(&p,64,bytes) != 0) return NULL;
+  }
+  std::lock_guard<std::mutex> lock(allocMutex);
+  allocPinned[p]=pinned;
+  return p;
+}
+
+void alignedFree(void *p)
+{
+  if(!p) return;
+  bool pinned=false;
+  {
+    std::lock_guard<std::mutex> lock(allocMutex);
+    auto it=allocPinned.find(p);
+    if(it == allocPinned.end()) return;
+    pinned=it->second;
+    allocPinned.erase(it);
+  }
+  if(pinned) cudaFreeHost(p);
+  else free(p);
+}
+
+void report(const char *where, const std::string& what)
+{
+  setLastError(what);
+  fprintf(stderr,"fftwpp_gb300: %s: %s\n",where,what.c_str());
+}
+
+fgb_conv *make(int dim, const int *kinds, const long *L, const long *M,
+               const long *m, int A, int B, int mult, int prec, long batch,
+               const char *where)
+{
+  try {
+    fgb_conv *c=new fgb_conv;
+    c->conv.reset(new Conv(dim,kinds,L,M,m,A,B,mult,prec,batch));
+    if(cudaStreamCreateWithFlags(&c->stream,cudaStreamNonBlocking) !=
+       cudaSuccess) {
+      cudaGetLastError();
+      delete c;
+      report(where,"cannot create a CUDA stream");
+      return NULL;
+    }
+    return c;
+  } catch(std::exception& e) {
+    report(where,e.what());
+    return NULL;
+  }
+}
+
+void destroy(fgb_conv *c)
+{
+  if(!c) return;
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int convolveHost(fgb_conv *c, void *a, void *b, const char *where)
+{
+  if(!c) {report(where,"null handle"); return -1;}
+  void *in[2]={a,b};
+  cudaError_t e=c->conv->runHost(in,in,c->stream);
+  if(e != cudaSuccess) {
+    report(where,cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
+long defaultM(int kind, long L)
+{
+  if(kind == KIND_CENTERED || kind == KIND_HERMITIAN)
+    return 3*(long) ceilquotient(L,2)-2*(L % 2);
+  return 2*L-1;
+}
+
+// Host restatement of HermitianSymmetrizeX/XY for interleaved complex data
+// (convolve.h:1175-1258); these prepare host inputs before a convolve call.
+void symX(size_t Hx, size_t Hy, size_t x0, double *f, size_t Sx)
+{
+  double *F=f+2*x0*Sx;
+  for(size_t i=1; i < Hx; ++i) {
+    F[-2*(long) (i*Sx)]=F[2*i*Sx];
+    F[-2*(long) (i*Sx)+1]=-F[2*i*Sx+1];
+  }
+  F[1]=0.0;
+  if(x0 == Hx)
+    for(size_t j=0; j < 2*Hy; ++j) f[j]=0.0;
+}
+
+void symXY(size_t Hx, size_t Hy, size_t Hz, size_t x0, size_t y0, double *f)
+{
+  size_t Ly=y0+Hy;
+  size_t Sy=Hz, Sx=Ly*Hz;
+  size_t origin=x0*Sx+y0*Sy;
+  double *F=f+2*origin;
+  for(size_t i=1; i < Hx; ++i) {
+    F[-2*(long) (i*Sx)]=F[2*i*Sx];
+    F[-2*(long) (i*Sx)+1]=-F[2*i*Sx+1];
+  }
+  F[1]=0.0;
+  for(long i=-(long) Hx+1; i < (long) Hx; ++i) {
+    long mm=(long) origin-i*(long) Sx;
+    long pp=(long) origin+i*(long) Sx;
+    for(size_t j=1; j < Hy; ++j) {
+      long dst=mm-(long) (j*Sy), src=pp+(long) (j*Sy);
+      f[2*dst]=f[2*src];
+      f[2*dst+1]=-f[2*src+1];
+    }
+  }
+  if(x0 == Hx)
+    for(size_t j=0; j < Ly; ++j)
+      for(size_t k=0; k < Hz; ++k) f[2*(Sy*j+k)]=f[2*(Sy*j+k)+1]=0.0;
+  if(y0 == Hy) {
+    size_t Lx=x0+Hx;
+    for(size_t i=0; i < Lx; ++i)
+      for(size_t k=0; k < Hz; ++k) f[2*(Sx*i+k)]=f[2*(Sx*i+k)+1]=0.0;
+  }
+}
+
+template<typename T>
+__global__ void symXKernel(size_t Hx, size_t Hy, size_t x0, cplx<T> *f)
+{
+  // One thread per mirrored row i; row 0 of the Nyquist case is zeroed by
+  // a separate grid-stride loop below.
+  size_t i=blockIdx.x*(size_t) blockDim.x+threadIdx.x;
+  cplx<T> *F=f+x0*Hy;
+  if(i >= 1 && i < Hx) {
+    cplx<T> v=F[i*Hy];
+    F[-(long) (i*Hy)]=mk(v.x,-v.y);
+  }
+  if(i == 0) F[0].y=(T) 0;
+}
+
+template<typename T>
+__global__ void zeroRowKernel(size_t n, cplx<T> *f)
+{
+  size_t i=blockIdx.x*(size_t) blockDim.x+threadIdx.x;
+  if(i < n) f[i]=mk((T) 0,(T) 0);
+}
+
+} // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// FFTW++-compatible ABI (wrappers/cfftw++.cc).
+
+double *create_doubleAlign(size_t n)
+{
+  return (double *) alignedAlloc(n*sizeof(double));
+}
+
+void delete_doubleAlign(double *p) {alignedFree(p);}
+
+void *create_complexAlign(size_t n)
+{
+  return alignedAlloc(n*2*sizeof(double));
+}
+
+void delete_complexAlign(void *p) {alignedFree(p);}
+
+size_t get_fftwpp_maxthreads(void) {return maxthreads;}
+void set_fftwpp_maxthreads(size_t n) {maxthreads=n;}
+
+void *fftwpp_create_conv1d(size_t L)
+{
+  int k[]={KIND_PAD};
+  long Ls[]={(long) L}, Ms[]={defaultM(KIND_PAD,L)};
+  return make(1,k,Ls,Ms,NULL,2,1,MULT_BINARY,PREC_F64,1,"fftwpp_create_conv1d");
+}
+void fftwpp_conv1d_delete(void *c) {destroy((fgb_conv *) c);}
+void fftwpp_conv1d_convolve(void *c, void *a, void *b)
+{
+  convolveHost((fgb_conv *) c,a,b,"fftwpp_conv1d_convolve");
+}
+
+void *fftwpp_create_hconv1d(size_t L)
+{
+  int k[]={KIND_HERMITIAN};
+  long Ls[]={(long) L}, Ms[]={defaultM(KIND_HERMITIAN,L)};
+  return make(1,k,Ls,Ms,NULL,2,1,MULT_REALBINARY,PREC_F64,1,
+              "fftwpp_create_hconv1d");
+}
+void fftwpp_hconv1d_delete(void *c) {destroy((fgb_conv *) c);}
+void fftwpp_HermitianSymmetrize(double *f) {f[1]=0.0;}
+void fftwpp_hconv1d_convolve(void *c, void *a, void *b)
+{
+  convolveHost((fgb_conv *) c,a,b,"fftwpp_hconv1d_convolve");
+}
+
+void *fftwpp_create_conv2d(size_t Lx, size_t Ly)
+{
+  int k[]={KIND_PAD,KIND_PAD};
+  long Ls[]={(long) Lx,(long) Ly};
+  long Ms[]={defaultM(KIND_PAD,Lx),defaultM(KIND_PAD,Ly)};
+  return make(2,k,Ls,Ms,NULL,2,1,MULT_BINARY,PREC_F64,1,"fftwpp_create_conv2d");
+}
+void fftwpp_conv2d_delete(void *c) {destroy((fgb_conv *) c);}
+void fftwpp_HermitianSymmetrizeX(size_t Hx, size_t Hy, size_t x0, double *f)
+{
+  symX(Hx,Hy,x0,f,Hy);
+}
+void fftwpp_conv2d_convolve(void *c, void *a, void *b)
+{
+  convolveHost((fgb_conv *) c,a,b,"fftwpp_conv2d_convolve");
+}
+
+void *fftwpp_create_hconv2d(size_t Lx, size_t Ly)
+{
+  int k[]={KIND_CENTERED,KIND_HERMITIAN};
+  long Ls[]={(long) Lx,(long) Ly};
+  long Ms[]={defaultM(KIND_CENTERED,Lx),defaultM(KIND_HERMITIAN,Ly)};
+  return make(2,k,Ls,Ms,NULL,2,1,MULT_REALBINARY,PREC_F64,1,
+              "fftwpp_create_hconv2d");
+}
+void fftwpp_hconv2d_delete(void *c) {destroy((fgb_conv *) c);}
+void fftwpp_hconv2d_convolve(void *c, void *a, void *b)
+{
+  convolveHost((fgb_conv *) c,a,b,"fftwpp_hconv2d_convolve");
+}
+
+void *fftwpp_create_conv3d(size_t Lx, size_t Ly, size_t Lz)
+{
+  int k[]={KIND_PAD,KIND_PAD,KIND_PAD};
+  long Ls[]={(long) Lx,(long) Ly,(long) Lz};
+  long Ms[]={defaultM(KIND_PAD,Lx),defaultM(KIND_PAD,Ly),defaultM(KIND_PAD,Lz)};
+  return make(3,k,Ls,Ms,NULL,2,1,MULT_BINARY,PREC_F64,1,"fftwpp_create_conv3d");
+}
+void fftwpp_conv3d_delete(void *c) {destroy((fgb_conv *) c);}
+void fftwpp_HermitianSymmetrizeXY(size_t Hx, size_t Hy, size_t Hz, size_t x0,
+                                  size_t y0, double *f)
+{
+  symXY(Hx,Hy,Hz,x0,y0,f);
+}
+void fftwpp_conv3d_convolve(void *c, void *a, void *b)
+{
+  convolveHost((fgb_conv *) c,a,b,"fftwpp_conv3d_convolve");
+}
+
+void *fftwpp_create_hconv3d(size_t Lx, size_t Ly, size_t Lz)
+{
+  int k[]={KIND_CENTERED,KIND_CENTERED,KIND_HERMITIAN};
+  long Ls[]={(long) Lx,(long) Ly,(long) Lz};
+  long Ms[]={defaultM(KIND_CENTERED,Lx),defaultM(KIND_CENTERED,Ly),
+             defaultM(KIND_HERMITIAN,Lz)};
+  return make(3,k,Ls,Ms,NULL,2,1,MULT_REALBINARY,PREC_F64,1,
+              "fftwpp_create_hconv3d");
+}
+void fftwpp_hconv3d_delete(void *c) {destroy((fgb_conv *) c);}
+void fftwpp_hconv3d_convolve(void *c, void *a, void *b)
+{
+  convolveHost((fgb_conv *) c,a,b,"fftwpp_hconv3d_convolve");
+}
+
+// ---------------------------------------------------------------------------
+// Device-pointer API (include/fftwpp_gb300.h).
+
+fgb_conv *fgb_create(int dim, const int *kinds, const size_t *L,
+                     const size_t *M, const size_t *m, int A, int B, int mult,
+                     int precision, size_t batch)
+{
+  if(dim < 1 || dim > 3 || !kinds || !L || !M) {
+    report("fgb_create","bad arguments");
+    return NULL;
+  }
+  long Ls[3], Ms[3], ms[3];
+  for(int d=0; d < dim; ++d) {
+    Ls[d]=(long) L[d];
+    Ms[d]=(long) M[d];
+    ms[d]=m ? (long) m[d] : 0;
+  }
+  return make(dim,kinds,Ls,Ms,ms,A,B,mult,precision,(long) batch,"fgb_create");
+}
+
+int fgb_convolve_device(fgb_conv *c, void *const *in, void *const *out,
+                        void *stream)
+{
+  if(!c || !in || !out) {report("fgb_convolve_device","bad arguments"); return -1;}
+  cudaError_t e=c->conv->run(in,out,(cudaStream_t) stream);
+  if(e != cudaSuccess) {
+    report("fgb_convolve_device",cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
+int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out)
+{
+  if(!c || !in || !out) {report("fgb_convolve_host","bad arguments"); return -1;}
+  cudaError_t e=c->conv->runHost(in,out,c->stream);
+  if(e != cudaSuccess) {
+    report("fgb_convolve_host",cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
+int fgb_info(const fgb_conv *c, long *info)
+{
+  if(!c || !info) return -1;
+  const ConvInfo& I=c->conv->info();
+  for(int k=0; k < 27; ++k) info[k]=0;
+  for(int d=0; d < I.dim; ++d) {
+    const AxisPlan& a=I.axis[d];
+    long *o=info+8*d;
+    o[0]=a.m; o[1]=a.p; o[2]=a.q; o[3]=a.N; o[4]=a.stored; o[5]=a.cshift;
+    o[6]=a.tile; o[7]=a.rows;
+  }
+  info[24]=c->conv->launches();
+  info[25]=(long) c->conv->stagingBytes();
+  info[26]=I.longRow ? 1 : 0;
+  return 0;
+}
+
+void fgb_destroy(fgb_conv *c) {destroy(c);}
+
+const char *fgb_last_error(void)
+{
+  static thread_local std::string s;
+  s=lastError();
+  return s.c_str();
+}
+
+void fgb_parameters(size_t L, size_t M, size_t m, int centered,
+                    size_t *p, size_t *n, size_t *q)
+{
+  refParameters(L,M,m,centered != 0,*p,*n,*q);
+}
+
+size_t fgb_nextfftsize(size_t m) {return nextfftsize(m);}
+
+// Transformed index (fftBase::index, convolve.h:297-326; fftPadReal::index,
+// convolve.h:956-979).  D0 = n mod D (or D), the remainder block of the
+// residue loop (convolve.cc:701-703); overwrite is not modelled.
+size_t fgb_index(int kind, size_t m, size_t p, size_t q, size_t n, size_t D,
+                 size_t r, size_t i)
+{
+  if(q == 1) return i;
+  if(kind == KIND_REAL) {
+    size_t s=i % m;
+    size_t P=p == 2 ? 1 : p;
+    r += i/(P*m);
+    if(p <= 2) {
+      if(r == 0) return q*i;
+      if(2*r == q) return q*m-(q*2*i+r);
+    } else {
+      size_t u=(i/m) % p;
+      if(r == 0) {
+        if(2*u == p) return q*m-(q*2*s+u*n);
+        return s == 0 ? u*n : q*m-(q*s-u*n);
+      } else if(2*r == n)
+        return q*m-(q*s+2*u*n+r);
+      else
+        return q*(m-s)-(u*n+r);
+    }
+    return q*(m-s)-r;
+  }
+  bool centered=kind == KIND_CENTERED || kind == KIND_HERMITIAN;
+  size_t D0=n % D;
+  if(D0 == 0) D0=D;
+  size_t P=(p+1)/2;
+  size_t s=i % m;
+  size_t u;
+  if(D > 1 && ((centered && p % 2 == 0) || p <= 2)) {
+    u=(i/m) % P;
+    size_t offset=r == 0 && i >= P*m && D0 % 2 == 1 ? 1 : 0;
+    size_t incr=(i+P*m*offset)/(2*P*m);
+    r += incr;
+    if(i/(P*m)-2*incr+offset == 1) {
+      if((!centered && p == 2) || (r > 0 && u == 0))
+        s=s > 0 ? s-1 : m-1;
+      if(r == 0)
+        r=n/2;
+      else {
+        r=n-r;
+        u=u > 0 ? u-1 : P-1;
+      }
+    }
+  } else {
+    u=(i/m) % p;
+    r += i/(p*m);
+  }
+  return q*s+n*u+r;
+}
+
+int fgb_hermitian_symmetrize_x_device(size_t Hx, size_t Hy, size_t x0,
+                                      void *f, int precision, void *stream)
+{
+  cudaStream_t s=(cudaStream_t) stream;
+  unsigned grid=(unsigned) ((Hx+255)/256);
+  if(precision == PREC_F64) {
+    symXKernel<double><<<grid,256,0,s>>>(Hx,Hy,x0,(cplx<double> *) f);
+    if(x0 == Hx)
+      zeroRowKernel<double><<<(unsigned) ((Hy+255)/256),256,0,s>>>(Hy,(cplx<double> *) f);
+  } else {
+    symXKernel<float><<<grid,256,0,s>>>(Hx,Hy,x0,(cplx<float> *) f);
+    if(x0 == Hx)
+      zeroRowKernel<float><<<(unsigned) ((Hy+255)/256),256,0,s>>>(Hy,(cplx<float> *) f);
+  }
+  cudaError_t e=cudaGetLastError();
+  if(e != cudaSuccess) {
+    report("fgb_hermitian_symmetrize_x_device",cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
+} // extern "C"

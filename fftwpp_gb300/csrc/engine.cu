@@ -1,0 +1,619 @@
+// engine.cu -- planning and launch sequences of the GB300 hybrid convolution.
+#include "engine.h"
+#include "kernels.cuh"
+
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <stdexcept>
+#include <tuple>
+
+namespace fgb {
+
+// ---------------------------------------------------------------------------
+// Integer rules (restated from convolve.cc:114-175 and :403-410).
+
+size_t ceilquotient(size_t a, size_t b) {return (a+b-1)/b;}
+
+static size_t ceilpow2(size_t n)
+{
+  size_t p=1;
+  while(p < n) p <<= 1;
+  return p;
+}
+
+static size_t ceilpow(size_t b, size_t n)
+{
+  size_t p=1;
+  while(p < n) p *= b;
+  return p;
+}
+
+size_t nextfftsize(size_t m)
+{
+  size_t N=ceilpow2(m);
+  if(m == N) return m;
+  for(size_t ni=1; ni < N; ni *= 7)
+    for(size_t nj=ni; nj < N; nj *= 5)
+      for(size_t nk=nj; nk < N; nk *= 3)
+        N=std::min(N,nk*ceilpow2(ceilquotient(m,nk)));
+  return N;
+}
+
+size_t nextpuresize(size_t m)
+{
+  size_t M=ceilpow2(m);
+  if(m == M) return m;
+  M=std::min(M,ceilpow(3,m));
+  if(m == M) return m;
+  M=std::min(M,ceilpow(5,m));
+  if(m == M) return m;
+  return std::min(M,ceilpow(7,m));
+}
+
+bool ispure(size_t m)
+{
+  return m == ceilpow(2,m) || m == ceilpow(3,m) || m == ceilpow(5,m) ||
+    m == ceilpow(7,m);
+}
+
+void refParameters(size_t L, size_t M, size_t m, bool centered,
+                   size_t& p, size_t& n, size_t& q)
+{
+  p=ceilquotient(L,m);
+  size_t P=(centered && p % 2 == 0) || p == 2 ? p/2 : p;
+  n=ceilquotient(M,P*m);
+  q=P*n;
+}
+
+bool smooth(size_t n)
+{
+  if(n == 0) return false;
+  for(size_t f : {2,3,5,7})
+    while(n % f == 0) n /= f;
+  return n == 1;
+}
+
+// ---------------------------------------------------------------------------
+// Errors.
+
+static thread_local std::string errorText;
+std::string lastError() {return errorText;}
+void setLastError(const std::string& s) {errorText=s;}
+
+// ---------------------------------------------------------------------------
+// Twiddle tables.
+
+const void *twiddles(long n, int prec)
+{
+  static std::mutex mu;
+  static std::map<std::tuple<int,long,int>,void *> cache;
+  int dev=0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  auto key=std::make_tuple(dev,n,prec);
+  auto it=cache.find(key);
+  if(it != cache.end()) return it->second;
+
+  // exp(2 pi i t/n) from the exact rational angle t/n, reduced to the
+  // first octant so that the long double evaluation stays accurate.
+  std::vector<double> c(n), s(n);
+  const long double pi=3.141592653589793238462643383279502884L;
+  for(long t=0; t < n; ++t) {
+    // angle = 2 pi t/n; fold by symmetry into [0, pi/4].
+    long tt=t;
+    long double sign_c=1, sign_s=1;
+    long u=tt;
+    // Use 8t vs n comparisons with exact integer arithmetic.
+    long double a;
+    bool swap=false;
+    if(2*u > n) {u=n-u; sign_s=-1;}                 // [0, pi]
+    if(4*u > n) {u=n-2*u; sign_c=-sign_c;           // pi - angle
+      // angle' = pi - angle = 2 pi (n/2 - u)/n  -> represent as 2*pi*u'/(2n)
+      a=pi*(long double) u/(long double) n;
+      // a in [0, pi/2)
+    } else
+      a=2*pi*(long double) u/(long double) n;
+    if(a > pi/4) {a=pi/2-a; swap=true;}
+    long double cv=cosl(a), sv=sinl(a);
+    if(swap) std::swap(cv,sv);
+    c[t]=(double) (sign_c*cv);
+    s[t]=(double) (sign_s*sv);
+  }
+  void *d=NULL;
+  if(prec == PREC_F64) {
+    std::vector<double2> h(n);
+    for(long t=0; t < n; ++t) h[t]=make_double2(c[t],s[t]);
+    if(cudaMalloc(&d,n*sizeof(double2)) != cudaSuccess) return NULL;
+    cudaMemcpy(d,h.data(),n*sizeof(double2),cudaMemcpyHostToDevice);
+  } else {
+    std::vector<float4> h(n);
+    for(long t=0; t < n; ++t) {
+      float hx=(float) c[t], hy=(float) s[t];
+      h[t]=make_float4(hx,hy,(float) (c[t]-(double) hx),
+                       (float) (s[t]-(double) hy));
+    }
+    if(cudaMalloc(&d,n*sizeof(float4)) != cudaSuccess) return NULL;
+    cudaMemcpy(d,h.data(),n*sizeof(float4),cudaMemcpyHostToDevice);
+  }
+  cache[key]=d;
+  return d;
+}
+
+static FFTPlanDev fftPlan(long n, int prec)
+{
+  if(!smooth(n))
+    throw std::runtime_error("transform length "+std::to_string(n)+
+                             " is not a product of 2, 3, 5 and 7");
+  FFTPlanDev p;
+  p.n=(int) n;
+  p.nst=0;
+  long r=n;
+  // Largest radices first: 8, then 4 or 2, then odd primes.
+  while(r % 8 == 0) {p.radix[p.nst++]=8; r /= 8;}
+  if(r % 4 == 0) {p.radix[p.nst++]=4; r /= 4;}
+  if(r % 2 == 0) {p.radix[p.nst++]=2; r /= 2;}
+  while(r % 7 == 0) {p.radix[p.nst++]=7; r /= 7;}
+  while(r % 5 == 0) {p.radix[p.nst++]=5; r /= 5;}
+  while(r % 3 == 0) {p.radix[p.nst++]=3; r /= 3;}
+  if(p.nst > FGB_MAXSTAGES)
+    throw std::runtime_error("too many FFT stages");
+  p.tw=twiddles(n,prec);
+  if(!p.tw) throw std::runtime_error("twiddle table allocation failed");
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// Planning.
+
+static const size_t SMEM_MAX=227*1024;
+
+static size_t elem(int prec) {return prec == PREC_F64 ? 16 : 8;}
+
+static size_t rowNeed(int prec, long L, long m, int A, int B)
+{
+  return prec == PREC_F64 ? rowSmem<double>(L,m,A,B) : rowSmem<float>(L,m,A,B);
+}
+
+static size_t hermNeed(int prec, long H, long Nh, int A)
+{
+  return prec == PREC_F64 ? hermRowSmem<double>(H,Nh,A) :
+    hermRowSmem<float>(H,Nh,A);
+}
+
+static size_t outerNeed(int prec, long L, long m, int tile)
+{
+  size_t f=prec == PREC_F64 ? outerFwdSmem<double>(m,tile) :
+    outerFwdSmem<float>(m,tile);
+  size_t b=prec == PREC_F64 ? outerBwdSmem<double>(L,m,tile) :
+    outerBwdSmem<float>(L,m,tile);
+  return std::max(f,b);
+}
+
+static double fftCost(long m) {return m*std::log2((double) std::max(m,2L));}
+
+// Inner (row) axis, complex data: residue block m and residue count q.
+static bool planRowComplex(AxisPlan& a, long mForce, int A, int B, int prec)
+{
+  bool centered=a.kind == KIND_CENTERED;
+  if(mForce > 0) {
+    size_t p,n,q;
+    refParameters(a.L,a.M,mForce,centered,p,n,q);
+    if(!smooth(mForce)) return false;
+    a.m=mForce; a.q=q;
+  } else {
+    double best=1e300;
+    long bm=0, bq=0;
+    for(long q=1; q <= 64; ++q) {
+      long m=nextfftsize(ceilquotient(a.M,q));
+      if(m*q < a.M) continue;
+      if(rowNeed(prec,a.L,m,A,B) > SMEM_MAX) continue;
+      long p=ceilquotient(a.L,m);
+      double cost=q*((A+B)*fftCost(m)+A*p*(double) m+(A+B)*(double) m);
+      if(cost < best) {best=cost; bm=m; bq=q;}
+    }
+    if(!bm) return false;
+    a.m=bm; a.q=bq;
+  }
+  a.N=a.m*a.q;
+  a.p=ceilquotient(a.L,a.m);
+  a.cshift=centered ? (int) (a.L/2) : 0;
+  return rowNeed(prec,a.L,a.m,A,B) <= SMEM_MAX;
+}
+
+static long evenSmooth(long M)
+{
+  long N=std::max(M,2L);
+  if(N % 2) ++N;
+  while(!smooth(N/2)) N += 2;
+  return N;
+}
+
+static bool planRowHermitian(AxisPlan& a, long mForce, int A, int prec)
+{
+  long M=a.M;
+  if(mForce > 0) {
+    size_t p,n,q;
+    refParameters(a.L,a.M,mForce,true,p,n,q);
+    M=std::max<long>(M,mForce*q);
+  }
+  a.N=evenSmooth(M);
+  a.m=a.N; a.q=1; a.p=1;
+  a.cshift=0;
+  return hermNeed(prec,a.stored,a.N/2,A) <= SMEM_MAX;
+}
+
+static void planOuter(AxisPlan& a, long mForce, int prec)
+{
+  int tile=prec == PREC_F64 ? 8 : 16;
+  if(a.kind == KIND_REAL) {
+    a.N=evenSmooth(mForce > 0 ? std::max(a.M,mForce) : a.M);
+    a.m=a.N; a.q=1; a.p=1; a.cshift=0;
+    a.rows=a.N/2+1;
+    long Nh=a.N/2;
+    while(tile > 1 && (prec == PREC_F64 ? outerRealSmem<double>(a.L,Nh,tile) :
+                       outerRealSmem<float>(a.L,Nh,tile)) > SMEM_MAX)
+      tile /= 2;
+    a.tile=tile;
+    return;
+  }
+  bool centered=a.kind == KIND_CENTERED;
+  if(mForce > 0) {
+    size_t p,n,q;
+    refParameters(a.L,a.M,mForce,centered,p,n,q);
+    if(!smooth(mForce))
+      throw std::runtime_error("forced m must be a product of 2,3,5,7");
+    a.m=mForce; a.q=q;
+  } else {
+    long N=nextfftsize(a.M);
+    double best=1e300;
+    long bm=0;
+    for(long m=1; m <= N; ++m) {
+      if(N % m || !smooth(m)) continue;
+      long q=N/m;
+      if(outerNeed(prec,a.L,m,1) > SMEM_MAX) continue;
+      long p=ceilquotient(a.L,m);
+      double cost=q*(fftCost(m)+p*(double) m)+fftCost(m)+0.25*a.L;
+      if(cost < best) {best=cost; bm=m;}
+    }
+    if(!bm) throw std::runtime_error("no outer padding plan fits");
+    a.m=bm; a.q=N/bm;
+  }
+  a.N=a.m*a.q;
+  a.p=ceilquotient(a.L,a.m);
+  a.cshift=centered ? (int) (a.L/2) : 0;
+  a.rows=a.N;
+  while(tile > 1 && outerNeed(prec,a.L,a.m,tile) > SMEM_MAX) tile /= 2;
+  if(outerNeed(prec,a.L,a.m,tile) > SMEM_MAX)
+    throw std::runtime_error("outer axis too long for shared memory");
+  a.tile=tile;
+}
+
+Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
+           const long *mForce, int A, int B, int mult, int prec, long batch)
+  : batch(batch), staging(0), hostIn(NULL), hostOut(NULL), nlaunch(0)
+{
+  if(dim < 1 || dim > 3) throw std::runtime_error("dimension must be 1, 2 or 3");
+  if(A < 1 || A > FGB_MAXA || B < 1 || B > A)
+    throw std::runtime_error("need 1 <= B <= A <= 8");
+  if(prec != PREC_F64 && prec != PREC_F32)
+    throw std::runtime_error("unknown precision");
+  if(batch < 1) throw std::runtime_error("batch must be positive");
+  I.dim=dim; I.A=A; I.B=B; I.mult=mult; I.prec=prec;
+  I.longRow=false; I.rowM=I.rowQ=0;
+  for(int d=0; d < dim; ++d) {
+    AxisPlan& a=I.axis[d];
+    a.kind=kinds[d];
+    a.L=L[d];
+    a.M=M[d];
+    if(a.kind < 0 || a.kind > 3) throw std::runtime_error("unknown axis kind");
+    if(a.L < 1) throw std::runtime_error("L must be positive");
+    if(a.L > a.M)
+      throw std::runtime_error("L="+std::to_string(a.L)+" is greater than M="+
+                               std::to_string(a.M));
+    if(a.kind == KIND_HERMITIAN && d != dim-1)
+      throw std::runtime_error("a Hermitian axis must be the innermost");
+    if(a.kind == KIND_REAL && d != 0)
+      throw std::runtime_error("a real axis must be the outermost");
+    a.stored=a.kind == KIND_HERMITIAN ? (long) ceilquotient(a.L,2) : a.L;
+    a.tile=1;
+    a.rows=0;
+  }
+  if(dim > 1 && batch != 1)
+    throw std::runtime_error("batched problems are one-dimensional");
+
+  for(int d=0; d < dim-1; ++d) planOuter(I.axis[d],mForce ? mForce[d] : 0,prec);
+  AxisPlan& in=I.axis[dim-1];
+  long mf=mForce ? mForce[dim-1] : 0;
+  bool ok;
+  if(in.kind == KIND_HERMITIAN) ok=planRowHermitian(in,mf,A,prec);
+  else ok=planRowComplex(in,mf,A,B,prec);
+  if(in.kind == KIND_REAL && dim == 1) in.rows=0;
+  if(!ok) {
+    if(dim != 1 || in.kind != KIND_PAD)
+      throw std::runtime_error("row too long for one CTA (only 1D complex "
+                               "fftPad data takes the long path)");
+    // Long 1D: N = rowM * rowQ; columns of length rowQ (outer, explicit,
+    // with the W_N^{t r} twiddle), rows of length rowM (unpadded).
+    long N=nextfftsize(in.M);
+    long best=0;
+    for(long m=1; m <= N; ++m)
+      if(N % m == 0 && smooth(m) && rowNeed(prec,m,m,A,B) <= SMEM_MAX / 2)
+        best=m;
+    if(!best) throw std::runtime_error("no long-row plan");
+    I.longRow=true;
+    I.rowM=best;
+    I.rowQ=N/best;
+    in.N=N; in.m=best; in.q=N/best; in.p=ceilquotient(in.L,best);
+    in.cshift=0;
+    int tile=prec == PREC_F64 ? 8 : 16;
+    while(tile > 1 && outerNeed(prec,in.p,I.rowQ,tile) > SMEM_MAX) tile /= 2;
+    in.tile=tile;
+    if(mForce && mForce[0] > 0)
+      throw std::runtime_error("forced m not supported on the long path");
+  }
+  allocate();
+}
+
+Conv::~Conv()
+{
+  for(void *p : bufs) cudaFree(p);
+  if(hostIn) cudaFree(hostIn);
+  if(hostOut) cudaFree(hostOut);
+}
+
+size_t Conv::elemBytes() const
+{
+  if(I.axis[0].kind == KIND_REAL) return elem(I.prec)/2;
+  return elem(I.prec);
+}
+
+size_t Conv::elements() const
+{
+  size_t n=batch;
+  for(int d=0; d < I.dim; ++d) n *= I.axis[d].stored;
+  return n;
+}
+
+void Conv::allocate()
+{
+  size_t e=elem(I.prec);
+  int A=I.A;
+  auto get=[&](size_t bytes) {
+    void *p=NULL;
+    if(cudaMalloc(&p,bytes) != cudaSuccess)
+      throw std::runtime_error("device allocation of "+std::to_string(bytes)+
+                               " bytes failed");
+    bufs.push_back(p);
+    staging += bytes;
+  };
+  if(I.dim == 1) {
+    if(I.longRow) for(int a=0; a < A; ++a) get(e*(size_t) I.axis[0].N);
+    nlaunch=I.longRow ? 3 : 1;
+  } else if(I.dim == 2) {
+    size_t rows=I.axis[0].rows;
+    size_t C=I.axis[1].stored;
+    for(int a=0; a < A; ++a) get(e*rows*C);
+    nlaunch=3;
+  } else {
+    size_t rx=I.axis[0].rows, ry=I.axis[1].rows;
+    size_t Ly=I.axis[1].L, nz=I.axis[2].stored;
+    for(int a=0; a < A; ++a) get(e*rx*Ly*nz);
+    for(int a=0; a < A; ++a) get(e*rx*ry*nz);
+    nlaunch=5;
+  }
+}
+
+int Conv::launches() const {return nlaunch;}
+
+// ---------------------------------------------------------------------------
+// Launch sequences.
+
+template<typename T>
+cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
+{
+  typedef cplx<T> Cx;
+  const int A=I.A, B=I.B;
+  const int threads=256;
+  cudaError_t e;
+  double scale=1.0;
+  for(int d=0; d < I.dim; ++d) scale /= (double) I.axis[d].N;
+
+  auto rowPlan=[&](RowPlan<T>& P, const AxisPlan& a) {
+    P.L=(int) a.stored; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
+    P.cshift=a.cshift; P.A=A; P.B=B; P.mult=I.mult;
+    P.realIO=a.kind == KIND_REAL && I.dim == 1;
+    P.fp=fftPlan(a.m,I.prec);
+    P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
+  };
+  auto hermPlan=[&](HermRowPlan<T>& P, const AxisPlan& a) {
+    P.H=(int) a.stored; P.N=(int) a.N; P.Nh=(int) (a.N/2);
+    P.A=A; P.B=B; P.mult=I.mult;
+    P.fp=fftPlan(a.N/2,I.prec);
+    P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
+  };
+  auto outerPlan=[&](OuterPlan<T>& P, const AxisPlan& a) {
+    P.L=(int) a.L; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
+    P.cshift=a.cshift; P.tile=a.tile;
+    P.fp=fftPlan(a.kind == KIND_REAL ? a.N/2 : a.m,I.prec);
+    P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
+    P.twX=NULL; P.NX=1;
+  };
+
+  if(I.dim == 1 && !I.longRow) {
+    const AxisPlan& a=I.axis[0];
+    if(a.kind == KIND_HERMITIAN) {
+      HermRowPlan<T> P;
+      hermPlan(P,a);
+      for(int i=0; i < A; ++i) P.in[i]=(const Cx *) in[i];
+      for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
+      P.rowStride=a.stored; P.nrows=batch; P.scale=(T) scale;
+      return launchHermRow<T>(P,threads,batch,s);
+    }
+    RowPlan<T> P;
+    rowPlan(P,a);
+    for(int i=0; i < A; ++i) P.in[i]=(const Cx *) in[i];
+    for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
+    P.rowStride=a.stored; P.nrows=batch; P.scale=(T) scale;
+    return launchRow<T>(P,threads,batch,s);
+  }
+
+  if(I.dim == 1) {  // long 1D complex
+    const AxisPlan& a=I.axis[0];
+    long m=I.rowM, q=I.rowQ;
+    OuterPlan<T> O;
+    O.L=(int) a.p; O.m=(int) q; O.q=1; O.N=(int) q; O.cshift=0;
+    O.tile=a.tile;
+    O.fp=fftPlan(q,I.prec);
+    O.twN=(const typename TwT<T>::type *) twiddles(q,I.prec);
+    O.twX=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
+    O.NX=a.N;
+    O.count=A; O.nbatch=1; O.inBatch=O.outBatch=0;
+    O.inRow=m; O.outRow=m; O.C=(int) m; O.Ltot=a.L;
+    O.scale=(T) 1;
+    for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) bufs[i];}
+    e=launchOuterFwd<T>(O,threads,s);
+    if(e != cudaSuccess) return e;
+    AxisPlan ra=a;
+    ra.stored=m; ra.L=m; ra.m=m; ra.q=1; ra.N=m; ra.cshift=0;
+    RowPlan<T> P;
+    rowPlan(P,ra);
+    for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
+    for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
+    P.rowStride=m; P.nrows=q; P.scale=(T) 1;
+    e=launchRow<T>(P,threads,q,s);
+    if(e != cudaSuccess) return e;
+    O.count=B;
+    O.Ltot=a.L;
+    O.scale=(T) scale;
+    for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) bufs[i]; O.out[i]=(Cx *) out[i];}
+    return launchOuterBwd<T>(O,threads,s);
+  }
+
+  if(I.dim == 2) {
+    const AxisPlan& ax=I.axis[0];
+    const AxisPlan& ay=I.axis[1];
+    long C=ay.stored;
+    OuterPlan<T> O;
+    outerPlan(O,ax);
+    O.count=A; O.nbatch=1; O.inBatch=O.outBatch=0;
+    O.inRow=C; O.outRow=C; O.C=(int) C; O.Ltot=(long long) ax.L*C;
+    O.scale=(T) 1;
+    for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) bufs[i];}
+    e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(O,threads,s) :
+      launchOuterFwd<T>(O,threads,s);
+    if(e != cudaSuccess) return e;
+    if(ay.kind == KIND_HERMITIAN) {
+      HermRowPlan<T> P;
+      hermPlan(P,ay);
+      for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
+      for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
+      P.rowStride=C; P.nrows=ax.rows; P.scale=(T) 1;
+      e=launchHermRow<T>(P,threads,ax.rows,s);
+    } else {
+      RowPlan<T> P;
+      rowPlan(P,ay);
+      for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
+      for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
+      P.rowStride=C; P.nrows=ax.rows; P.scale=(T) 1;
+      e=launchRow<T>(P,threads,ax.rows,s);
+    }
+    if(e != cudaSuccess) return e;
+    O.count=B;
+    O.scale=(T) scale;
+    for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) bufs[i]; O.out[i]=(Cx *) out[i];}
+    return ax.kind == KIND_REAL ? launchOuterRealBwd<T>(O,threads,s) :
+      launchOuterBwd<T>(O,threads,s);
+  }
+
+  // dim == 3
+  const AxisPlan& ax=I.axis[0];
+  const AxisPlan& ay=I.axis[1];
+  const AxisPlan& az=I.axis[2];
+  long nz=az.stored;
+  long Cx_=ay.L*nz;
+  void **bx=bufs.data();
+  void **by=bufs.data()+A;
+
+  OuterPlan<T> X;
+  outerPlan(X,ax);
+  X.count=A; X.nbatch=1; X.inBatch=X.outBatch=0;
+  X.inRow=Cx_; X.outRow=Cx_; X.C=(int) Cx_; X.Ltot=(long long) ax.L*Cx_;
+  X.scale=(T) 1;
+  for(int i=0; i < A; ++i) {X.in[i]=(const Cx *) in[i]; X.out[i]=(Cx *) bx[i];}
+  e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(X,threads,s) :
+    launchOuterFwd<T>(X,threads,s);
+  if(e != cudaSuccess) return e;
+
+  OuterPlan<T> Y;
+  outerPlan(Y,ay);
+  Y.count=A; Y.nbatch=(int) ax.rows;
+  Y.inBatch=ay.L*nz; Y.outBatch=ay.rows*nz;
+  Y.inRow=nz; Y.outRow=nz; Y.C=(int) nz; Y.Ltot=(long long) ay.L*nz;
+  Y.scale=(T) 1;
+  for(int i=0; i < A; ++i) {Y.in[i]=(const Cx *) bx[i]; Y.out[i]=(Cx *) by[i];}
+  e=launchOuterFwd<T>(Y,threads,s);
+  if(e != cudaSuccess) return e;
+
+  long nrows=ax.rows*ay.rows;
+  if(az.kind == KIND_HERMITIAN) {
+    HermRowPlan<T> P;
+    hermPlan(P,az);
+    for(int i=0; i < A; ++i) P.in[i]=(const Cx *) by[i];
+    for(int i=0; i < B; ++i) P.out[i]=(Cx *) by[i];
+    P.rowStride=nz; P.nrows=nrows; P.scale=(T) 1;
+    e=launchHermRow<T>(P,threads,nrows,s);
+  } else {
+    RowPlan<T> P;
+    rowPlan(P,az);
+    for(int i=0; i < A; ++i) P.in[i]=(const Cx *) by[i];
+    for(int i=0; i < B; ++i) P.out[i]=(Cx *) by[i];
+    P.rowStride=nz; P.nrows=nrows; P.scale=(T) 1;
+    e=launchRow<T>(P,threads,nrows,s);
+  }
+  if(e != cudaSuccess) return e;
+
+  Y.count=B;
+  for(int i=0; i < B; ++i) {Y.in[i]=(const Cx *) by[i]; Y.out[i]=(Cx *) bx[i];}
+  std::swap(Y.inBatch,Y.outBatch);
+  e=launchOuterBwd<T>(Y,threads,s);
+  if(e != cudaSuccess) return e;
+
+  X.count=B;
+  X.scale=(T) scale;
+  for(int i=0; i < B; ++i) {X.in[i]=(const Cx *) bx[i]; X.out[i]=(Cx *) out[i];}
+  return ax.kind == KIND_REAL ? launchOuterRealBwd<T>(X,threads,s) :
+    launchOuterBwd<T>(X,threads,s);
+}
+
+cudaError_t Conv::run(const void *const *in, void *const *out, cudaStream_t s)
+{
+  if(I.prec == PREC_F64) return runT<double>(in,out,s);
+  return runT<float>(in,out,s);
+}
+
+cudaError_t Conv::runHost(const void *const *in, void *const *out,
+                          cudaStream_t s)
+{
+  size_t bytes=elements()*elemBytes();
+  int A=I.A, B=I.B;
+  if(!hostIn) {
+    if(cudaMalloc(&hostIn,bytes*A) != cudaSuccess) return cudaErrorMemoryAllocation;
+  }
+  std::vector<void *> din(A), dout(B);
+  for(int a=0; a < A; ++a) {
+    din[a]=(char *) hostIn+a*bytes;
+    cudaError_t e=cudaMemcpyAsync(din[a],in[a],bytes,cudaMemcpyHostToDevice,s);
+    if(e != cudaSuccess) return e;
+  }
+  for(int b=0; b < B; ++b) dout[b]=din[b];
+  cudaError_t e=run(din.data(),dout.data(),s);
+  if(e != cudaSuccess) return e;
+  for(int b=0; b < B; ++b) {
+    e=cudaMemcpyAsync(out[b],dout[b],bytes,cudaMemcpyDeviceToHost,s);
+    if(e != cudaSuccess) return e;
+  }
+  return cudaStreamSynchronize(s);
+}
+
+} // namespace fgb

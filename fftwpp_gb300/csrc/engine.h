@@ -1,0 +1,90 @@
+// engine.h -- host side of the GB300 hybrid dealiased convolution.
+//
+// A Conv object is the GPU counterpart of a chain of FFTW++ padded
+// transforms plus a Convolution/Convolution2/Convolution3 driver
+// (convolve.h:982-1893): it owns the per-axis padding plans, the device
+// twiddle tables and the HBM staging buffers of the outer axes, and launches
+// the kernel sequence on a caller-supplied stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+namespace fgb {
+
+enum AxisKind {KIND_PAD=0, KIND_CENTERED=1, KIND_HERMITIAN=2, KIND_REAL=3};
+enum Precision {PREC_F64=0, PREC_F32=1};
+
+// Integer rules shared with the reference (convolve.cc:114-175, 403-410).
+size_t ceilquotient(size_t a, size_t b);
+size_t nextfftsize(size_t m);
+size_t nextpuresize(size_t m);
+bool ispure(size_t m);
+void refParameters(size_t L, size_t M, size_t m, bool centered,
+                   size_t& p, size_t& n, size_t& q);
+bool smooth(size_t n);   // n = 2^a 3^b 5^c 7^d
+
+struct AxisPlan {
+  int kind;
+  long L, M;          // data length, minimum padded length
+  long stored;        // values stored along the axis (ceil(L/2) if Hermitian)
+  long m, q, N, p;    // residue block length, residues, padded length, folds
+  int cshift;         // centred origin offset
+  int tile;           // outer kernels: columns per CTA
+  long rows;          // outer axis: rows produced (N, or N/2+1 if real)
+};
+
+struct ConvInfo {
+  int dim;
+  int A, B, mult, prec;
+  AxisPlan axis[3];
+  bool longRow;       // 1D data too long for one CTA: outer/row/outer path
+  long rowM, rowQ;    // long path: row length and column DFT length
+};
+
+class Conv {
+public:
+  // kinds/L/M/mForce: per dimension, outermost first.  mForce[d] = 0 lets
+  // the planner choose.  Throws std::runtime_error on invalid input.
+  Conv(int dim, const int *kinds, const long *L, const long *M,
+       const long *mForce, int A, int B, int mult, int prec, long batch=1);
+  ~Conv();
+
+  // Device pointers: A inputs, B outputs (outputs may alias inputs), each a
+  // dense row-major array in the stored layout; `batch` independent
+  // problems back to back in every array.
+  cudaError_t run(const void *const *in, void *const *out, cudaStream_t s);
+
+  // Host pointers: copy in, run, copy out (synchronous on s).
+  cudaError_t runHost(const void *const *in, void *const *out,
+                      cudaStream_t s);
+
+  const ConvInfo& info() const {return I;}
+  size_t elemBytes() const;        // bytes per stored element
+  size_t elements() const;         // stored elements per array (x batch)
+  int launches() const;            // kernels launched per run()
+  size_t stagingBytes() const {return staging;}
+
+private:
+  ConvInfo I;
+  long batch;
+  std::vector<void *> bufs;        // device staging buffers
+  size_t staging;
+  void *hostIn, *hostOut;          // device copies for runHost
+  int nlaunch;
+  template<typename T> cudaError_t runT(const void *const *in,
+                                        void *const *out, cudaStream_t s);
+  void allocate();
+};
+
+// Twiddle table W_n^t = exp(2 pi i t/n), t < n, on the current device,
+// cached for the life of the process.  prec selects double2 or the float4
+// (hi, lo) split.
+const void *twiddles(long n, int prec);
+
+std::string lastError();
+void setLastError(const std::string& s);
+
+} // namespace fgb

@@ -1,0 +1,206 @@
+// fft_smem.cuh -- shared-memory staged Stockham FFT with register radix
+// codelets (radix 2, 3, 4, 5, 7, 8), for the GB300 engine.
+//
+// A transform of length n = prod(radix[s]) runs on `ncol` interleaved
+// columns held in shared memory: element i of column c lives at x[i*ld+c].
+// Stage s (radix R, Ns = product of earlier radices) maps, for every
+// butterfly j < n/R and column c,
+//     a_r = x[j + r n/R] * W_{Ns R}^{S r (j mod Ns)}            (r < R)
+//     y[(j - j mod Ns) R + (j mod Ns) + r Ns] = DFT_R^S(a)_r
+// which is the self-sorting Stockham formulation: the output of the last
+// stage is in natural order, and every stage reads and writes with unit
+// column stride so neighbouring threads touch neighbouring words.
+// Twiddles W_n^t = exp(2 pi i t/n), t < n, come from one precomputed table
+// of the transform length (generated on the host in long double); the
+// stage twiddle W_{Ns R}^{rk} is table entry r*k*n/(Ns R).
+//
+// DFT sign convention: S = +1 computes sum_j x_j exp(+2 pi i jk/n), the sign
+// FFTW++ uses for its forward padded transforms; S = -1 the inverse (both
+// unnormalised).
+#pragma once
+
+#include "complex.cuh"
+
+namespace fgb {
+
+#define FGB_MAXSTAGES 20
+
+struct FFTPlanDev {
+  int n;
+  int nst;
+  int radix[FGB_MAXSTAGES];
+  const void *tw;         // TwT<T>::type[n]
+};
+
+// Radix constants (exact decimal expansions of the algebraic values).
+#define FGB_SQRT1_2 0.707106781186547524400844362105
+#define FGB_SQRT3_2 0.866025403784438646763723170753
+#define FGB_C51 0.309016994374947424102293417183
+#define FGB_S51 0.951056516295153572116439333379
+#define FGB_C52 -0.809016994374947424102293417183
+#define FGB_S52 0.587785252292473129168705954639
+#define FGB_C71 0.623489801858733530525004884004
+#define FGB_S71 0.781831482468029808708444526674
+#define FGB_C72 -0.222520933956314404288902564497
+#define FGB_S72 0.974927912181823607018131682994
+#define FGB_C73 -0.900968867902419126236102319507
+#define FGB_S73 0.433883739117558120475768332849
+
+template<int R, int S, typename T> struct Codelet;
+
+template<int S, typename T> struct Codelet<2,S,T> {
+  static __device__ __forceinline__ void run(cplx<T> *a) {
+    cplx<T> t=a[0];
+    a[0]=t+a[1];
+    a[1]=t-a[1];
+  }
+};
+
+template<int S, typename T> struct Codelet<4,S,T> {
+  static __device__ __forceinline__ void run(cplx<T> *a) {
+    cplx<T> s02=a[0]+a[2], d02=a[0]-a[2];
+    cplx<T> s13=a[1]+a[3], d13=mulI<S>(a[1]-a[3]);
+    a[0]=s02+s13;
+    a[2]=s02-s13;
+    a[1]=d02+d13;
+    a[3]=d02-d13;
+  }
+};
+
+template<int S, typename T> struct Codelet<8,S,T> {
+  static __device__ __forceinline__ void run(cplx<T> *a) {
+    const T h=(T) FGB_SQRT1_2;
+    cplx<T> e[4]={a[0],a[2],a[4],a[6]};
+    cplx<T> o[4]={a[1],a[3],a[5],a[7]};
+    Codelet<4,S,T>::run(e);
+    Codelet<4,S,T>::run(o);
+    // o[k] *= W_8^{S k}
+    cplx<T> o1=o[1], o3=o[3];
+    o[1]=mk((o1.x-(T) S*o1.y)*h,(o1.y+(T) S*o1.x)*h);          // (1+Si)/sqrt2
+    o[2]=mulI<S>(o[2]);
+    o[3]=mk((-o3.x-(T) S*o3.y)*h,(-o3.y+(T) S*o3.x)*h);        // (-1+Si)/sqrt2
+#pragma unroll
+    for(int k=0; k < 4; ++k) {
+      a[k]=e[k]+o[k];
+      a[k+4]=e[k]-o[k];
+    }
+  }
+};
+
+template<int S, typename T> struct Codelet<3,S,T> {
+  static __device__ __forceinline__ void run(cplx<T> *a) {
+    const T c=(T) -0.5;
+    const T s=(T) S*(T) FGB_SQRT3_2;
+    cplx<T> t=a[1]+a[2];
+    cplx<T> d=a[1]-a[2];
+    cplx<T> b=mk(fma(c,t.x,a[0].x),fma(c,t.y,a[0].y));
+    cplx<T> r=mk(-s*d.y,s*d.x);                                 // i*s*d
+    a[0]=a[0]+t;
+    a[1]=b+r;
+    a[2]=b-r;
+  }
+};
+
+template<int S, typename T> struct Codelet<5,S,T> {
+  static __device__ __forceinline__ void run(cplx<T> *a) {
+    const T c1=(T) FGB_C51, c2=(T) FGB_C52;
+    const T s1=(T) S*(T) FGB_S51, s2=(T) S*(T) FGB_S52;
+    cplx<T> t1=a[1]+a[4], d1=a[1]-a[4];
+    cplx<T> t2=a[2]+a[3], d2=a[2]-a[3];
+    cplx<T> x0=a[0];
+    cplx<T> b1=mk(fma(c1,t1.x,fma(c2,t2.x,x0.x)),fma(c1,t1.y,fma(c2,t2.y,x0.y)));
+    cplx<T> b2=mk(fma(c2,t1.x,fma(c1,t2.x,x0.x)),fma(c2,t1.y,fma(c1,t2.y,x0.y)));
+    // i*(s1 d1 + s2 d2) and i*(s2 d1 - s1 d2)
+    cplx<T> e1=mk(fma(s1,d1.x,s2*d2.x),fma(s1,d1.y,s2*d2.y));
+    cplx<T> e2=mk(fma(s2,d1.x,-s1*d2.x),fma(s2,d1.y,-s1*d2.y));
+    cplx<T> i1=mk(-e1.y,e1.x), i2=mk(-e2.y,e2.x);
+    a[0]=x0+t1+t2;
+    a[1]=b1+i1;
+    a[4]=b1-i1;
+    a[2]=b2+i2;
+    a[3]=b2-i2;
+  }
+};
+
+template<int S, typename T> struct Codelet<7,S,T> {
+  static __device__ __forceinline__ void run(cplx<T> *a) {
+    const T C1=(T) FGB_C71, C2=(T) FGB_C72, C3=(T) FGB_C73;
+    const T S1=(T) S*(T) FGB_S71, S2=(T) S*(T) FGB_S72, S3=(T) S*(T) FGB_S73;
+    cplx<T> t1=a[1]+a[6], d1=a[1]-a[6];
+    cplx<T> t2=a[2]+a[5], d2=a[2]-a[5];
+    cplx<T> t3=a[3]+a[4], d3=a[3]-a[4];
+    cplx<T> x0=a[0];
+    // cos(2 pi jk/7), sin(2 pi jk/7) for j=1,2,3 and k=1,2,3:
+    // j=1: (C1,C2,C3), (S1,S2,S3); j=2: (C2,C3,C1), (S2,-S3,-S1);
+    // j=3: (C3,C1,C2), (S3,-S1,S2).
+    cplx<T> b1=mk(x0.x+C1*t1.x+C2*t2.x+C3*t3.x,x0.y+C1*t1.y+C2*t2.y+C3*t3.y);
+    cplx<T> b2=mk(x0.x+C2*t1.x+C3*t2.x+C1*t3.x,x0.y+C2*t1.y+C3*t2.y+C1*t3.y);
+    cplx<T> b3=mk(x0.x+C3*t1.x+C1*t2.x+C2*t3.x,x0.y+C3*t1.y+C1*t2.y+C2*t3.y);
+    cplx<T> e1=mk(S1*d1.x+S2*d2.x+S3*d3.x,S1*d1.y+S2*d2.y+S3*d3.y);
+    cplx<T> e2=mk(S2*d1.x-S3*d2.x-S1*d3.x,S2*d1.y-S3*d2.y-S1*d3.y);
+    cplx<T> e3=mk(S3*d1.x-S1*d2.x+S2*d3.x,S3*d1.y-S1*d2.y+S2*d3.y);
+    a[0]=x0+t1+t2+t3;
+    cplx<T> i1=mk(-e1.y,e1.x), i2=mk(-e2.y,e2.x), i3=mk(-e3.y,e3.x);
+    a[1]=b1+i1; a[6]=b1-i1;
+    a[2]=b2+i2; a[5]=b2-i2;
+    a[3]=b3+i3; a[4]=b3-i3;
+  }
+};
+
+template<typename T, int R, int S>
+__device__ __forceinline__ void fftStage(const cplx<T> *__restrict__ x,
+                                         cplx<T> *__restrict__ y,
+                                         int n, int Ns, int ncol, int ld,
+                                         const typename TwT<T>::type *__restrict__ tw,
+                                         int tid, int nthr)
+{
+  const int nR=n/R;
+  const int tstride=n/(Ns*R);
+  const int total=nR*ncol;
+  for(int idx=tid; idx < total; idx += nthr) {
+    int j=idx/ncol;
+    int c=idx-j*ncol;
+    int k=j % Ns;
+    cplx<T> a[R];
+#pragma unroll
+    for(int r=0; r < R; ++r) a[r]=x[(j+r*nR)*ld+c];
+    if(k != 0) {
+#pragma unroll
+      for(int r=1; r < R; ++r) a[r]=twmul<S>(a[r],tw[r*k*tstride]);
+    }
+    Codelet<R,S,T>::run(a);
+    int base=(j-k)*R+k;
+#pragma unroll
+    for(int r=0; r < R; ++r) y[(base+r*Ns)*ld+c]=a[r];
+  }
+}
+
+// Transform ncol columns (stride ld) of x in place through the ping-pong
+// buffer y.  Every thread of the block must call it; the caller has
+// synchronised after filling x.  Returns the buffer holding the result
+// (x or y) and leaves the block synchronised.
+template<typename T, int S>
+__device__ cplx<T> *fftSmem(cplx<T> *x, cplx<T> *y, const FFTPlanDev& p,
+                            int ncol, int ld, int tid, int nthr)
+{
+  const typename TwT<T>::type *tw=(const typename TwT<T>::type *) p.tw;
+  int Ns=1;
+  for(int s=0; s < p.nst; ++s) {
+    int R=p.radix[s];
+    switch(R) {
+      case 8: fftStage<T,8,S>(x,y,p.n,Ns,ncol,ld,tw,tid,nthr); break;
+      case 4: fftStage<T,4,S>(x,y,p.n,Ns,ncol,ld,tw,tid,nthr); break;
+      case 2: fftStage<T,2,S>(x,y,p.n,Ns,ncol,ld,tw,tid,nthr); break;
+      case 3: fftStage<T,3,S>(x,y,p.n,Ns,ncol,ld,tw,tid,nthr); break;
+      case 5: fftStage<T,5,S>(x,y,p.n,Ns,ncol,ld,tw,tid,nthr); break;
+      case 7: fftStage<T,7,S>(x,y,p.n,Ns,ncol,ld,tw,tid,nthr); break;
+      default: break;
+    }
+    __syncthreads();
+    cplx<T> *t=x; x=y; y=t;
+    Ns *= R;
+  }
+  return x;
+}
+
+} // namespace fgb

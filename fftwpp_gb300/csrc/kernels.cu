@@ -1,0 +1,534 @@
+// kernels.cu -- GB300 (sm_103a) kernels of the hybrid dealiased convolution.
+// See kernels.cuh for the decomposition; reference routines are cited per
+// kernel.
+#include "kernels.cuh"
+
+namespace fgb {
+
+// ---------------------------------------------------------------------------
+// Multipliers (convolve.cc:26-110 and the 2D advection Jacobian), applied to
+// the A values X[0..A-1] of one transformed slot; results overwrite
+// X[0..B-1].  "Real" multipliers act lane-wise on the two doubles of a slot,
+// which is how the reference applies them to its double-valued buffers
+// (realMultBinary, convolve.cc:60-83).
+template<typename T>
+__device__ __forceinline__ void applyMult(int kind, cplx<T> *X, int A)
+{
+  switch(kind) {
+    case MULT_BINARY:
+      X[0]=cmul(X[0],X[1]);
+      break;
+    case MULT_REALBINARY:
+      X[0]=mk(X[0].x*X[1].x,X[0].y*X[1].y);
+      break;
+    case MULT_CORRELATION:
+      X[0]=cmulconj(X[0],X[1]);
+      break;
+    case MULT_REALJACOBIAN:
+      X[0]=mk(fma(X[0].x,X[3].x,-X[1].x*X[2].x),
+              fma(X[0].y,X[3].y,-X[1].y*X[2].y));
+      break;
+    case MULT_JACOBIAN:
+      X[0]=cmul(X[0],X[3])-cmul(X[1],X[2]);
+      break;
+    case MULT_REALJACADJ: {
+      // Inputs u0..u3 and the back-propagated field g; outputs the four
+      // lane-wise partial products dJ/du_i * g of J = u0 u3 - u1 u2.
+      cplx<T> g=X[4];
+      cplx<T> u0=X[0], u1=X[1], u2=X[2], u3=X[3];
+      X[0]=mk(g.x*u3.x,g.y*u3.y);
+      X[1]=mk(-g.x*u2.x,-g.y*u2.y);
+      X[2]=mk(-g.x*u1.x,-g.y*u1.y);
+      X[3]=mk(g.x*u0.x,g.y*u0.y);
+      break;
+    }
+    case MULT_DOT: {
+      // Sum of A/2 binary products: X[0] = sum_k X[k] X[A/2+k].
+      int K=A/2;
+      cplx<T> s=cmul(X[0],X[K]);
+      for(int k=1; k < K; ++k) s=s+cmul(X[k],X[K+k]);
+      X[0]=s;
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// Exponent ((s-c) mod N)*r mod N of a residue twiddle.
+__device__ __forceinline__ int twExp(int s, int c, int r, int N)
+{
+  int d=s-c;
+  if(d < 0) d += N;
+  return (int) (((unsigned long long) d*(unsigned long long) r) %
+                (unsigned long long) N);
+}
+
+__device__ __forceinline__ int posmod(int a, int m)
+{
+  int r=a % m;
+  return r < 0 ? r+m : r;
+}
+
+// ---------------------------------------------------------------------------
+// Row kernel, complex data (fftPad / fftPadCentered along the contiguous
+// axis): fold + pre-twiddle (forwardInner: Zetaqp/Zetaqm), m-point FFT, fused
+// multiplier, inverse FFT, post-twiddle and accumulation over residues
+// (backwardInner), normalisation (Convolution::normalize).
+template<typename T>
+__global__ void __launch_bounds__(256)
+rowConvKernel(const RowPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  const int A=P.A, B=P.B, L=P.L, m=P.m, N=P.N, c=P.cshift;
+  cplx<T> *fin=(cplx<T> *) smemRaw;
+  cplx<T> *acc=fin+A*L;
+  cplx<T> *x=acc+B*L;
+  cplx<T> *y=x+m*A;
+  const int tid=threadIdx.x, nthr=blockDim.x;
+  const typename TwT<T>::type *tw=P.twN;
+
+  for(long long row=blockIdx.x; row < P.nrows; row += gridDim.x) {
+    long long base=row*P.rowStride;
+    for(int i=tid; i < A*L; i += nthr) {
+      int a=i/L, s=i-a*L;
+      fin[i]=P.realIO ? mk(((const T *) P.in[a])[base+s],(T) 0) :
+        P.in[a][base+s];
+    }
+    for(int i=tid; i < B*L; i += nthr) acc[i]=mk((T) 0,(T) 0);
+    __syncthreads();
+
+    for(int r=0; r < P.q; ++r) {
+      // Fold the data into one length-m block with the residue twiddles.
+      for(int i=tid; i < m*A; i += nthr) {
+        int t=i/A, a=i-t*A;
+        int s0=posmod(t+c,m);
+        cplx<T> sum=mk((T) 0,(T) 0);
+        for(int s=s0; s < L; s += m) {
+          cplx<T> v=fin[a*L+s];
+          if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
+          sum=sum+v;
+        }
+        x[i]=sum;
+      }
+      __syncthreads();
+      cplx<T> *X=fftSmem<T,1>(x,y,P.fp,A,A,tid,nthr);
+      cplx<T> *Y=X == x ? y : x;
+      for(int j=tid; j < m; j += nthr) {
+        cplx<T> v[FGB_MAXA];
+        for(int a=0; a < A; ++a) v[a]=X[j*A+a];
+        applyMult(P.mult,v,A);
+        for(int b=0; b < B; ++b) X[j*A+b]=v[b];
+      }
+      __syncthreads();
+      cplx<T> *Z=fftSmem<T,-1>(X,Y,P.fp,B,A,tid,nthr);
+      for(int i=tid; i < B*L; i += nthr) {
+        int b=i/L, s=i-b*L;
+        int t=posmod(s-c,m);
+        cplx<T> v=Z[t*A+b];
+        if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
+        acc[i]=acc[i]+v;
+      }
+      __syncthreads();
+    }
+    for(int i=tid; i < B*L; i += nthr) {
+      int b=i/L, s=i-b*L;
+      if(P.realIO) ((T *) P.out[b])[base+s]=acc[i].x*P.scale;
+      else P.out[b][base+s]=acc[i]*P.scale;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Row kernel, Hermitian data (fftPadHermitian along the contiguous axis,
+// explicit padding to an even real length N): the H stored modes are packed
+// into a length-N/2 complex sequence whose sign +1 FFT yields the N real
+// physical values as (u[2t], u[2t+1]) pairs; the multiplier acts on those
+// doubles; the sign -1 FFT of the packed product is unpacked into the H
+// output modes (real-to-complex).
+template<typename T>
+__global__ void __launch_bounds__(256)
+hermRowKernel(const HermRowPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  const int A=P.A, B=P.B, H=P.H, Nh=P.Nh;
+  cplx<T> *zin=(cplx<T> *) smemRaw;
+  cplx<T> *x=zin+A*H;
+  cplx<T> *y=x+Nh*A;
+  const int tid=threadIdx.x, nthr=blockDim.x;
+  const typename TwT<T>::type *tw=P.twN;
+  const T half=(T) 0.5;
+
+  for(long long row=blockIdx.x; row < P.nrows; row += gridDim.x) {
+    long long base=row*P.rowStride;
+    for(int i=tid; i < A*H; i += nthr) {
+      int a=i/H, k=i-a*H;
+      zin[i]=P.in[a][base+k];
+    }
+    __syncthreads();
+    // Y[k] = (Z[k] + conj Z[Nh-k]) + i W_N^k (Z[k] - conj Z[Nh-k])
+    for(int i=tid; i < Nh*A; i += nthr) {
+      int k=i/A, a=i-k*A;
+      cplx<T> zk=k < H ? zin[a*H+k] : mk((T) 0,(T) 0);
+      if(k == 0) zk.y=(T) 0;
+      int kk=Nh-k;
+      cplx<T> zc=kk < H ? conjg(zin[a*H+kk]) : mk((T) 0,(T) 0);
+      cplx<T> s=zk+zc;
+      cplx<T> d=twmul<1>(zk-zc,tw[k]);
+      x[i]=mk(s.x-d.y,s.y+d.x);
+    }
+    __syncthreads();
+    cplx<T> *X=fftSmem<T,1>(x,y,P.fp,A,A,tid,nthr);
+    cplx<T> *Y=X == x ? y : x;
+    for(int t=tid; t < Nh; t += nthr) {
+      cplx<T> v[FGB_MAXA];
+      for(int a=0; a < A; ++a) v[a]=X[t*A+a];
+      applyMult(P.mult,v,A);
+      for(int b=0; b < B; ++b) X[t*A+b]=v[b];
+    }
+    __syncthreads();
+    cplx<T> *Z=fftSmem<T,-1>(X,Y,P.fp,B,A,tid,nthr);
+    // V[k] = E[k] + W_N^{-k} O[k],  E=(Zk+conj Zm)/2, O=(Zk-conj Zm)/(2i)
+    for(int i=tid; i < B*H; i += nthr) {
+      int b=i/H, k=i-b*H;
+      cplx<T> zk=Z[k*A+b];
+      int km=k == 0 ? 0 : Nh-k;
+      cplx<T> zm=conjg(Z[km*A+b]);
+      cplx<T> e=(zk+zm)*half;
+      cplx<T> dd=zk-zm;
+      cplx<T> o=mk(dd.y*half,-dd.x*half);
+      cplx<T> v=e+twmul<-1>(o,tw[k]);
+      P.out[b][base+k]=v*P.scale;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Outer forward, complex data: residue block r of the padded transform along
+// a strided axis for `tile` adjacent columns.
+template<typename T>
+__global__ void __launch_bounds__(256)
+outerFwdKernel(const OuterPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  const int tile=P.tile, m=P.m, N=P.N, c=P.cshift, L=P.L;
+  cplx<T> *x=(cplx<T> *) smemRaw;
+  cplx<T> *y=x+m*tile;
+  const int tid=threadIdx.x, nthr=blockDim.x;
+  const int col0=blockIdx.x*tile;
+  const int r=blockIdx.y;
+  const int a=blockIdx.z % P.count;
+  const long long batch=blockIdx.z/P.count;
+  const cplx<T> *src=P.in[a]+batch*P.inBatch;
+  cplx<T> *dst=P.out[a]+batch*P.outBatch;
+  const typename TwT<T>::type *tw=P.twN;
+
+  for(int i=tid; i < m*tile; i += nthr) {
+    int t=i/tile, cc=i-t*tile;
+    int col=col0+cc;
+    cplx<T> sum=mk((T) 0,(T) 0);
+    if(col < P.C) {
+      int s0=posmod(t+c,m);
+      for(int s=s0; s < L; s += m) {
+        long long off=(long long) s*P.inRow+col;
+        if(off >= P.Ltot) break;
+        cplx<T> v=src[off];
+        if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
+        sum=sum+v;
+      }
+    }
+    x[i]=sum;
+  }
+  __syncthreads();
+  cplx<T> *X=fftSmem<T,1>(x,y,P.fp,tile,tile,tid,nthr);
+  for(int i=tid; i < m*tile; i += nthr) {
+    int j=i/tile, cc=i-j*tile;
+    int col=col0+cc;
+    if(col < P.C) {
+      cplx<T> v=X[i];
+      long long k=(long long) r*m+j;
+      if(P.twX) {
+        unsigned long long e=((unsigned long long) col*(unsigned long long) k)
+          % (unsigned long long) P.NX;
+        v=twmul<1>(v,P.twX[e]);
+      }
+      dst[k*P.outRow+col]=v;
+    }
+  }
+}
+
+// Outer backward, complex data: all residues of a column tile, accumulated.
+template<typename T>
+__global__ void __launch_bounds__(256)
+outerBwdKernel(const OuterPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  const int tile=P.tile, m=P.m, N=P.N, c=P.cshift, L=P.L;
+  cplx<T> *acc=(cplx<T> *) smemRaw;
+  cplx<T> *x=acc+L*tile;
+  cplx<T> *y=x+m*tile;
+  const int tid=threadIdx.x, nthr=blockDim.x;
+  const int col0=blockIdx.x*tile;
+  const int b=blockIdx.z % P.count;
+  const long long batch=blockIdx.z/P.count;
+  const cplx<T> *src=P.in[b]+batch*P.inBatch;
+  cplx<T> *dst=P.out[b]+batch*P.outBatch;
+  const typename TwT<T>::type *tw=P.twN;
+
+  for(int i=tid; i < L*tile; i += nthr) acc[i]=mk((T) 0,(T) 0);
+  for(int r=0; r < P.q; ++r) {
+    for(int i=tid; i < m*tile; i += nthr) {
+      int j=i/tile, cc=i-j*tile;
+      int col=col0+cc;
+      cplx<T> v=mk((T) 0,(T) 0);
+      if(col < P.C) {
+        long long k=(long long) r*m+j;
+        v=src[k*P.inRow+col];
+        if(P.twX) {
+          unsigned long long e=((unsigned long long) col*(unsigned long long) k)
+            % (unsigned long long) P.NX;
+          v=twmul<-1>(v,P.twX[e]);
+        }
+      }
+      x[i]=v;
+    }
+    __syncthreads();
+    cplx<T> *X=fftSmem<T,-1>(x,y,P.fp,tile,tile,tid,nthr);
+    for(int i=tid; i < L*tile; i += nthr) {
+      int s=i/tile, cc=i-s*tile;
+      int t=posmod(s-c,m);
+      cplx<T> v=X[t*tile+cc];
+      if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
+      acc[i]=acc[i]+v;
+    }
+    __syncthreads();
+  }
+  for(int i=tid; i < L*tile; i += nthr) {
+    int s=i/tile, cc=i-s*tile;
+    int col=col0+cc;
+    long long off=(long long) s*P.outRow+col;
+    if(col < P.C && off < P.Ltot) dst[off]=acc[i]*P.scale;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Outer forward, real data (fftPadReal with explicit padding to even N):
+// pack z[t] = f[2t] + i f[2t+1], sign +1 FFT of length N/2, unpack the
+// N/2+1 non-negative modes F(k) = E[k] + W_N^k O[k].
+template<typename T>
+__global__ void __launch_bounds__(256)
+outerRealFwdKernel(const OuterPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  const int tile=P.tile, L=P.L, Nh=P.N/2;
+  cplx<T> *x=(cplx<T> *) smemRaw;
+  cplx<T> *y=x+Nh*tile;
+  const int tid=threadIdx.x, nthr=blockDim.x;
+  const int col0=blockIdx.x*tile;
+  const int a=blockIdx.z % P.count;
+  const long long batch=blockIdx.z/P.count;
+  const T *src=(const T *) P.in[a]+batch*P.inBatch;
+  cplx<T> *dst=P.out[a]+batch*P.outBatch;
+  const typename TwT<T>::type *tw=P.twN;
+  const T half=(T) 0.5;
+
+  for(int i=tid; i < Nh*tile; i += nthr) {
+    int t=i/tile, cc=i-t*tile;
+    int col=col0+cc;
+    T re=0, im=0;
+    if(col < P.C) {
+      int s=2*t;
+      if(s < L) re=src[(long long) s*P.inRow+col];
+      if(s+1 < L) im=src[(long long) (s+1)*P.inRow+col];
+    }
+    x[i]=mk(re,im);
+  }
+  __syncthreads();
+  cplx<T> *X=fftSmem<T,1>(x,y,P.fp,tile,tile,tid,nthr);
+  for(int i=tid; i < (Nh+1)*tile; i += nthr) {
+    int k=i/tile, cc=i-k*tile;
+    int col=col0+cc;
+    if(col >= P.C) continue;
+    int k0=k == Nh ? 0 : k;
+    int km=k == 0 || k == Nh ? 0 : Nh-k;
+    cplx<T> zk=X[k0*tile+cc];
+    cplx<T> zm=conjg(X[km*tile+cc]);
+    cplx<T> e=(zk+zm)*half;
+    cplx<T> dd=zk-zm;
+    cplx<T> o=mk(dd.y*half,-dd.x*half);
+    cplx<T> v;
+    if(k == Nh) v=e-o;
+    else v=e+twmul<1>(o,tw[k]);
+    dst[(long long) k*P.outRow+col]=v;
+  }
+}
+
+// Outer backward, real data: Hermitian-extend the N/2+1 modes, pack
+// Y[k] = (G[k] + conj G[Nh-k]) + i W_N^{-k} (G[k] - conj G[Nh-k]), sign -1
+// FFT of length N/2, unpack h[2t] = Re y[t], h[2t+1] = Im y[t].
+template<typename T>
+__global__ void __launch_bounds__(256)
+outerRealBwdKernel(const OuterPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  const int tile=P.tile, L=P.L, Nh=P.N/2;
+  cplx<T> *x=(cplx<T> *) smemRaw;
+  cplx<T> *y=x+Nh*tile;
+  const int tid=threadIdx.x, nthr=blockDim.x;
+  const int col0=blockIdx.x*tile;
+  const int b=blockIdx.z % P.count;
+  const long long batch=blockIdx.z/P.count;
+  const cplx<T> *src=P.in[b]+batch*P.inBatch;
+  T *dst=(T *) P.out[b]+batch*P.outBatch;
+  const typename TwT<T>::type *tw=P.twN;
+
+  for(int i=tid; i < Nh*tile; i += nthr) {
+    int k=i/tile, cc=i-k*tile;
+    int col=col0+cc;
+    cplx<T> v=mk((T) 0,(T) 0);
+    if(col < P.C) {
+      cplx<T> gk=src[(long long) k*P.inRow+col];
+      if(k == 0) gk.y=(T) 0;
+      cplx<T> gm=src[(long long) (Nh-k)*P.inRow+col];
+      if(k == 0) gm.y=(T) 0;
+      gm=conjg(gm);
+      cplx<T> s=gk+gm;
+      cplx<T> d=twmul<-1>(gk-gm,tw[k]);
+      v=mk(s.x-d.y,s.y+d.x);
+    }
+    x[i]=v;
+  }
+  __syncthreads();
+  cplx<T> *X=fftSmem<T,-1>(x,y,P.fp,tile,tile,tid,nthr);
+  for(int i=tid; i < Nh*tile; i += nthr) {
+    int t=i/tile, cc=i-t*tile;
+    int col=col0+cc;
+    if(col >= P.C) continue;
+    cplx<T> v=X[i]*P.scale;
+    int s=2*t;
+    if(s < L) dst[(long long) s*P.outRow+col]=v.x;
+    if(s+1 < L) dst[(long long) (s+1)*P.outRow+col]=v.y;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers.
+
+template<typename T> size_t rowSmem(int L, int m, int A, int B)
+{
+  return sizeof(cplx<T>)*((size_t) (A+B)*L+2*(size_t) m*A);
+}
+template<typename T> size_t hermRowSmem(int H, int Nh, int A)
+{
+  return sizeof(cplx<T>)*((size_t) A*H+2*(size_t) Nh*A);
+}
+template<typename T> size_t outerFwdSmem(int m, int tile)
+{
+  return sizeof(cplx<T>)*2*(size_t) m*tile;
+}
+template<typename T> size_t outerBwdSmem(int L, int m, int tile)
+{
+  return sizeof(cplx<T>)*((size_t) L*tile+2*(size_t) m*tile);
+}
+template<typename T> size_t outerRealSmem(int L, int Nh, int tile)
+{
+  return sizeof(cplx<T>)*2*(size_t) (Nh+1)*tile;
+}
+
+template<typename K>
+static cudaError_t setSmem(K kernel, size_t bytes)
+{
+  if(bytes > 48*1024)
+    return cudaFuncSetAttribute(kernel,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int) bytes);
+  return cudaSuccess;
+}
+
+template<typename T>
+cudaError_t launchRow(const RowPlan<T>& P, int threads, long long grid,
+                      cudaStream_t s)
+{
+  size_t sm=rowSmem<T>(P.L,P.m,P.A,P.B);
+  cudaError_t e=setSmem(rowConvKernel<T>,sm);
+  if(e != cudaSuccess) return e;
+  rowConvKernel<T><<<(unsigned) grid,threads,sm,s>>>(P);
+  return cudaGetLastError();
+}
+
+template<typename T>
+cudaError_t launchHermRow(const HermRowPlan<T>& P, int threads,
+                          long long grid, cudaStream_t s)
+{
+  size_t sm=hermRowSmem<T>(P.H,P.Nh,P.A);
+  cudaError_t e=setSmem(hermRowKernel<T>,sm);
+  if(e != cudaSuccess) return e;
+  hermRowKernel<T><<<(unsigned) grid,threads,sm,s>>>(P);
+  return cudaGetLastError();
+}
+
+template<typename T>
+cudaError_t launchOuterFwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
+{
+  size_t sm=outerFwdSmem<T>(P.m,P.tile);
+  cudaError_t e=setSmem(outerFwdKernel<T>,sm);
+  if(e != cudaSuccess) return e;
+  dim3 grid((P.C+P.tile-1)/P.tile,P.q,P.nbatch*P.count);
+  outerFwdKernel<T><<<grid,threads,sm,s>>>(P);
+  return cudaGetLastError();
+}
+
+template<typename T>
+cudaError_t launchOuterBwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
+{
+  size_t sm=outerBwdSmem<T>(P.L,P.m,P.tile);
+  cudaError_t e=setSmem(outerBwdKernel<T>,sm);
+  if(e != cudaSuccess) return e;
+  dim3 grid((P.C+P.tile-1)/P.tile,1,P.nbatch*P.count);
+  outerBwdKernel<T><<<grid,threads,sm,s>>>(P);
+  return cudaGetLastError();
+}
+
+template<typename T>
+cudaError_t launchOuterRealFwd(const OuterPlan<T>& P, int threads,
+                               cudaStream_t s)
+{
+  size_t sm=outerRealSmem<T>(P.L,P.N/2,P.tile);
+  cudaError_t e=setSmem(outerRealFwdKernel<T>,sm);
+  if(e != cudaSuccess) return e;
+  dim3 grid((P.C+P.tile-1)/P.tile,1,P.nbatch*P.count);
+  outerRealFwdKernel<T><<<grid,threads,sm,s>>>(P);
+  return cudaGetLastError();
+}
+
+template<typename T>
+cudaError_t launchOuterRealBwd(const OuterPlan<T>& P, int threads,
+                               cudaStream_t s)
+{
+  size_t sm=outerRealSmem<T>(P.L,P.N/2,P.tile);
+  cudaError_t e=setSmem(outerRealBwdKernel<T>,sm);
+  if(e != cudaSuccess) return e;
+  dim3 grid((P.C+P.tile-1)/P.tile,1,P.nbatch*P.count);
+  outerRealBwdKernel<T><<<grid,threads,sm,s>>>(P);
+  return cudaGetLastError();
+}
+
+#define FGB_INSTANTIATE(T) \
+  template cudaError_t launchRow<T>(const RowPlan<T>&,int,long long,cudaStream_t); \
+  template cudaError_t launchHermRow<T>(const HermRowPlan<T>&,int,long long,cudaStream_t); \
+  template cudaError_t launchOuterFwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
+  template cudaError_t launchOuterBwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
+  template cudaError_t launchOuterRealFwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
+  template cudaError_t launchOuterRealBwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
+  template size_t rowSmem<T>(int,int,int,int); \
+  template size_t hermRowSmem<T>(int,int,int); \
+  template size_t outerFwdSmem<T>(int,int); \
+  template size_t outerBwdSmem<T>(int,int,int); \
+  template size_t outerRealSmem<T>(int,int,int);
+
+FGB_INSTANTIATE(double)
+FGB_INSTANTIATE(float)
+
+} // namespace fgb

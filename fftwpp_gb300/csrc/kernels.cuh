@@ -1,0 +1,111 @@
+// kernels.cuh -- parameter blocks of the GB300 hybrid-convolution kernels.
+//
+// Three kernel families cover every padded-transform kind of FFTW++'s
+// convolve.h on one GPU:
+//
+//  * row kernels: the whole padded sub-convolution along the contiguous
+//    (innermost) axis of one row, on chip: load the A input rows, for every
+//    residue r form the folded, pre-twiddled length-m block, FFT (+1), apply
+//    the multiplier, inverse FFT (-1) and accumulate the post-twiddled block
+//    into the B output rows.  Padded data never leaves shared memory
+//    (fftPad/fftPadCentered residue loop, convolve.cc:849-1965; multiplier
+//    convolve.cc:26-110; Convolution::convolveRaw convolve.cc:7513-7575).
+//    A Hermitian variant runs the complex-to-real / real-to-complex pair
+//    through a half-length complex FFT (fftPadHermitian, convolve.cc:4309).
+//  * outer forward kernels: one CTA per (column tile, residue r, batch,
+//    input) computes the residue block r of the padded transform along a
+//    strided axis for a tile of adjacent columns and writes it to an HBM
+//    staging buffer laid out [residue][j][column] (fftPad*::forward*Many,
+//    the x/y stages of Convolution2/3, convolve.h:1415-1420).
+//  * outer backward kernels: one CTA per (column tile, batch, output) loops
+//    over all residues, inverse-transforms each block and accumulates into
+//    its output tile (fftPad*::backward*Many).  Real data along the outer
+//    axis (fftPadReal) uses an explicit packed real FFT instead.
+#pragma once
+
+#include "fft_smem.cuh"
+
+namespace fgb {
+
+#define FGB_MAXA 8
+
+enum MultKind {
+  MULT_NONE=0, MULT_BINARY=1, MULT_REALBINARY=2, MULT_CORRELATION=3,
+  MULT_REALJACOBIAN=4, MULT_JACOBIAN=5, MULT_REALJACADJ=6, MULT_DOT=7
+};
+
+template<typename T>
+struct RowPlan {
+  const cplx<T> *in[FGB_MAXA];
+  cplx<T> *out[FGB_MAXA];
+  long long rowStride;     // elements between consecutive rows
+  long long nrows;
+  int L;                   // stored complex values per row
+  int m, q, N;             // residue block length, residues, padded length
+  int cshift;              // centred origin offset (0 for fftPad)
+  int A, B, mult;
+  int realIO;              // real data in and out (1D fftPadReal rows)
+  T scale;
+  FFTPlanDev fp;           // length-m complex FFT
+  const typename TwT<T>::type *twN;   // W_N^t, t < N
+};
+
+template<typename T>
+struct HermRowPlan {
+  const cplx<T> *in[FGB_MAXA];
+  cplx<T> *out[FGB_MAXA];
+  long long rowStride;
+  long long nrows;
+  int H;                   // stored Hermitian modes (k = 0..H-1)
+  int N, Nh;               // real padded length (even) and N/2
+  int A, B, mult;
+  T scale;
+  FFTPlanDev fp;           // length-Nh complex FFT
+  const typename TwT<T>::type *twN;   // W_N^t, t < N
+};
+
+template<typename T>
+struct OuterPlan {
+  const cplx<T> *in[FGB_MAXA];
+  cplx<T> *out[FGB_MAXA];
+  int count;               // arrays processed (A forward, B backward)
+  long long inBatch, outBatch;   // elements between batches
+  int nbatch;
+  long long inRow, outRow; // elements between consecutive axis positions
+  int C;                   // columns per axis position
+  long long Ltot;          // element (s,c) of the data side is valid iff
+                           // s*dataRow + c < Ltot
+  int L, m, q, N, cshift;
+  int tile;
+  T scale;
+  FFTPlanDev fp;           // length-m (complex) or length-N/2 (real) FFT
+  const typename TwT<T>::type *twN;
+  const typename TwT<T>::type *twX;  // optional W_NX^{col*k} (1D long path)
+  long long NX;
+};
+
+// Host launchers (kernels.cu).
+template<typename T> cudaError_t launchRow(const RowPlan<T>& P, int threads,
+                                           long long grid, cudaStream_t s);
+template<typename T> cudaError_t launchHermRow(const HermRowPlan<T>& P,
+                                               int threads, long long grid,
+                                               cudaStream_t s);
+template<typename T> cudaError_t launchOuterFwd(const OuterPlan<T>& P,
+                                                int threads, cudaStream_t s);
+template<typename T> cudaError_t launchOuterBwd(const OuterPlan<T>& P,
+                                                int threads, cudaStream_t s);
+template<typename T> cudaError_t launchOuterRealFwd(const OuterPlan<T>& P,
+                                                    int threads,
+                                                    cudaStream_t s);
+template<typename T> cudaError_t launchOuterRealBwd(const OuterPlan<T>& P,
+                                                    int threads,
+                                                    cudaStream_t s);
+
+// Shared-memory bytes each kernel needs (for plan-time sizing).
+template<typename T> size_t rowSmem(int L, int m, int A, int B);
+template<typename T> size_t hermRowSmem(int H, int Nh, int A);
+template<typename T> size_t outerFwdSmem(int m, int tile);
+template<typename T> size_t outerBwdSmem(int L, int m, int tile);
+template<typename T> size_t outerRealSmem(int L, int Nh, int tile);
+
+} // namespace fgb

@@ -1,0 +1,155 @@
+"""Device-tensor interface to the GB300 hybrid dealiased convolution.
+
+PyTorch supplies device memory and the current CUDA stream only; every
+convolution runs in the hand-written kernels of lib_fftwpp.so through the C
+ABI of include/fftwpp_gb300.h.  There is no CPU or library fallback: if the
+native library is missing, construction raises.
+
+The class mirrors the reference's composition of padded transforms and a
+Convolution driver (convolve.h:471-1893): one padded-transform kind per axis
+(PAD = fftPad, CENTERED = fftPadCentered, HERMITIAN = fftPadHermitian,
+REAL = fftPadReal), a minimum padded length M per axis, A inputs, B outputs
+and a multiplier.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Sequence
+
+from . import _native
+from ._native import CENTERED, F32, F64, HERMITIAN, MULT, PAD, REAL
+
+__all__ = ["HybridConvolution", "PAD", "CENTERED", "HERMITIAN", "REAL",
+           "default_M"]
+
+
+def default_M(kind: int, L: int, A: int = 2) -> int:
+    """Default minimum padded length of the reference's C wrappers
+    (wrappers/HybridConvolution.h:19, 39)."""
+    if kind in (CENTERED, HERMITIAN):
+        return 3 * ((L + 1) // 2) - 2 * (L % 2)
+    return A * L - A + 1
+
+
+class HybridConvolution:
+    """A planned convolution on the current CUDA device.
+
+    kinds, L, M: per axis, outermost first.  m: optional forced residue
+    block lengths (the reference's Application m).  precision: "f64" (the
+    drop-in mode) or "f32" (FP32 data with split hi+lo twiddles).
+    batch: independent 1D problems stored back to back.
+    """
+
+    def __init__(self, kinds: Sequence[int], L: Sequence[int],
+                 M: Sequence[int] | None = None, *, m: Sequence[int] | None = None,
+                 A: int = 2, B: int = 1, mult: str = "binary",
+                 precision: str = "f64", batch: int = 1):
+        import torch
+        self.lib = _native.load()
+        self.kinds = list(kinds)
+        self.L = list(L)
+        self.dim = len(self.kinds)
+        if M is None:
+            M = [default_M(k, l, A) for k, l in zip(self.kinds, self.L)]
+        self.M = list(M)
+        self.A, self.B = A, B
+        self.mult = mult
+        self.precision = precision
+        self.prec = F64 if precision == "f64" else F32
+        self.batch = batch
+        self.real = self.kinds[0] == REAL
+        sz = ctypes.c_size_t
+        d = self.dim
+        karr = (ctypes.c_int * d)(*self.kinds)
+        Larr = (sz * d)(*self.L)
+        Marr = (sz * d)(*self.M)
+        marr = (sz * d)(*(m or [0] * d))
+        torch.cuda.current_device()   # make sure a context exists
+        self.handle = self.lib.fgb_create(d, karr, Larr, Marr, marr, A, B,
+                                          MULT[mult], self.prec, batch)
+        if not self.handle:
+            raise ValueError(_native.last_error())
+        info = (ctypes.c_long * 27)()
+        self.lib.fgb_info(self.handle, info)
+        self.axes = []
+        for a in range(d):
+            o = info[8 * a: 8 * a + 8]
+            self.axes.append(dict(m=o[0], p=o[1], q=o[2], N=o[3], stored=o[4],
+                                  cshift=o[5], tile=o[6], rows=o[7]))
+        self.launches = info[24]
+        self.staging_bytes = info[25]
+        self.long_path = bool(info[26])
+        self.shape = tuple(ax["stored"] for ax in self.axes)
+        if batch > 1:
+            self.shape = (batch,) + self.shape
+
+    # -- layout -------------------------------------------------------------
+    @property
+    def dtype(self):
+        import torch
+        if self.real:
+            return torch.float64 if self.prec == F64 else torch.float32
+        return torch.complex128 if self.prec == F64 else torch.complex64
+
+    @property
+    def normalization(self) -> int:
+        n = 1
+        for ax in self.axes:
+            n *= ax["N"]
+        return n
+
+    def _check(self, t):
+        import torch
+        if not isinstance(t, torch.Tensor) or not t.is_cuda:
+            raise TypeError("inputs must be CUDA tensors")
+        if t.dtype != self.dtype:
+            raise TypeError(f"expected {self.dtype}, got {t.dtype}")
+        if tuple(t.shape) != self.shape or not t.is_contiguous():
+            raise ValueError(f"expected a contiguous tensor of shape "
+                             f"{self.shape}, got {tuple(t.shape)}")
+
+    # -- execution ----------------------------------------------------------
+    def convolve(self, *inputs, out=None, stream=None):
+        """Convolve A device tensors; returns the B outputs (new tensors
+        unless `out` is given; out may alias the inputs)."""
+        import torch
+        if len(inputs) != self.A:
+            raise ValueError(f"expected {self.A} inputs")
+        for t in inputs:
+            self._check(t)
+        if out is None:
+            out = [torch.empty_like(inputs[0]) for _ in range(self.B)]
+        for t in out:
+            self._check(t)
+        ins = (ctypes.c_void_p * self.A)(*[t.data_ptr() for t in inputs])
+        outs = (ctypes.c_void_p * self.B)(*[t.data_ptr() for t in out])
+        s = stream if stream is not None else torch.cuda.current_stream()
+        rc = self.lib.fgb_convolve_device(self.handle, ins, outs,
+                                          ctypes.c_void_p(s.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(_native.last_error())
+        return out
+
+    def convolve_host(self, *arrays):
+        """Convolve host numpy arrays through the host-pointer C entry
+        (copies in and out inside the call); results overwrite arrays[0..B-1]."""
+        import numpy as np
+        if len(arrays) != self.A:
+            raise ValueError(f"expected {self.A} inputs")
+        for a in arrays:
+            if not (isinstance(a, np.ndarray) and a.flags["C_CONTIGUOUS"]):
+                raise TypeError("host inputs must be C-contiguous numpy arrays")
+        ptrs = (ctypes.c_void_p * self.A)(*[a.ctypes.data for a in arrays])
+        rc = self.lib.fgb_convolve_host(self.handle, ptrs, ptrs)
+        if rc != 0:
+            raise RuntimeError(_native.last_error())
+        return list(arrays[:self.B])
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            try:
+                self.lib.fgb_destroy(h)
+            except Exception:
+                pass
+            self.handle = None

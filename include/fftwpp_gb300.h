@@ -1,0 +1,100 @@
+/* fftwpp_gb300.h -- device-pointer C ABI of the GB300 hybrid dealiased
+ * convolution (lib_fftwpp.so).
+ *
+ * These entry points generalise the reference's C wrapper
+ * (wrappers/cfftw++.h) to everything its C++ API can wire
+ * (convolve.h:471-1893): any dimension 1-3, any padded-transform kind per
+ * axis, any minimum padded length, A inputs / B outputs, a built-in
+ * multiplier, FP64 or FP32-compensated arithmetic, a batch of independent
+ * 1D problems, and device pointers on a caller-supplied CUDA stream.  No
+ * PyTorch types appear: pointers and sizes only.
+ *
+ * Layout: every array is dense row-major in its stored shape (a Hermitian
+ * innermost axis stores ceil(L/2) modes; a real outermost axis means real
+ * data throughout); complex values are interleaved (re, im).
+ * Status codes: 0 on success, negative on error (fgb_last_error()).
+ */
+#ifndef FFTWPP_GB300_H
+#define FFTWPP_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Padded-transform kinds (convolve.h:471, 592, 701, 805). */
+#define FGB_PAD 0        /* fftPad */
+#define FGB_CENTERED 1   /* fftPadCentered */
+#define FGB_HERMITIAN 2  /* fftPadHermitian (innermost axis only) */
+#define FGB_REAL 3       /* fftPadReal (outermost axis only) */
+
+/* Built-in multipliers (convolve.cc:26-110) and additions. */
+#define FGB_MULT_NONE 0
+#define FGB_MULT_BINARY 1          /* multBinary: F0 *= F1 */
+#define FGB_MULT_REALBINARY 2      /* realMultBinary, lane-wise doubles */
+#define FGB_MULT_CORRELATION 3     /* multcorrelation: F0 *= conj(F1) */
+#define FGB_MULT_REALJACOBIAN 4    /* F0 = F0 F3 - F1 F2 on real data */
+#define FGB_MULT_JACOBIAN 5        /* same on complex data */
+#define FGB_MULT_REALJACADJ 6      /* adjoint of FGB_MULT_REALJACOBIAN */
+#define FGB_MULT_DOT 7             /* F0 = sum_k F_k F_{A/2+k} */
+
+#define FGB_F64 0
+#define FGB_F32 1                  /* FP32 data, split hi+lo twiddles */
+
+typedef struct fgb_conv fgb_conv;
+
+/* Plan a convolution.  kinds, L, M: per axis, outermost first.  m: NULL or
+ * per-axis forced residue block length (0 = planner's choice), the
+ * Application m of the reference (convolve.h:103-111).  batch > 1 runs
+ * independent 1D problems stored back to back.  Replaces the constructors
+ * fftPad*(L,M,app,...) + Convolution{,2,3}(...) (convolve.h:515-1603).
+ * Returns NULL on error. */
+fgb_conv *fgb_create(int dim, const int *kinds, const size_t *L,
+                     const size_t *M, const size_t *m, int A, int B,
+                     int mult, int precision, size_t batch);
+
+/* Convolve device arrays on `stream` (a cudaStream_t, NULL = legacy
+ * default stream): in[A] inputs, out[B] outputs (out[b] may equal in[b]).
+ * Inputs in[B..A-1] are preserved.  Replaces Convolution::convolve
+ * (convolve.h:1157-1160) with normalisation by 1/prod(m q). */
+int fgb_convolve_device(fgb_conv *c, void *const *in, void *const *out,
+                        void *stream);
+
+/* Same on host arrays: copies in, runs, copies out, synchronises. */
+int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out);
+
+/* Plan parameters: for each axis d, info[8d..8d+7] = m, p, q, N, stored
+ * length, centred offset, outer tile, rows produced.  info[24] = kernels per
+ * convolution, info[25] = staging bytes, info[26] = 1 if the 1D long path
+ * is used.  Mirrors the public members m,p,q,M of fftBase
+ * (convolve.h:123-145). */
+int fgb_info(const fgb_conv *c, long *info);
+
+void fgb_destroy(fgb_conv *c);
+
+/* Text of the last error on this thread. */
+const char *fgb_last_error(void);
+
+/* The reference's integer rules, exported for tests:
+ * fftBase::parameters (convolve.cc:403-410) and nextfftsize
+ * (convolve.cc:114-124). */
+void fgb_parameters(size_t L, size_t M, size_t m, int centered,
+                    size_t *p, size_t *n, size_t *q);
+size_t fgb_nextfftsize(size_t m);
+
+/* Transformed index of entry i of residue block r (fftBase::index,
+ * convolve.h:297-326, and fftPadReal::index, convolve.h:956-979) for the
+ * reference's parameters (m,p,q,n,D) of a 1D transform. */
+size_t fgb_index(int kind, size_t m, size_t p, size_t q, size_t n, size_t D,
+                 size_t r, size_t i);
+
+/* Hermitian symmetrisation of device arrays (convolve.h:1175-1258). */
+int fgb_hermitian_symmetrize_x_device(size_t Hx, size_t Hy, size_t x0,
+                                      void *f, int precision, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

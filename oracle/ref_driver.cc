@@ -198,7 +198,9 @@ long ref_forward_layout(int kind, size_t L, size_t M, size_t m, size_t D,
   if(fft->overwrite) {delete fft; return -2;}
   Complex *f=ComplexAlign(L);
   Complex *F=ComplexAlign(fft->outputSize());
-  Complex *W0=ComplexAlign(std::max(fft->workSizeW(),(size_t) 1));
+  // In-place plans take W=NULL (tests/hybrid.cc:63: ComplexAlign(0) is NULL).
+  size_t wsize=fft->workSizeW();
+  Complex *W0=wsize ? ComplexAlign(wsize) : NULL;
   memcpy((double *) f,in,2*L*sizeof(double));
   fft->pad(W0);
   size_t total=0;
@@ -217,7 +219,7 @@ long ref_forward_layout(int kind, size_t L, size_t M, size_t m, size_t D,
     info[6]=fft->R;
     info[7]=fft->M;
   }
-  deleteAlign(W0);
+  if(W0) deleteAlign(W0);
   deleteAlign(F);
   deleteAlign(f);
   delete fft;
