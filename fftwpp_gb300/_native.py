@@ -49,6 +49,10 @@ def load():
     lib.fgb_convolve_host.argtypes = [vp, P(vp), P(vp)]
     lib.fgb_info.restype = ctypes.c_int
     lib.fgb_info.argtypes = [vp, P(ctypes.c_long)]
+    lib.fgb_timing.restype = ctypes.c_int
+    lib.fgb_timing.argtypes = [vp, ctypes.c_int]
+    lib.fgb_timing_collect.restype = ctypes.c_int
+    lib.fgb_timing_collect.argtypes = [vp, P(ctypes.c_double), ctypes.c_int]
     lib.fgb_destroy.restype = None
     lib.fgb_destroy.argtypes = [vp]
     lib.fgb_last_error.restype = ctypes.c_char_p

@@ -338,7 +338,7 @@ int fgb_info(const fgb_conv *c, long *info)
 {
   if(!c || !info) return -1;
   const ConvInfo& I=c->conv->info();
-  for(int k=0; k < 27; ++k) info[k]=0;
+  for(int k=0; k < 32; ++k) info[k]=0;
   for(int d=0; d < I.dim; ++d) {
     const AxisPlan& a=I.axis[d];
     long *o=info+8*d;
@@ -348,7 +348,32 @@ int fgb_info(const fgb_conv *c, long *info)
   info[24]=c->conv->launches();
   info[25]=(long) c->conv->stagingBytes();
   info[26]=I.longRow ? 1 : 0;
+  for(int d=0; d < I.dim; ++d) info[27+d]=I.axis[d].tileB;
   return 0;
+}
+
+int fgb_set_normalize(fgb_conv *c, int normalize)
+{
+  if(!c) return -1;
+  c->conv->setNormalize(normalize != 0);
+  return 0;
+}
+
+int fgb_timing(fgb_conv *c, int enable)
+{
+  if(!c) return -1;
+  cudaError_t e=c->conv->enableTiming(enable != 0);
+  if(e != cudaSuccess) {
+    report("fgb_timing",cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
+int fgb_timing_collect(fgb_conv *c, double *ms, int n)
+{
+  if(!c || !ms) return -1;
+  return c->conv->collect(ms,n);
 }
 
 void fgb_destroy(fgb_conv *c) {destroy(c);}

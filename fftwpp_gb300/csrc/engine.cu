@@ -243,18 +243,60 @@ static bool planRowHermitian(AxisPlan& a, long mForce, int A, int prec)
   return hermNeed(prec,a.stored,a.N/2,A) <= SMEM_MAX;
 }
 
-static void planOuter(AxisPlan& a, long mForce, int prec)
+// Estimated FP64/FP32 arithmetic instructions of one length-n transform in
+// the radix order fftPlan uses (codelet + twiddles per point, stage 0 has
+// unit twiddles).
+static double fftInstr(long n)
 {
-  int tile=prec == PREC_F64 ? 8 : 16;
+  std::vector<int> rad;
+  long r=n;
+  while(r % 8 == 0) {rad.push_back(8); r /= 8;}
+  if(r % 4 == 0) {rad.push_back(4); r /= 4;}
+  if(r % 2 == 0) {rad.push_back(2); r /= 2;}
+  while(r % 7 == 0) {rad.push_back(7); r /= 7;}
+  while(r % 5 == 0) {rad.push_back(5); r /= 5;}
+  while(r % 3 == 0) {rad.push_back(3); r /= 3;}
+  double per=0;
+  for(size_t i=0; i < rad.size(); ++i) {
+    int R=rad[i];
+    double code=R == 8 ? 7.0 : R == 4 ? 4.0 : R == 2 ? 2.0 : R == 3 ? 4.7 :
+      R == 5 ? 6.8 : 8.6;
+    double tw=i == 0 ? 0.0 : 4.0*(R-1)/R;
+    per += code+tw;
+  }
+  return per*n;
+}
+
+static const int NSM=152;
+
+// Largest power-of-two tile <= maxTile whose kernel fits in shared memory
+// and still gives at least three waves of CTAs over the SMs.
+template<typename F>
+static int pickTile(int maxTile, long C, long factor, F smem)
+{
+  int tile=maxTile;
+  while(tile > 1 && (smem(tile) > SMEM_MAX ||
+                     ceilquotient(C,tile)*factor < 3*NSM))
+    tile /= 2;
+  while(tile > 1 && smem(tile) > SMEM_MAX) tile /= 2;
+  return tile;
+}
+
+static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
+                      int A, int B)
+{
+  int maxTile=prec == PREC_F64 ? 8 : 16;
   if(a.kind == KIND_REAL) {
     a.N=evenSmooth(mForce > 0 ? std::max(a.M,mForce) : a.M);
     a.m=a.N; a.q=1; a.p=1; a.cshift=0;
     a.rows=a.N/2+1;
     long Nh=a.N/2;
-    while(tile > 1 && (prec == PREC_F64 ? outerRealSmem<double>(a.L,Nh,tile) :
-                       outerRealSmem<float>(a.L,Nh,tile)) > SMEM_MAX)
-      tile /= 2;
-    a.tile=tile;
+    auto sm=[&](int t) {
+      return prec == PREC_F64 ? outerRealSmem<double>(a.L,Nh,t) :
+        outerRealSmem<float>(a.L,Nh,t);
+    };
+    a.tile=pickTile(maxTile,C,nbatch*A,sm);
+    a.tileB=pickTile(maxTile,C,nbatch*B,sm);
     return;
   }
   bool centered=a.kind == KIND_CENTERED;
@@ -273,7 +315,11 @@ static void planOuter(AxisPlan& a, long mForce, int prec)
       long q=N/m;
       if(outerNeed(prec,a.L,m,1) > SMEM_MAX) continue;
       long p=ceilquotient(a.L,m);
-      double cost=q*(fftCost(m)+p*(double) m)+fftCost(m)+0.25*a.L;
+      // Residue r > 0 folds p terms with a complex twiddle each (forward)
+      // and post-twiddles every output (backward); r = 0 only adds.
+      double fwd=q*fftInstr(m)+m*(2.0*p+(q-1)*6.0*p);
+      double bwd=q*fftInstr(m)+a.L*(2.0+(q-1)*6.0);
+      double cost=A*fwd+B*bwd;
       if(cost < best) {best=cost; bm=m;}
     }
     if(!bm) throw std::runtime_error("no outer padding plan fits");
@@ -283,15 +329,24 @@ static void planOuter(AxisPlan& a, long mForce, int prec)
   a.p=ceilquotient(a.L,a.m);
   a.cshift=centered ? (int) (a.L/2) : 0;
   a.rows=a.N;
-  while(tile > 1 && outerNeed(prec,a.L,a.m,tile) > SMEM_MAX) tile /= 2;
-  if(outerNeed(prec,a.L,a.m,tile) > SMEM_MAX)
+  auto smf=[&](int t) {
+    return prec == PREC_F64 ? outerFwdSmem<double>(a.m,t) :
+      outerFwdSmem<float>(a.m,t);
+  };
+  auto smb=[&](int t) {
+    return prec == PREC_F64 ? outerBwdSmem<double>(a.L,a.m,t) :
+      outerBwdSmem<float>(a.L,a.m,t);
+  };
+  a.tile=pickTile(maxTile,C,nbatch*a.q*A,smf);
+  a.tileB=pickTile(maxTile,C,nbatch*B,smb);
+  if(smf(a.tile) > SMEM_MAX || smb(a.tileB) > SMEM_MAX)
     throw std::runtime_error("outer axis too long for shared memory");
-  a.tile=tile;
 }
 
 Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
            const long *mForce, int A, int B, int mult, int prec, long batch)
-  : batch(batch), staging(0), hostIn(NULL), hostOut(NULL), nlaunch(0)
+  : batch(batch), staging(0), hostIn(NULL), hostOut(NULL), nlaunch(0),
+    timing(false), normalize(true), marks(0)
 {
   if(dim < 1 || dim > 3) throw std::runtime_error("dimension must be 1, 2 or 3");
   if(A < 1 || A > FGB_MAXA || B < 1 || B > A)
@@ -316,13 +371,18 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
     if(a.kind == KIND_REAL && d != 0)
       throw std::runtime_error("a real axis must be the outermost");
     a.stored=a.kind == KIND_HERMITIAN ? (long) ceilquotient(a.L,2) : a.L;
-    a.tile=1;
+    a.tile=a.tileB=1;
     a.rows=0;
   }
   if(dim > 1 && batch != 1)
     throw std::runtime_error("batched problems are one-dimensional");
 
-  for(int d=0; d < dim-1; ++d) planOuter(I.axis[d],mForce ? mForce[d] : 0,prec);
+  for(int d=0; d < dim-1; ++d) {
+    long C=1, nb=1;
+    for(int e=d+1; e < dim; ++e) C *= I.axis[e].stored;
+    for(int e=0; e < d; ++e) nb *= I.axis[e].rows;
+    planOuter(I.axis[d],mForce ? mForce[d] : 0,prec,C,nb,A,B);
+  }
   AxisPlan& in=I.axis[dim-1];
   long mf=mForce ? mForce[dim-1] : 0;
   bool ok;
@@ -346,9 +406,9 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
     I.rowQ=N/best;
     in.N=N; in.m=best; in.q=N/best; in.p=ceilquotient(in.L,best);
     in.cshift=0;
-    int tile=prec == PREC_F64 ? 8 : 16;
-    while(tile > 1 && outerNeed(prec,in.p,I.rowQ,tile) > SMEM_MAX) tile /= 2;
-    in.tile=tile;
+    auto sm=[&](int t) {return outerNeed(prec,in.p,I.rowQ,t);};
+    in.tile=pickTile(prec == PREC_F64 ? 8 : 16,I.rowM,A,sm);
+    in.tileB=pickTile(prec == PREC_F64 ? 8 : 16,I.rowM,B,sm);
     if(mForce && mForce[0] > 0)
       throw std::runtime_error("forced m not supported on the long path");
   }
@@ -357,6 +417,7 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
 
 Conv::~Conv()
 {
+  for(cudaEvent_t ev : events) cudaEventDestroy(ev);
   for(void *p : bufs) cudaFree(p);
   if(hostIn) cudaFree(hostIn);
   if(hostOut) cudaFree(hostOut);
@@ -406,6 +467,35 @@ void Conv::allocate()
 
 int Conv::launches() const {return nlaunch;}
 
+cudaError_t Conv::enableTiming(bool on)
+{
+  timing=on;
+  if(on && events.empty()) {
+    events.resize(nlaunch+1);
+    for(auto& ev : events) {
+      cudaError_t e=cudaEventCreate(&ev);
+      if(e != cudaSuccess) return e;
+    }
+  }
+  return cudaSuccess;
+}
+
+void Conv::tick(cudaStream_t s)
+{
+  if(timing && marks < (int) events.size()) cudaEventRecord(events[marks++],s);
+}
+
+int Conv::collect(double *ms, int n)
+{
+  int k=std::min(n,marks-1);
+  for(int i=0; i < k; ++i) {
+    float t=0;
+    if(cudaEventElapsedTime(&t,events[i],events[i+1]) == cudaSuccess)
+      ms[i] += t;
+  }
+  return k;
+}
+
 // ---------------------------------------------------------------------------
 // Launch sequences.
 
@@ -417,7 +507,10 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   const int threads=256;
   cudaError_t e;
   double scale=1.0;
-  for(int d=0; d < I.dim; ++d) scale /= (double) I.axis[d].N;
+  if(normalize)
+    for(int d=0; d < I.dim; ++d) scale /= (double) I.axis[d].N;
+  marks=0;
+  tick(s);
 
   auto rowPlan=[&](RowPlan<T>& P, const AxisPlan& a) {
     P.L=(int) a.stored; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
@@ -448,14 +541,18 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
       for(int i=0; i < A; ++i) P.in[i]=(const Cx *) in[i];
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
       P.rowStride=a.stored; P.nrows=batch; P.scale=(T) scale;
-      return launchHermRow<T>(P,threads,batch,s);
+      e=launchHermRow<T>(P,threads,batch,s);
+      tick(s);
+      return e;
     }
     RowPlan<T> P;
     rowPlan(P,a);
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) in[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
     P.rowStride=a.stored; P.nrows=batch; P.scale=(T) scale;
-    return launchRow<T>(P,threads,batch,s);
+    e=launchRow<T>(P,threads,batch,s);
+    tick(s);
+    return e;
   }
 
   if(I.dim == 1) {  // long 1D complex
@@ -473,6 +570,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.scale=(T) 1;
     for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) bufs[i];}
     e=launchOuterFwd<T>(O,threads,s);
+    tick(s);
     if(e != cudaSuccess) return e;
     AxisPlan ra=a;
     ra.stored=m; ra.L=m; ra.m=m; ra.q=1; ra.N=m; ra.cshift=0;
@@ -482,12 +580,16 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
     P.rowStride=m; P.nrows=q; P.scale=(T) 1;
     e=launchRow<T>(P,threads,q,s);
+    tick(s);
     if(e != cudaSuccess) return e;
     O.count=B;
+    O.tile=a.tileB;
     O.Ltot=a.L;
     O.scale=(T) scale;
     for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) bufs[i]; O.out[i]=(Cx *) out[i];}
-    return launchOuterBwd<T>(O,threads,s);
+    e=launchOuterBwd<T>(O,threads,s);
+    tick(s);
+    return e;
   }
 
   if(I.dim == 2) {
@@ -502,6 +604,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) bufs[i];}
     e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(O,threads,s) :
       launchOuterFwd<T>(O,threads,s);
+    tick(s);
     if(e != cudaSuccess) return e;
     if(ay.kind == KIND_HERMITIAN) {
       HermRowPlan<T> P;
@@ -518,12 +621,16 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
       P.rowStride=C; P.nrows=ax.rows; P.scale=(T) 1;
       e=launchRow<T>(P,threads,ax.rows,s);
     }
+    tick(s);
     if(e != cudaSuccess) return e;
     O.count=B;
+    O.tile=ax.tileB;
     O.scale=(T) scale;
     for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) bufs[i]; O.out[i]=(Cx *) out[i];}
-    return ax.kind == KIND_REAL ? launchOuterRealBwd<T>(O,threads,s) :
+    e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(O,threads,s) :
       launchOuterBwd<T>(O,threads,s);
+    tick(s);
+    return e;
   }
 
   // dim == 3
@@ -543,6 +650,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   for(int i=0; i < A; ++i) {X.in[i]=(const Cx *) in[i]; X.out[i]=(Cx *) bx[i];}
   e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(X,threads,s) :
     launchOuterFwd<T>(X,threads,s);
+  tick(s);
   if(e != cudaSuccess) return e;
 
   OuterPlan<T> Y;
@@ -553,6 +661,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   Y.scale=(T) 1;
   for(int i=0; i < A; ++i) {Y.in[i]=(const Cx *) bx[i]; Y.out[i]=(Cx *) by[i];}
   e=launchOuterFwd<T>(Y,threads,s);
+  tick(s);
   if(e != cudaSuccess) return e;
 
   long nrows=ax.rows*ay.rows;
@@ -571,19 +680,25 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.rowStride=nz; P.nrows=nrows; P.scale=(T) 1;
     e=launchRow<T>(P,threads,nrows,s);
   }
+  tick(s);
   if(e != cudaSuccess) return e;
 
   Y.count=B;
+  Y.tile=ay.tileB;
   for(int i=0; i < B; ++i) {Y.in[i]=(const Cx *) by[i]; Y.out[i]=(Cx *) bx[i];}
   std::swap(Y.inBatch,Y.outBatch);
   e=launchOuterBwd<T>(Y,threads,s);
+  tick(s);
   if(e != cudaSuccess) return e;
 
   X.count=B;
+  X.tile=ax.tileB;
   X.scale=(T) scale;
   for(int i=0; i < B; ++i) {X.in[i]=(const Cx *) bx[i]; X.out[i]=(Cx *) out[i];}
-  return ax.kind == KIND_REAL ? launchOuterRealBwd<T>(X,threads,s) :
+  e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(X,threads,s) :
     launchOuterBwd<T>(X,threads,s);
+  tick(s);
+  return e;
 }
 
 cudaError_t Conv::run(const void *const *in, void *const *out, cudaStream_t s)

@@ -32,7 +32,7 @@ struct AxisPlan {
   long stored;        // values stored along the axis (ceil(L/2) if Hermitian)
   long m, q, N, p;    // residue block length, residues, padded length, folds
   int cshift;         // centred origin offset
-  int tile;           // outer kernels: columns per CTA
+  int tile, tileB;    // outer kernels: columns per CTA (forward, backward)
   long rows;          // outer axis: rows produced (N, or N/2+1 if real)
 };
 
@@ -67,6 +67,15 @@ public:
   int launches() const;            // kernels launched per run()
   size_t stagingBytes() const {return staging;}
 
+  // Optional per-launch timing: when enabled, run() records a CUDA event on
+  // its stream before the first and after every kernel; collect() (after
+  // the stream is synchronised) adds each launch's elapsed time to ms[].
+  cudaError_t enableTiming(bool on);
+  int collect(double *ms, int n);
+
+  // Normalise by 1/prod(N) (Convolution::convolve) or not (convolveRaw).
+  void setNormalize(bool on) {normalize=on;}
+
 private:
   ConvInfo I;
   long batch;
@@ -74,6 +83,11 @@ private:
   size_t staging;
   void *hostIn, *hostOut;          // device copies for runHost
   int nlaunch;
+  bool timing;
+  bool normalize;
+  std::vector<cudaEvent_t> events;
+  int marks;
+  void tick(cudaStream_t s);
   template<typename T> cudaError_t runT(const void *const *in,
                                         void *const *out, cudaStream_t s);
   void allocate();

@@ -69,13 +69,14 @@ class HybridConvolution:
                                           MULT[mult], self.prec, batch)
         if not self.handle:
             raise ValueError(_native.last_error())
-        info = (ctypes.c_long * 27)()
+        info = (ctypes.c_long * 32)()
         self.lib.fgb_info(self.handle, info)
         self.axes = []
         for a in range(d):
             o = info[8 * a: 8 * a + 8]
             self.axes.append(dict(m=o[0], p=o[1], q=o[2], N=o[3], stored=o[4],
-                                  cshift=o[5], tile=o[6], rows=o[7]))
+                                  cshift=o[5], tile=o[6], rows=o[7],
+                                  tileB=info[27 + a]))
         self.launches = info[24]
         self.staging_bytes = info[25]
         self.long_path = bool(info[26])
@@ -144,6 +145,37 @@ class HybridConvolution:
         if rc != 0:
             raise RuntimeError(_native.last_error())
         return list(arrays[:self.B])
+
+    # -- per-kernel timing ---------------------------------------------------
+    def launch_names(self) -> list[str]:
+        """Kernel launched at each position of one convolve call."""
+        k = self.kinds
+        if self.dim == 1:
+            if self.long_path:
+                return ["outer_fwd_cols", "row_conv", "outer_bwd_cols"]
+            return ["herm_row" if k[0] == HERMITIAN else "row_conv"]
+        inner = "herm_row" if k[-1] == HERMITIAN else "row_conv"
+        x = "real" if k[0] == REAL else ""
+        if self.dim == 2:
+            return [f"outer{x}_fwd_x", inner, f"outer{x}_bwd_x"]
+        return [f"outer{x}_fwd_x", "outer_fwd_y", inner, "outer_bwd_y",
+                f"outer{x}_bwd_x"]
+
+    def enable_timing(self, on: bool = True) -> None:
+        if self.lib.fgb_timing(self.handle, int(on)) != 0:
+            raise RuntimeError(_native.last_error())
+        if on:
+            self._ms = [0.0] * self.launches
+
+    def collect_timing(self) -> None:
+        """Accumulate the last call's per-kernel times (stream synchronised)."""
+        buf = (ctypes.c_double * self.launches)(*([0.0] * self.launches))
+        n = self.lib.fgb_timing_collect(self.handle, buf, self.launches)
+        for i in range(max(n, 0)):
+            self._ms[i] += buf[i]
+
+    def kernel_ms(self) -> list[float]:
+        return list(self._ms)
 
     def __del__(self):
         h = getattr(self, "handle", None)

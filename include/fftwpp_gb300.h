@@ -67,9 +67,23 @@ int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out);
 /* Plan parameters: for each axis d, info[8d..8d+7] = m, p, q, N, stored
  * length, centred offset, outer tile, rows produced.  info[24] = kernels per
  * convolution, info[25] = staging bytes, info[26] = 1 if the 1D long path
- * is used.  Mirrors the public members m,p,q,M of fftBase
+ * is used, info[27+d] = backward tile of axis d (info holds 32 longs).  Mirrors the public members m,p,q,M of fftBase
  * (convolve.h:123-145). */
 int fgb_info(const fgb_conv *c, long *info);
+
+/* Normalisation switch: 1 (default) scales the result by 1/prod(m q) as
+ * Convolution::convolve does; 0 returns the unnormalised sum of
+ * Convolution::convolveRaw (convolve.h:1151-1160). */
+int fgb_set_normalize(fgb_conv *c, int normalize);
+
+/* Per-kernel timing (no reference counterpart: the reference times whole
+ * convolutions on the CPU, convolve.cc:177-232).  With timing enabled every
+ * convolve call records a CUDA event on its stream before the first and
+ * after each kernel; after synchronising the stream, fgb_timing_collect
+ * adds the elapsed milliseconds of launch i to ms[i] (i < n) and returns
+ * the number of launches of the last call. */
+int fgb_timing(fgb_conv *c, int enable);
+int fgb_timing_collect(fgb_conv *c, double *ms, int n);
 
 void fgb_destroy(fgb_conv *c);
 

@@ -213,13 +213,17 @@ def main():
                          D or [0] * len(kinds), I or [-1] * len(kinds),
                          mult_for(kinds), src))
             n += 1
-    # Jacobian multiplier (A=4, B=1) on centred-Hermitian 2D data.
+    # Jacobian multiplier (A=4, B=1) on centred-Hermitian 2D data.  Explicit
+    # plans (m = M) are forced: the reference's two-pass schedule (loop2,
+    # convolve.cc:7538-7549 and convolve.h:1487-1498) overwrites the residue-0
+    # product before its backward transform whenever A - B > B, so an
+    # optimiser-chosen 2-pass plan returns a wrong result for A=4, B=1.
     for (Lx, Ly) in ((7, 7), (15, 15)):
         kinds = [CEN, HER]
         Mx, My = 3 * ((Lx + 1) // 2) - 2, 3 * ((Ly + 1) // 2) - 2
         fs = rand_inputs(kinds, [Lx, Ly], 4, seed=77 + Lx)
-        h, info = ref.convolve(fs, kinds, [Lx, Ly], [Mx, My],
-                               mult="realjacobian")
+        h, info = ref.convolve(fs, kinds, [Lx, Ly], [Mx, My], ms=[Mx, My],
+                               Ds=[1, 1], Is=[0, 0], mult="realjacobian")
         key = f"c{n:04d}"
         for a in range(4):
             out[key + f"_in{a}"] = fs[a]

@@ -1,0 +1,116 @@
+"""CPU: the C-ABI library loads, exports every symbol include/*.h declares,
+and its host-side integer rules match the reference's (golden fixtures).
+No compute call is made here; creating a plan without a GPU must fail loudly
+(there is no CPU fallback)."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_exports_every_declared_symbol(native_lib):
+    from fftwpp_gb300 import _native
+    syms = _native.header_symbols()
+    assert len(syms) >= 35
+    missing = [s for s in syms if not hasattr(native_lib, s)]
+    assert not missing, missing
+
+
+def test_reference_abi_names_present(native_lib):
+    # wrappers/cfftw++.cc:27-163
+    for name in ["create_doubleAlign", "delete_doubleAlign",
+                 "create_complexAlign", "delete_complexAlign",
+                 "get_fftwpp_maxthreads", "set_fftwpp_maxthreads",
+                 "fftwpp_create_conv1d", "fftwpp_conv1d_convolve",
+                 "fftwpp_conv1d_delete", "fftwpp_create_hconv1d",
+                 "fftwpp_hconv1d_convolve", "fftwpp_hconv1d_delete",
+                 "fftwpp_HermitianSymmetrize", "fftwpp_create_conv2d",
+                 "fftwpp_conv2d_convolve", "fftwpp_conv2d_delete",
+                 "fftwpp_HermitianSymmetrizeX", "fftwpp_create_hconv2d",
+                 "fftwpp_hconv2d_convolve", "fftwpp_hconv2d_delete",
+                 "fftwpp_create_conv3d", "fftwpp_conv3d_convolve",
+                 "fftwpp_conv3d_delete", "fftwpp_HermitianSymmetrizeXY",
+                 "fftwpp_create_hconv3d", "fftwpp_hconv3d_convolve",
+                 "fftwpp_hconv3d_delete"]:
+        assert hasattr(native_lib, name), name
+
+
+def test_maxthreads_roundtrip(native_lib):
+    old = native_lib.get_fftwpp_maxthreads()
+    native_lib.set_fftwpp_maxthreads(7)
+    assert native_lib.get_fftwpp_maxthreads() == 7
+    native_lib.set_fftwpp_maxthreads(old)
+
+
+def test_parameters_match_reference(native_lib):
+    p = np.load(os.path.join(GOLD, "params.npz"))
+    sz = ctypes.c_size_t
+    a, b, c = sz(), sz(), sz()
+    for L, M, m, cen, pp, nn, qq in p["parameters"][::7]:
+        native_lib.fgb_parameters(int(L), int(M), int(m), int(cen),
+                                  ctypes.byref(a), ctypes.byref(b),
+                                  ctypes.byref(c))
+        assert (a.value, b.value, c.value) == (pp, nn, qq)
+    for m, n in p["nextfftsize"]:
+        assert native_lib.fgb_nextfftsize(int(m)) == n
+
+
+def test_index_matches_reference(native_lib):
+    """fgb_index reproduces fftBase::index on every golden layout."""
+    from test_oracle import LAYOUTS, layout_stream
+    for lay in LAYOUTS:
+        stream, (m, p, q, n, D, D0, centered) = layout_stream(lay)
+        kind = 1 if centered else 0
+        got = [native_lib.fgb_index(kind, m, p, q, n, D, r, k)
+               for r, k in stream]
+        assert np.array_equal(np.array(got), lay["idx"]), lay["key"]
+
+
+def test_hermitian_symmetrize_host(native_lib):
+    """fftwpp_HermitianSymmetrizeX/XY agree with the oracle's restatement
+    of convolve.h:1175-1258."""
+    from oracle import hybrid as H
+    rng = np.random.default_rng(4)
+    for Lx, Hy in ((7, 4), (8, 5)):
+        f = rng.normal(size=(Lx, Hy)) + 1j * rng.normal(size=(Lx, Hy))
+        g = f.copy()
+        native_lib.fftwpp_HermitianSymmetrizeX((Lx + 1) // 2, Hy, Lx // 2,
+                                               ctypes.c_void_p(f.ctypes.data))
+        H.hermitian_symmetrize_x(g, (Lx + 1) // 2, Hy, Lx // 2)
+        assert np.array_equal(f, g)
+    for Lx, Ly, Hz in ((5, 5, 3), (6, 4, 2)):
+        f = rng.normal(size=(Lx, Ly, Hz)) + 1j * rng.normal(size=(Lx, Ly, Hz))
+        g = f.copy()
+        native_lib.fftwpp_HermitianSymmetrizeXY(
+            (Lx + 1) // 2, (Ly + 1) // 2, Hz, Lx // 2, Ly // 2,
+            ctypes.c_void_p(f.ctypes.data))
+        H.hermitian_symmetrize_xy(g, (Lx + 1) // 2, (Ly + 1) // 2, Hz,
+                                  Lx // 2, Ly // 2)
+        assert np.array_equal(f, g)
+
+
+def test_no_cpu_fallback(native_lib):
+    """Without a GPU, planning fails with an error instead of computing on
+    the host."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    sz = ctypes.c_size_t
+    k = (ctypes.c_int * 1)(0)
+    L = (sz * 1)(16)
+    M = (sz * 1)(31)
+    h = native_lib.fgb_create(1, k, L, M, None, 2, 1, 1, 0, 1)
+    assert not h
+    from fftwpp_gb300 import _native
+    assert _native.last_error()
+
+
+def test_missing_library_is_loud(tmp_path, monkeypatch):
+    from fftwpp_gb300 import _native
+    monkeypatch.setattr(_native, "LIB_PATH", str(tmp_path / "absent.so"))
+    monkeypatch.setattr(_native, "_lib", None)
+    with pytest.raises(_native.NativeLibraryMissing):
+        _native.load()

@@ -1,0 +1,186 @@
+"""GPU: the reference-facing boundaries against the CPU oracle --
+the C++ class set (include/convolve.h, driven by tests/cpp/api_driver.cc the
+way the reference's test programs wire it), the FFTW++ C ABI through the
+Python mirror of wrappers/fftwpp.py, and the golden reference outputs."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import hybrid as H
+from oracle.direct import directconv, directconvh2, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def api_driver(native_lib, tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("api") / "api_driver")
+    lib_dir = os.path.join(ROOT, "fftwpp_gb300")
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "cpp", "api_driver.cc"), "-L", lib_dir,
+           "-l:lib_fftwpp.so", f"-Wl,-rpath,{lib_dir}", "-o", exe]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def _run(exe, case, fs, L, M, tmp_path):
+    A = len(fs)
+    inp = tmp_path / "in.bin"
+    out = tmp_path / "out.bin"
+    np.concatenate([np.ascontiguousarray(f).view(np.float64).ravel()
+                    for f in fs]).tofile(inp)
+    subprocess.run([exe, case, str(A), str(inp), str(out), *map(str, L),
+                    *map(str, M)], check=True)
+    raw = np.fromfile(out, dtype=np.float64)
+    if fs[0].dtype == np.complex128:
+        return raw.view(np.complex128).reshape(fs[0].shape)
+    return raw.reshape(fs[0].shape)
+
+
+def _inputs(kinds, L, A, seed):
+    rng = np.random.default_rng(seed)
+    shape = list(L)
+    if kinds[-1] == H.HERMITIAN:
+        shape[-1] = (L[-1] + 1) // 2
+    out = []
+    for _ in range(A):
+        if kinds[0] == H.REAL:
+            f = rng.normal(size=shape)
+        else:
+            f = rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+        if kinds[-1] == H.HERMITIAN and len(kinds) == 2:
+            H.hermitian_symmetrize_x(f, (L[0] + 1) // 2, shape[1], L[0] // 2)
+        if kinds[-1] == H.HERMITIAN and len(kinds) == 1:
+            f[0] = f[0].real
+        if kinds[-1] == H.HERMITIAN and len(kinds) == 3:
+            H.hermitian_symmetrize_xy(f, (L[0] + 1) // 2, (L[1] + 1) // 2,
+                                      shape[2], L[0] // 2, L[1] // 2)
+        out.append(np.ascontiguousarray(f))
+    return out
+
+
+API_CASES = [
+    ("pad1", [H.PAD], [64], [127], "binary"),
+    ("cen1", [H.CENTERED], [63], [94], "binary"),
+    ("her1", [H.HERMITIAN], [63], [94], "realbinary"),
+    ("real1", [H.REAL], [64], [127], "binary"),
+    ("pad2", [H.PAD, H.PAD], [16, 12], [31, 23], "binary"),
+    ("her2", [H.CENTERED, H.HERMITIAN], [31, 31], [46, 46], "realbinary"),
+    ("real2", [H.REAL, H.PAD], [16, 12], [31, 23], "binary"),
+    ("pad3", [H.PAD, H.PAD, H.PAD], [6, 5, 4], [11, 9, 7], "binary"),
+    ("real3", [H.REAL, H.PAD, H.PAD], [6, 5, 4], [11, 9, 7], "binary"),
+    ("her3", [H.CENTERED, H.CENTERED, H.HERMITIAN], [7, 7, 7], [10, 10, 10],
+     "realbinary"),
+]
+
+
+@pytest.mark.parametrize("case", API_CASES, ids=[c[0] for c in API_CASES])
+def test_cpp_api(case, api_driver, tmp_path):
+    name, kinds, L, M, mult = case
+    fs = _inputs(kinds, L, 2, seed=len(L) * 100 + L[0])
+    got = _run(api_driver, name, fs, L, M, tmp_path)
+    want = H.convolve(fs, kinds, L, M, mult=mult)[0]
+    assert rel_l2(got, want) <= 1e-13
+
+
+def test_cpp_api_raw_and_jacobian(api_driver, tmp_path):
+    fs = _inputs([H.PAD], [50], 2, seed=9)
+    raw = _run(api_driver, "raw1", fs, [50], [99], tmp_path)
+    want = H.convolve(fs, [H.PAD], [50], [99])[0]
+    assert rel_l2(raw, want) <= 1e-13
+    kinds, L, M = [H.CENTERED, H.HERMITIAN], [15, 15], [22, 22]
+    fs = _inputs(kinds, L, 4, seed=12)
+    got = _run(api_driver, "jac2", fs, L, M, tmp_path)
+    want = H.convolve(fs, kinds, L, M, mult="realjacobian")[0]
+    assert rel_l2(got, want) <= 1e-13
+
+
+def test_python_wrapper_convolution(native_lib):
+    """fftwpp_gb300.fftwpp.Convolution: the reference's Python API
+    (wrappers/fftwpp.py:84-223), checked against the direct sum."""
+    from fftwpp_gb300 import fftwpp
+    N = 8
+    f = fftwpp.complex_align([N])
+    g = fftwpp.complex_align([N])
+    for i in range(N):
+        f[i] = complex(i + 1, i + 3)
+        g[i] = complex(i + 2, 2 * i + 3)
+    want = directconv(f.copy(), g.copy())
+    c = fftwpp.Convolution(f.shape)
+    c.convolve(f, g)
+    assert rel_l2(f, want) <= 1e-13
+    for shape in [(4, 4), (4, 4, 4), (33, 17)]:
+        rng = np.random.default_rng(len(shape))
+        f = rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+        g = rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+        kinds = [H.PAD] * len(shape)
+        want = H.convolve([f, g], kinds, list(shape),
+                          [2 * s - 1 for s in shape])[0]
+        c = fftwpp.Convolution(shape)
+        c.convolve(f, g)
+        assert rel_l2(f, want) <= 1e-13
+
+
+def test_python_wrapper_hconvolution(native_lib):
+    """fftwpp_gb300.fftwpp.HConvolution symmetrises then convolves
+    (wrappers/fftwpp.py:316-349)."""
+    from fftwpp_gb300 import fftwpp
+    Nx, Ny = 4, 4
+    f = fftwpp.complex_align([2 * Nx - 1, Ny])
+    g = fftwpp.complex_align([2 * Nx - 1, Ny])
+    for i in range(len(f)):
+        for j in range(len(f[i])):
+            f[i][j] = complex(i + 1, j + 3)
+            g[i][j] = complex(i + 2, 2 * j + 3)
+    c = fftwpp.HConvolution(f.shape)
+    fs, gs = f.copy(), g.copy()
+    H.hermitian_symmetrize_x(fs, Nx, Ny, Nx - 1)
+    H.hermitian_symmetrize_x(gs, Nx, Ny, Nx - 1)
+    want = directconvh2(fs, gs, True)
+    c.convolve(f, g)
+    assert rel_l2(f, want) <= 1e-13
+    # 1D and 3D
+    rng = np.random.default_rng(3)
+    h = rng.uniform(-1, 1, 6) + 1j * rng.uniform(-1, 1, 6)
+    k = rng.uniform(-1, 1, 6) + 1j * rng.uniform(-1, 1, 6)
+    want = H.convolve([h.copy(), k.copy()], [H.HERMITIAN], [11],
+                      [H.default_M(H.HERMITIAN, 11)], mult="realbinary")[0]
+    c1 = fftwpp.HConvolution(6)
+    c1.convolve(h, k)
+    assert rel_l2(h, want) <= 1e-13
+    sh = (5, 5, 3)
+    u = rng.uniform(-1, 1, sh) + 1j * rng.uniform(-1, 1, sh)
+    v = rng.uniform(-1, 1, sh) + 1j * rng.uniform(-1, 1, sh)
+    us, vs = u.copy(), v.copy()
+    for a in (us, vs):
+        H.hermitian_symmetrize_xy(a, 3, 3, 3, 2, 2)
+    want = H.convolve([us, vs], [H.CENTERED, H.CENTERED, H.HERMITIAN],
+                      [5, 5, 5], [7, 7, 7], mult="realbinary")[0]
+    c3 = fftwpp.HConvolution(sh)
+    c3.convolve(u, v)
+    assert rel_l2(u, want) <= 1e-13
+
+
+def test_golden_reference_outputs(native_lib):
+    """The GPU result equals the reference's own output (tests/golden/) on
+    every fixture: FP64 <= 1e-13, FP32-compensated <= 2e-6 relative L2."""
+    import torch
+    from fftwpp_gb300.gpu import HybridConvolution
+    from test_oracle import CASES
+    seen = 0
+    for c in CASES:
+        A = len(c["ins"])
+        for prec, tol in (("f64", 1e-13), ("f32", 2e-6)):
+            conv = HybridConvolution(c["kinds"], c["L"], c["M"], A=A, B=1,
+                                     mult=c["mult"], precision=prec)
+            ts = [torch.from_numpy(np.ascontiguousarray(f)).to(conv.dtype)
+                  .cuda() for f in c["ins"]]
+            got = conv.convolve(*ts)[0].cpu().numpy()
+            err = rel_l2(got, c["out"])
+            assert err <= tol, (c["key"], prec, err)
+        seen += 1
+    assert seen >= 500

@@ -1,0 +1,181 @@
+"""CPU: pin the oracle (numpy restatement + direct sums) to the reference's
+own outputs stored in tests/golden/ (generated by tests/golden/make_golden.py
+from FFTW++ compiled from its sources)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import direct as Dr
+from oracle import hybrid as H
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_cases():
+    data = np.load(os.path.join(GOLD, "conv_cases.npz"))
+    rows = []
+    for line in open(os.path.join(GOLD, "conv_cases.txt")):
+        if line.startswith("#"):
+            continue
+        key, kinds, L, M, m, D, I, mult, src = line.split()
+        ev = eval  # literal lists written by make_golden.py
+        A = 4 if mult == "realjacobian" else 2
+        ins = [data[f"{key}_in{a}"] for a in range(A)]
+        rows.append(dict(key=key, kinds=ev(kinds), L=ev(L), M=ev(M), m=ev(m),
+                         mult=mult, src=src, ins=ins, out=data[f"{key}_out"],
+                         info=data[f"{key}_info"]))
+    return rows
+
+
+CASES = load_cases()
+
+
+def test_fixture_count():
+    assert len(CASES) >= 500
+
+
+@pytest.mark.parametrize("idx", range(0, len(CASES), 1))
+def test_oracle_matches_reference(idx):
+    c = CASES[idx]
+    got = H.convolve(c["ins"], c["kinds"], c["L"], c["M"], mult=c["mult"])[0]
+    err = Dr.rel_l2(got, c["out"])
+    # The reference's own test tolerance is 1e-12 (tests/tests.py:223-224).
+    assert err < 1e-12, (c["key"], err)
+
+
+def test_oracle_forced_m_matches_reference():
+    """The residue decomposition with the reference's chosen (m, q)
+    reproduces the reference's output."""
+    n = 0
+    for c in CASES:
+        if len(c["kinds"]) != 1:
+            continue
+        m = int(c["info"][0][0])
+        got = H.convolve(c["ins"], c["kinds"], c["L"], c["M"], ms=[m],
+                         mult=c["mult"])[0]
+        assert Dr.rel_l2(got, c["out"]) < 1e-12, c["key"]
+        n += 1
+    assert n > 100
+
+
+def _direct(c):
+    kinds, f, g = c["kinds"], c["ins"][0], c["ins"][1]
+    if kinds == [H.PAD] or kinds == [H.REAL]:
+        return Dr.directconv(f, g)
+    if kinds == [H.CENTERED]:
+        return Dr.directconv_c(f, g)
+    if kinds == [H.HERMITIAN]:
+        return Dr.directconvh(f, g)
+    if kinds in ([H.PAD, H.PAD], [H.REAL, H.PAD]):
+        return Dr.directconv2(f, g)
+    if kinds == [H.CENTERED, H.HERMITIAN] and c["L"][1] % 2 == 1:
+        return Dr.directconvh2(f, g, c["L"][0] % 2 == 1)
+    if kinds in ([H.PAD, H.PAD, H.PAD], [H.REAL, H.PAD, H.PAD]):
+        return Dr.directconv3(f, g)
+    return None
+
+
+def test_reference_matches_direct_sums():
+    """The reference (with the clean-room FFT backend) against the
+    reference's own O(L^d) direct oracles (tests/direct.cc)."""
+    n = 0
+    for c in CASES:
+        if c["mult"] not in ("binary", "realbinary"):
+            continue
+        d = _direct(c)
+        if d is None:
+            continue
+        assert Dr.rel_l2(c["out"], d) < 1e-12, c["key"]
+        n += 1
+    assert n > 300
+
+
+def test_known_answer():
+    """tests/hybridconv.cc:50-69: f_j = iF e^{ij}, g_j = iG e^{ij} gives
+    h_j = iF iG (j+1) e^{ij}."""
+    kat = np.load(os.path.join(GOLD, "kat.npz"))
+    for L in (64, 256, 1024, 4096):
+        exact = kat[f"L{L}_exact"]
+        assert Dr.rel_l2(kat[f"L{L}_ref"], exact) < 1e-12
+        iF = complex(np.sqrt(3.0), np.sqrt(7.0))
+        iG = complex(np.sqrt(5.0), np.sqrt(11.0))
+        j = np.arange(L)
+        e = np.exp(1j * j)
+        got = H.convolve([iF * e, iG * e], [H.PAD], [L], [2 * L])[0]
+        assert Dr.rel_l2(got, exact) < 1e-12
+
+
+def test_parameters_and_nextfftsize():
+    p = np.load(os.path.join(GOLD, "params.npz"))
+    for L, M, m, c, pp, nn, qq in p["parameters"]:
+        assert H.parameters(int(L), int(M), int(m), bool(c)) == (pp, nn, qq)
+    for m, n in p["nextfftsize"]:
+        assert H.nextfftsize(int(m)) == n
+
+
+def load_layouts():
+    data = np.load(os.path.join(GOLD, "layouts.npz"))
+    rows = []
+    for line in open(os.path.join(GOLD, "layouts.txt")):
+        if line.startswith("#"):
+            continue
+        key, kind, L, M, m, D, I = line.split()
+        rows.append(dict(key=key, kind=int(kind), L=int(L), M=int(M),
+                         F=data[key + "_F"], idx=data[key + "_idx"],
+                         info=data[key + "_info"]))
+    return rows
+
+
+LAYOUTS = load_layouts()
+
+
+def layout_stream(lay):
+    """(r, k) pairs in the order the reference emits them: residue blocks
+    r += increment(r) (convolve.h:394-396), entries k < noutputs(r)
+    (convolve.h:435-437) with blocksize l = m*P (convolve.cc:549-557)."""
+    m, p, q, n, D, I, R, N = [int(x) for x in lay["info"]]
+    centered = lay["kind"] == H.CENTERED
+    if q == 1:
+        return [(0, k) for k in range(N)], (m, p, q, n, 1, 1, centered)
+    if centered:
+        conj = D > 1 and (p == 1 or p % 2 == 0)      # convolve.h:653
+        P = 1 if p == 2 else p // 2
+    else:
+        conj = D > 1 and p <= 2                      # convolve.h:384-386
+        P = 1 if p == 2 else p
+    D0 = n % D or D
+    dr = D // 2 if conj else D
+    out = []
+    r = 0
+    while r < R:
+        for k in range(m * P * (D0 if r == 0 else D)):
+            out.append((r, k))
+        r += dr if r > 0 else ((D0 + 1) // 2 if conj else D0)
+    return out, (m, p, q, n, D, D0, centered)
+
+
+def test_layout_index_map():
+    """fftBase::index restated in the oracle reproduces the reference's
+    transformed index of every entry of every residue block."""
+    for lay in LAYOUTS:
+        stream, (m, p, q, n, D, D0, centered) = layout_stream(lay)
+        assert len(stream) == len(lay["idx"]), lay["key"]
+        got = [H.index_base(r, k, m=m, p=p, q=q, n=n, D=D, D0=D0,
+                            centered=centered) for r, k in stream]
+        assert np.array_equal(np.array(got), lay["idx"]), lay["key"]
+
+
+def test_layout_values_are_padded_dft():
+    """Every forward output F of residue block entry k equals the explicit
+    padded DFT (FFTW sign +1) at the transformed index idx[k]; centred data
+    carries the extra phase of its origin offset floor(L/2)."""
+    for lay in LAYOUTS:
+        L, kind = lay["L"], lay["kind"]
+        N = int(lay["info"][7])
+        f = (np.arange(L) + 1) + 1j * (np.arange(L) + 2)
+        s = np.arange(L)
+        c = L // 2 if kind == H.CENTERED else 0
+        k = lay["idx"]
+        full = np.exp(2j * np.pi * (np.outer(k, s - c) % N) / N) @ f
+        assert Dr.rel_l2(lay["F"], full) < 1e-12, lay["key"]
