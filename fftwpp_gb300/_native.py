@@ -53,6 +53,21 @@ def load():
     lib.fgb_timing.argtypes = [vp, ctypes.c_int]
     lib.fgb_timing_collect.restype = ctypes.c_int
     lib.fgb_timing_collect.argtypes = [vp, P(ctypes.c_double), ctypes.c_int]
+    lib.fgb_batch_create.restype = vp
+    lib.fgb_batch_create.argtypes = [ctypes.c_int, P(sz), P(sz), ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int]
+    lib.fgb_batch_convolve_device.restype = ctypes.c_int
+    lib.fgb_batch_convolve_device.argtypes = [vp, P(vp), P(vp), vp,
+                                              ctypes.c_int]
+    lib.fgb_batch_info.restype = ctypes.c_int
+    lib.fgb_batch_info.argtypes = [vp, P(ctypes.c_long)]
+    lib.fgb_batch_choice.restype = ctypes.c_long
+    lib.fgb_batch_choice.argtypes = [vp, ctypes.c_int]
+    lib.fgb_batch_error.restype = ctypes.c_int
+    lib.fgb_batch_error.argtypes = [vp]
+    lib.fgb_batch_destroy.restype = None
+    lib.fgb_batch_destroy.argtypes = [vp]
     lib.fgb_destroy.restype = None
     lib.fgb_destroy.argtypes = [vp]
     lib.fgb_last_error.restype = ctypes.c_char_p

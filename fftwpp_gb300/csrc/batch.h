@@ -1,0 +1,61 @@
+// batch.h -- many independent 1D convolutions of uneven lengths in one
+// persistent launch (kernels.cuh, BatchArgs), optionally replayed from a
+// captured CUDA graph.
+#pragma once
+
+#include "engine.h"
+
+#include <vector>
+
+namespace fgb {
+
+class BatchConv {
+public:
+  // n problems of lengths L[i] padded to >= M[i]; data packed back to back
+  // in every input/output array.  choice: NULL or per-problem plan
+  // (> 0 residue block m of a one-CTA problem, < 0 minus the row length of
+  // a long problem); tune: time the candidate plans (autotuner).
+  BatchConv(int n, const long *L, const long *M, const long *choice, int A,
+            int B, int mult, int prec, int kind, bool tune);
+  ~BatchConv();
+
+  cudaError_t run(const void *const *in, void *const *out, cudaStream_t s);
+  // Capture the launch (counter reset + persistent kernel) once per set of
+  // array pointers and replay the graph on s.
+  cudaError_t runGraph(const void *const *in, void *const *out,
+                       cudaStream_t s);
+  // Nonzero if a bounded wait inside the kernel gave up (reading clears it).
+  int error();
+
+  long choice(int i) const;
+  int tasks() const {return ntasks;}
+  int gridSize() const {return grid;}
+  size_t smemBytes() const {return smem;}
+  long totalLength() const {return total;}
+  int shortProblems() const {return nsmall;}
+  int longProblems() const {return nlong;}
+
+  static std::vector<long> candidates(long L, long M, int A, int B, int prec,
+                                      size_t budget);
+
+private:
+  int n, A, B, mult, prec, kind;
+  std::vector<long> Ls, Ms, offsets, choices;
+  long total;
+  void *dProbs, *dTasks, *dCounters, *staging;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+  cudaStream_t captureStream;
+  std::vector<const void *> graphKey;
+  size_t smem, budget;
+  int grid;
+  size_t stagingSize;
+  int ntasks, nsmall, nlong;
+
+  long tuned(long L, long M, const std::vector<long>& cand);
+  template<typename T> void build();
+  template<typename T> cudaError_t launch(const void *const *in,
+                                          void *const *out, cudaStream_t s);
+};
+
+} // namespace fgb

@@ -1,5 +1,6 @@
 // capi.cu -- C ABI of lib_fftwpp.so: the FFTW++-compatible entry points of
 // include/cfftw++.h and the device-pointer API of include/fftwpp_gb300.h.
+#include "batch.h"
 #include "engine.h"
 #include "kernels.cuh"
 
@@ -377,6 +378,67 @@ int fgb_timing_collect(fgb_conv *c, double *ms, int n)
 }
 
 void fgb_destroy(fgb_conv *c) {destroy(c);}
+
+// ---------------------------------------------------------------------------
+// Batched uneven 1D convolutions (include/fftwpp_gb300.h).
+
+struct fgb_batch {
+  std::unique_ptr<BatchConv> b;
+};
+
+fgb_batch *fgb_batch_create(int n, const size_t *L, const size_t *M, int A,
+                            int B, int mult, int precision, int kind,
+                            int tune)
+{
+  if(n < 1 || !L || !M) {report("fgb_batch_create","bad arguments"); return NULL;}
+  try {
+    std::vector<long> Ls(L,L+n), Ms(M,M+n);
+    fgb_batch *h=new fgb_batch;
+    h->b.reset(new BatchConv(n,Ls.data(),Ms.data(),NULL,A,B,mult,precision,
+                             kind,tune != 0));
+    return h;
+  } catch(std::exception& e) {
+    report("fgb_batch_create",e.what());
+    return NULL;
+  }
+}
+
+int fgb_batch_convolve_device(fgb_batch *h, void *const *in, void *const *out,
+                              void *stream, int use_graph)
+{
+  if(!h || !in || !out) {report("fgb_batch_convolve_device","bad arguments"); return -1;}
+  cudaError_t e=use_graph ? h->b->runGraph(in,out,(cudaStream_t) stream) :
+    h->b->run(in,out,(cudaStream_t) stream);
+  if(e != cudaSuccess) {
+    report("fgb_batch_convolve_device",cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
+int fgb_batch_info(const fgb_batch *h, long *info)
+{
+  if(!h || !info) return -1;
+  info[0]=h->b->tasks();
+  info[1]=h->b->gridSize();
+  info[2]=(long) h->b->smemBytes();
+  info[3]=h->b->shortProblems();
+  info[4]=h->b->longProblems();
+  info[5]=h->b->totalLength();
+  return 0;
+}
+
+long fgb_batch_choice(const fgb_batch *h, int i)
+{
+  return h ? h->b->choice(i) : 0;
+}
+
+int fgb_batch_error(fgb_batch *h)
+{
+  return h ? h->b->error() : -1;
+}
+
+void fgb_batch_destroy(fgb_batch *h) {delete h;}
 
 const char *fgb_last_error(void)
 {

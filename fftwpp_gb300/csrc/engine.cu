@@ -163,6 +163,8 @@ static FFTPlanDev fftPlan(long n, int prec)
   return p;
 }
 
+FFTPlanDev fftPlanPublic(long n, int prec) {return fftPlan(n,prec);}
+
 // ---------------------------------------------------------------------------
 // Planning.
 

@@ -75,11 +75,34 @@ __device__ __forceinline__ int posmod(int a, int m)
 // axis): fold + pre-twiddle (forwardInner: Zetaqp/Zetaqm), m-point FFT, fused
 // multiplier, inverse FFT, post-twiddle and accumulation over residues
 // (backwardInner), normalisation (Convolution::normalize).
-template<typename T>
-__global__ void __launch_bounds__(256)
-rowConvKernel(const RowPlan<T> P)
+// Load of data another CTA of the same launch may have written: CG bypasses
+// the (non-coherent) L1 with ld.global.cg.
+template<bool CG>
+__device__ __forceinline__ cplx<double> ldx(const cplx<double> *p)
 {
-  extern __shared__ __align__(16) unsigned char smemRaw[];
+  if(CG) {
+    double2 v=__ldcg((const double2 *) p);
+    return mk(v.x,v.y);
+  }
+  return *p;
+}
+
+template<bool CG>
+__device__ __forceinline__ cplx<float> ldx(const cplx<float> *p)
+{
+  if(CG) {
+    float2 v=__ldcg((const float2 *) p);
+    return mk(v.x,v.y);
+  }
+  return *p;
+}
+
+// One row of the complex row convolution (all residues), using the block's
+// shared memory.  Every thread of the block calls it.
+template<typename T, bool CG>
+__device__ __forceinline__ void rowConvRow(const RowPlan<T>& P, long long row,
+                                           unsigned char *smemRaw)
+{
   const int A=P.A, B=P.B, L=P.L, m=P.m, N=P.N, c=P.cshift;
   cplx<T> *fin=(cplx<T> *) smemRaw;
   cplx<T> *acc=fin+A*L;
@@ -88,12 +111,12 @@ rowConvKernel(const RowPlan<T> P)
   const int tid=threadIdx.x, nthr=blockDim.x;
   const typename TwT<T>::type *tw=P.twN;
 
-  for(long long row=blockIdx.x; row < P.nrows; row += gridDim.x) {
+  {
     long long base=row*P.rowStride;
     for(int i=tid; i < A*L; i += nthr) {
       int a=i/L, s=i-a*L;
       fin[i]=P.realIO ? mk(((const T *) P.in[a])[base+s],(T) 0) :
-        P.in[a][base+s];
+        ldx<CG>(P.in[a]+base+s);
     }
     for(int i=tid; i < B*L; i += nthr) acc[i]=mk((T) 0,(T) 0);
     __syncthreads();
@@ -138,6 +161,15 @@ rowConvKernel(const RowPlan<T> P)
     }
     __syncthreads();
   }
+}
+
+template<typename T>
+__global__ void __launch_bounds__(256)
+rowConvKernel(const RowPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  for(long long row=blockIdx.x; row < P.nrows; row += gridDim.x)
+    rowConvRow<T,false>(P,row,smemRaw);
 }
 
 // ---------------------------------------------------------------------------
@@ -208,19 +240,18 @@ hermRowKernel(const HermRowPlan<T> P)
 // ---------------------------------------------------------------------------
 // Outer forward, complex data: residue block r of the padded transform along
 // a strided axis for `tile` adjacent columns.
-template<typename T>
-__global__ void __launch_bounds__(256)
-outerFwdKernel(const OuterPlan<T> P)
+template<typename T, bool CG>
+__device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
+                                             int r, int z,
+                                             unsigned char *smemRaw)
 {
-  extern __shared__ __align__(16) unsigned char smemRaw[];
   const int tile=P.tile, m=P.m, N=P.N, c=P.cshift, L=P.L;
   cplx<T> *x=(cplx<T> *) smemRaw;
   cplx<T> *y=x+m*tile;
   const int tid=threadIdx.x, nthr=blockDim.x;
-  const int col0=blockIdx.x*tile;
-  const int r=blockIdx.y;
-  const int a=blockIdx.z % P.count;
-  const long long batch=blockIdx.z/P.count;
+  const int col0=ctile*tile;
+  const int a=z % P.count;
+  const long long batch=z/P.count;
   const cplx<T> *src=P.in[a]+batch*P.inBatch;
   cplx<T> *dst=P.out[a]+batch*P.outBatch;
   const typename TwT<T>::type *tw=P.twN;
@@ -234,7 +265,7 @@ outerFwdKernel(const OuterPlan<T> P)
       for(int s=s0; s < L; s += m) {
         long long off=(long long) s*P.inRow+col;
         if(off >= P.Ltot) break;
-        cplx<T> v=src[off];
+        cplx<T> v=ldx<CG>(src+off);
         if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
         sum=sum+v;
       }
@@ -257,22 +288,30 @@ outerFwdKernel(const OuterPlan<T> P)
       dst[k*P.outRow+col]=v;
     }
   }
+  __syncthreads();
+}
+
+template<typename T>
+__global__ void __launch_bounds__(256)
+outerFwdKernel(const OuterPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  outerFwdTile<T,false>(P,blockIdx.x,blockIdx.y,blockIdx.z,smemRaw);
 }
 
 // Outer backward, complex data: all residues of a column tile, accumulated.
-template<typename T>
-__global__ void __launch_bounds__(256)
-outerBwdKernel(const OuterPlan<T> P)
+template<typename T, bool CG>
+__device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
+                                             int z, unsigned char *smemRaw)
 {
-  extern __shared__ __align__(16) unsigned char smemRaw[];
   const int tile=P.tile, m=P.m, N=P.N, c=P.cshift, L=P.L;
   cplx<T> *acc=(cplx<T> *) smemRaw;
   cplx<T> *x=acc+L*tile;
   cplx<T> *y=x+m*tile;
   const int tid=threadIdx.x, nthr=blockDim.x;
-  const int col0=blockIdx.x*tile;
-  const int b=blockIdx.z % P.count;
-  const long long batch=blockIdx.z/P.count;
+  const int col0=ctile*tile;
+  const int b=z % P.count;
+  const long long batch=z/P.count;
   const cplx<T> *src=P.in[b]+batch*P.inBatch;
   cplx<T> *dst=P.out[b]+batch*P.outBatch;
   const typename TwT<T>::type *tw=P.twN;
@@ -285,7 +324,7 @@ outerBwdKernel(const OuterPlan<T> P)
       cplx<T> v=mk((T) 0,(T) 0);
       if(col < P.C) {
         long long k=(long long) r*m+j;
-        v=src[k*P.inRow+col];
+        v=ldx<CG>(src+k*P.inRow+col);
         if(P.twX) {
           unsigned long long e=((unsigned long long) col*(unsigned long long) k)
             % (unsigned long long) P.NX;
@@ -311,6 +350,15 @@ outerBwdKernel(const OuterPlan<T> P)
     long long off=(long long) s*P.outRow+col;
     if(col < P.C && off < P.Ltot) dst[off]=acc[i]*P.scale;
   }
+  __syncthreads();
+}
+
+template<typename T>
+__global__ void __launch_bounds__(256)
+outerBwdKernel(const OuterPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  outerBwdTile<T,false>(P,blockIdx.x,blockIdx.z,smemRaw);
 }
 
 // ---------------------------------------------------------------------------
@@ -411,6 +459,117 @@ outerRealBwdKernel(const OuterPlan<T> P)
     if(s < L) dst[(long long) s*P.outRow+col]=v.x;
     if(s+1 < L) dst[(long long) (s+1)*P.outRow+col]=v.y;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent batched kernel (see kernels.cuh).
+
+template<typename T, template<typename> class Plan>
+__device__ __forceinline__ void rebase(Plan<T>& plan, int count, bool relIn,
+                                       bool relOut, void *const *inBase,
+                                       void *const *outBase)
+{
+  for(int a=0; a < count; ++a) {
+    if(relIn)
+      plan.in[a]=(const cplx<T> *) ((char *) inBase[a]+(size_t) plan.in[a]);
+    if(relOut)
+      plan.out[a]=(cplx<T> *) ((char *) outBase[a]+(size_t) plan.out[a]);
+  }
+}
+
+template<typename T>
+__global__ void __launch_bounds__(256)
+batchKernel(const BatchArgs<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  __shared__ int slot;
+  __shared__ int gaveUp;
+  for(;;) {
+    if(threadIdx.x == 0) slot=atomicAdd(P.queue,1);
+    __syncthreads();
+    const int t=slot;
+    __syncthreads();
+    if(t >= P.ntasks) return;
+    const BatchTask tk=P.tasks[t];
+    const BatchProblem<T> *B=P.probs+tk.prob;
+    if(tk.type == TASK_ROW || tk.type == TASK_COLBWD) {
+      if(threadIdx.x == 0) {
+        volatile int *d=P.done+2*tk.prob+(tk.type == TASK_ROW ? 0 : 1);
+        const int target=tk.type == TASK_ROW ? B->nfwd : B->nrows;
+        long long it=0;
+        gaveUp=0;
+        while(*d < target) {
+          if(++it > P.spinLimit) {
+            gaveUp=1;
+            atomicExch(P.err,1);
+            break;
+          }
+          __nanosleep(100);
+        }
+        __threadfence();
+      }
+      __syncthreads();
+      if(gaveUp) continue;
+    }
+    switch(tk.type) {
+      case TASK_SMALL: {
+        RowPlan<T> R=B->row;
+        rebase(R,R.A,B->rel & 1,B->rel & 2,P.inBase,P.outBase);
+        rowConvRow<T,false>(R,tk.i,smemRaw);
+        break;
+      }
+      case TASK_COLFWD: {
+        OuterPlan<T> O=B->fwd;
+        rebase(O,O.count,B->rel & 4,false,P.inBase,P.outBase);
+        outerFwdTile<T,false>(O,tk.i,0,tk.j,smemRaw);
+        break;
+      }
+      case TASK_ROW: {
+        RowPlan<T> R=B->row;
+        rowConvRow<T,true>(R,tk.i,smemRaw);
+        break;
+      }
+      default: {
+        OuterPlan<T> O=B->bwd;
+        rebase(O,O.count,false,B->rel & 8,P.inBase,P.outBase);
+        outerBwdTile<T,true>(O,tk.i,tk.j,smemRaw);
+        break;
+      }
+    }
+    if(tk.type == TASK_COLFWD || tk.type == TASK_ROW) {
+      __threadfence();
+      __syncthreads();
+      if(threadIdx.x == 0)
+        atomicAdd(P.done+2*tk.prob+(tk.type == TASK_COLFWD ? 0 : 1),1);
+    }
+  }
+}
+
+template<typename T>
+cudaError_t launchBatch(const BatchArgs<T>& P, int grid, int threads,
+                        size_t smem, cudaStream_t s)
+{
+  if(smem > 48*1024) {
+    cudaError_t e=cudaFuncSetAttribute(batchKernel<T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int) smem);
+    if(e != cudaSuccess) return e;
+  }
+  batchKernel<T><<<grid,threads,smem,s>>>(P);
+  return cudaGetLastError();
+}
+
+template<typename T>
+int batchBlocksPerSM(int threads, size_t smem)
+{
+  if(smem > 48*1024)
+    cudaFuncSetAttribute(batchKernel<T>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,(int) smem);
+  int n=0;
+  if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n,batchKernel<T>,threads,
+                                                   smem) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -526,7 +685,9 @@ cudaError_t launchOuterRealBwd(const OuterPlan<T>& P, int threads,
   template size_t hermRowSmem<T>(int,int,int); \
   template size_t outerFwdSmem<T>(int,int); \
   template size_t outerBwdSmem<T>(int,int,int); \
-  template size_t outerRealSmem<T>(int,int,int);
+  template size_t outerRealSmem<T>(int,int,int); \
+  template cudaError_t launchBatch<T>(const BatchArgs<T>&,int,int,size_t,cudaStream_t); \
+  template int batchBlocksPerSM<T>(int,size_t);
 
 FGB_INSTANTIATE(double)
 FGB_INSTANTIATE(float)

@@ -84,6 +84,52 @@ struct OuterPlan {
   long long NX;
 };
 
+// ---------------------------------------------------------------------------
+// Persistent batched launch of many independent 1D convolutions of uneven
+// lengths (no reference counterpart: the reference runs one Convolution
+// object per problem).  Tasks are dequeued in topological order from one
+// global counter: the column-forward tiles of every long problem, then every
+// short problem as a whole row convolution, then the rows of the long
+// problems, then their column-backward tiles.  A row task waits until all
+// forward tiles of its problem are done, a backward tile until all rows are;
+// both waits are bounded (spinLimit polls), and a wait that gives up sets
+// *err and skips its task instead of hanging.
+enum BatchTaskType {TASK_SMALL=0, TASK_COLFWD=1, TASK_ROW=2, TASK_COLBWD=3};
+
+struct BatchTask {
+  int type, prob, i, j;     // i: row or column tile, j: array index
+};
+
+// Pointer fields of the plans hold offsets into the caller's packed arrays
+// when the matching bit of `rel` is set (bit 0 row.in, 1 row.out, 2 fwd.in,
+// 3 bwd.out); otherwise they are absolute staging-buffer addresses.
+template<typename T>
+struct BatchProblem {
+  RowPlan<T> row;
+  OuterPlan<T> fwd, bwd;
+  int rel;
+  int nfwd;                 // forward tiles of a long problem (tiles x A)
+  int nrows;                // rows of a long problem
+};
+
+template<typename T>
+struct BatchArgs {
+  const BatchProblem<T> *probs;
+  const BatchTask *tasks;
+  int ntasks;
+  int *queue;               // dequeue counter (zeroed before every launch)
+  int *done;                // 2 counters per problem (zeroed likewise)
+  int *err;                 // set when a wait gave up
+  long long spinLimit;
+  void *inBase[FGB_MAXA];
+  void *outBase[FGB_MAXA];
+};
+
+template<typename T> cudaError_t launchBatch(const BatchArgs<T>& P, int grid,
+                                             int threads, size_t smem,
+                                             cudaStream_t s);
+template<typename T> int batchBlocksPerSM(int threads, size_t smem);
+
 // Host launchers (kernels.cu).
 template<typename T> cudaError_t launchRow(const RowPlan<T>& P, int threads,
                                            long long grid, cudaStream_t s);

@@ -19,8 +19,8 @@ from typing import Sequence
 from . import _native
 from ._native import CENTERED, F32, F64, HERMITIAN, MULT, PAD, REAL
 
-__all__ = ["HybridConvolution", "PAD", "CENTERED", "HERMITIAN", "REAL",
-           "default_M"]
+__all__ = ["HybridConvolution", "BatchedConvolution", "PAD", "CENTERED",
+           "HERMITIAN", "REAL", "default_M"]
 
 
 def default_M(kind: int, L: int, A: int = 2) -> int:
@@ -182,6 +182,90 @@ class HybridConvolution:
         if h:
             try:
                 self.lib.fgb_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+
+class BatchedConvolution:
+    """Many independent 1D convolutions of uneven lengths in one persistent
+    kernel launch, optionally replayed from a captured CUDA graph.
+
+    lengths[i], M[i]: data length and minimum padded length of problem i
+    (default M = 2L-1).  Each input/output is one packed device tensor
+    holding all problems back to back.  tune=True times the candidate plans
+    of every distinct length on the GPU and keeps the fastest.
+    """
+
+    def __init__(self, lengths, M=None, *, A: int = 2, B: int = 1,
+                 mult: str = "binary", precision: str = "f64",
+                 kind: int = PAD, tune: bool = False):
+        import torch
+        self.lib = _native.load()
+        self.L = [int(x) for x in lengths]
+        self.M = [int(x) for x in (M if M is not None else
+                                   [2 * l - 1 for l in self.L])]
+        self.n = len(self.L)
+        self.A, self.B = A, B
+        self.prec = F64 if precision == "f64" else F32
+        sz = ctypes.c_size_t
+        torch.cuda.current_device()
+        self.handle = self.lib.fgb_batch_create(
+            self.n, (sz * self.n)(*self.L), (sz * self.n)(*self.M), A, B,
+            MULT[mult], self.prec, kind, int(tune))
+        if not self.handle:
+            raise ValueError(_native.last_error())
+        info = (ctypes.c_long * 6)()
+        self.lib.fgb_batch_info(self.handle, info)
+        self.tasks, self.grid, self.smem = info[0], info[1], info[2]
+        self.short_problems, self.long_problems = info[3], info[4]
+        self.total = info[5]
+        self.offsets = []
+        off = 0
+        for l in self.L:
+            self.offsets.append(off)
+            off += l
+
+    @property
+    def dtype(self):
+        import torch
+        return torch.complex128 if self.prec == F64 else torch.complex64
+
+    def choice(self, i: int) -> int:
+        return self.lib.fgb_batch_choice(self.handle, i)
+
+    def split(self, packed):
+        """Views of the problems inside a packed tensor."""
+        return [packed[o:o + l] for o, l in zip(self.offsets, self.L)]
+
+    def convolve(self, *inputs, out=None, graph: bool = True, stream=None):
+        import torch
+        if len(inputs) != self.A:
+            raise ValueError(f"expected {self.A} inputs")
+        for t in inputs:
+            if (t.dtype != self.dtype or not t.is_cuda or t.ndim != 1 or
+                    t.numel() != self.total or not t.is_contiguous()):
+                raise ValueError("inputs must be packed contiguous CUDA "
+                                 f"tensors of {self.total} {self.dtype}")
+        if out is None:
+            out = [torch.empty_like(inputs[0]) for _ in range(self.B)]
+        ins = (ctypes.c_void_p * self.A)(*[t.data_ptr() for t in inputs])
+        outs = (ctypes.c_void_p * self.B)(*[t.data_ptr() for t in out])
+        s = stream if stream is not None else torch.cuda.current_stream()
+        rc = self.lib.fgb_batch_convolve_device(
+            self.handle, ins, outs, ctypes.c_void_p(s.cuda_stream), int(graph))
+        if rc != 0:
+            raise RuntimeError(_native.last_error())
+        return out
+
+    def error(self) -> int:
+        return self.lib.fgb_batch_error(self.handle)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            try:
+                self.lib.fgb_batch_destroy(h)
             except Exception:
                 pass
             self.handle = None

@@ -87,6 +87,33 @@ int fgb_timing_collect(fgb_conv *c, double *ms, int n);
 
 void fgb_destroy(fgb_conv *c);
 
+/* Many independent 1D convolutions of uneven lengths in ONE persistent
+ * kernel launch (no reference counterpart: the reference constructs one
+ * Convolution per problem, convolve.h:1018-1022, and runs them one after
+ * another).  Problem i has L[i] values padded to >= M[i]; the data of all
+ * problems is packed back to back in each of the A input and B output
+ * device arrays (problem i starts at sum_{j<i} L[j]).  kind: FGB_PAD or
+ * FGB_CENTERED.  tune != 0 times the candidate plans of every distinct
+ * (L, M) on the GPU and keeps the fastest, the GPU counterpart of the
+ * reference's CPU optimiser (convolve.cc:177-470). */
+typedef struct fgb_batch fgb_batch;
+fgb_batch *fgb_batch_create(int n, const size_t *L, const size_t *M, int A,
+                            int B, int mult, int precision, int kind,
+                            int tune);
+/* use_graph != 0: capture the launch in a CUDA graph (once per pointer set)
+ * and replay it on `stream`. */
+int fgb_batch_convolve_device(fgb_batch *b, void *const *in,
+                              void *const *out, void *stream, int use_graph);
+/* info[0] tasks, [1] persistent grid, [2] shared bytes per CTA,
+ * [3] one-CTA problems, [4] long problems, [5] total packed length. */
+int fgb_batch_info(const fgb_batch *b, long *info);
+/* Plan of problem i: > 0 residue block m (one CTA), < 0 minus the row
+ * length of a long problem. */
+long fgb_batch_choice(const fgb_batch *b, int i);
+/* Nonzero if a bounded in-kernel wait gave up since the last call. */
+int fgb_batch_error(fgb_batch *b);
+void fgb_batch_destroy(fgb_batch *b);
+
 /* Text of the last error on this thread. */
 const char *fgb_last_error(void);
 
