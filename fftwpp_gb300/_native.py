@@ -53,6 +53,10 @@ def load():
     lib.fgb_timing.argtypes = [vp, ctypes.c_int]
     lib.fgb_timing_collect.restype = ctypes.c_int
     lib.fgb_timing_collect.argtypes = [vp, P(ctypes.c_double), ctypes.c_int]
+    lib.fgb_scale_columns_device.restype = ctypes.c_int
+    lib.fgb_scale_columns_device.argtypes = [sz, sz, ctypes.c_double,
+                                             ctypes.c_double, vp,
+                                             ctypes.c_int, vp]
     lib.fgb_batch_create.restype = vp
     lib.fgb_batch_create.argtypes = [ctypes.c_int, P(sz), P(sz), ctypes.c_int,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_int,

@@ -178,6 +178,19 @@ __global__ void zeroRowKernel(size_t n, cplx<T> *f)
   if(i < n) f[i]=mk((T) 0,(T) 0);
 }
 
+// f[i][j] *= (j == 0 ? s0 : s1) on a rows x cols complex array.
+template<typename T>
+__global__ void scaleColumnsKernel(size_t rows, size_t cols, T s0, T s1,
+                                   cplx<T> *f)
+{
+  size_t n=rows*cols;
+  for(size_t i=blockIdx.x*(size_t) blockDim.x+threadIdx.x; i < n;
+      i += (size_t) gridDim.x*blockDim.x) {
+    T s=i % cols == 0 ? s0 : s1;
+    f[i]=f[i]*s;
+  }
+}
+
 } // namespace
 
 extern "C" {
@@ -507,6 +520,27 @@ size_t fgb_index(int kind, size_t m, size_t p, size_t q, size_t n, size_t D,
     r += i/(p*m);
   }
   return q*s+n*u+r;
+}
+
+int fgb_scale_columns_device(size_t rows, size_t cols, double s0, double s1,
+                             void *f, int precision, void *stream)
+{
+  cudaStream_t s=(cudaStream_t) stream;
+  size_t n=rows*cols;
+  unsigned grid=(unsigned) std::min<size_t>((n+255)/256,4096);
+  if(grid == 0) return 0;
+  if(precision == PREC_F64)
+    scaleColumnsKernel<double><<<grid,256,0,s>>>(rows,cols,s0,s1,
+                                                 (cplx<double> *) f);
+  else
+    scaleColumnsKernel<float><<<grid,256,0,s>>>(rows,cols,(float) s0,
+                                                (float) s1,(cplx<float> *) f);
+  cudaError_t e=cudaGetLastError();
+  if(e != cudaSuccess) {
+    report("fgb_scale_columns_device",cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
 }
 
 int fgb_hermitian_symmetrize_x_device(size_t Hx, size_t Hy, size_t x0,

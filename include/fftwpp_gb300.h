@@ -130,6 +130,12 @@ size_t fgb_nextfftsize(size_t m);
 size_t fgb_index(int kind, size_t m, size_t p, size_t q, size_t n, size_t D,
                  size_t r, size_t i);
 
+/* f[i][j] *= (j == 0 ? s0 : s1) on a rows x cols complex device array: the
+ * weight of the k_y = 0 column of half-plane Hermitian data, used by the
+ * adjoint of the Hermitian convolutions (no reference counterpart). */
+int fgb_scale_columns_device(size_t rows, size_t cols, double s0, double s1,
+                             void *f, int precision, void *stream);
+
 /* Hermitian symmetrisation of device arrays (convolve.h:1175-1258). */
 int fgb_hermitian_symmetrize_x_device(size_t Hx, size_t Hy, size_t x0,
                                       void *f, int precision, void *stream);

@@ -343,7 +343,17 @@ def mult_realjacobian(F):
     return [(R[0] * R[3] - R[1] * R[2]).astype(np.complex128)]
 
 
+def mult_realjacadj(F):
+    """Adjoint products of the real Jacobian: inputs u0..u3 and the
+    back-propagated field g, outputs g u3, -g u2, -g u1, g u0."""
+    R = [f.real for f in F]
+    g = R[4]
+    return [(g * R[3]).astype(np.complex128), (-g * R[2]).astype(np.complex128),
+            (-g * R[1]).astype(np.complex128), (g * R[0]).astype(np.complex128)]
+
+
 MULTIPLIERS: dict[str, Callable] = {
+    "realjacadj": mult_realjacadj,
     "binary": mult_binary,
     "realbinary": mult_realbinary,
     "correlation": mult_correlation,
