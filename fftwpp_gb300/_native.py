@@ -57,6 +57,8 @@ def load():
     lib.fgb_scale_columns_device.argtypes = [sz, sz, ctypes.c_double,
                                              ctypes.c_double, vp,
                                              ctypes.c_int, vp]
+    lib.fgb_hconv2d_convolve_noalloc.restype = ctypes.c_int
+    lib.fgb_hconv2d_convolve_noalloc.argtypes = [vp, vp, vp, sz, sz, vp]
     lib.fgb_batch_create.restype = vp
     lib.fgb_batch_create.argtypes = [ctypes.c_int, P(sz), P(sz), ctypes.c_int,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_int,

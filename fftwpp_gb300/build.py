@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib_fftwpp.so")
-SOURCES = ["kernels.cu", "engine.cu", "batch.cu", "capi.cu"]
+SOURCES = ["kernels.cu", "engine.cu", "batch.cu", "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
          "-I", os.path.join(os.path.dirname(HERE), "include")]

@@ -130,6 +130,26 @@ size_t fgb_nextfftsize(size_t m);
 size_t fgb_index(int kind, size_t m, size_t p, size_t q, size_t n, size_t D,
                  size_t r, size_t i);
 
+/* 2D centred-Hermitian FP64 convolution that allocates no memory.  No
+ * counterpart in the reference (FFTW++ allocates its work arrays in every
+ * Convolution constructor).  For callers that cannot call cudaMalloc: an
+ * application whose own allocator owns the device memory, or a
+ * latency-critical loop in which an allocation would synchronise the
+ * device.  f, g, h: device arrays of Lx x ceil(Ly/2) complex128 modes in the
+ * layout of fftwpp_hconv2d_convolve (h may equal f); the result, normalised
+ * as Convolution::convolve does, goes to h.  Padding: the reference's
+ * default 3/2 rule (HybridConvolution.h:94-95).  All scratch (staging rows
+ * and twiddle tables) lives in one file-scope device array of
+ * FGB_NOALLOC_SCRATCH_BYTES = 32 MiB, held by every GPU that loads the
+ * library until the process exits; sizes that need more are rejected with
+ * an error (up to 1023 x 1023 fits).  The array is shared by all calls on a
+ * device and keeps the last call's contents; each call rewrites everything
+ * it reads.  Calls that overlap on the GPU race on it.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress); make
+ * it before any stream capture.  Returns 0, or -1 with fgb_last_error(). */
+int fgb_hconv2d_convolve_noalloc(const void *f, const void *g, void *h,
+                                 size_t Lx, size_t Ly, void *stream);
+
 /* f[i][j] *= (j == 0 ? s0 : s1) on a rows x cols complex device array: the
  * weight of the k_y = 0 column of half-plane Hermitian data, used by the
  * adjoint of the Hermitian convolutions (no reference counterpart). */
