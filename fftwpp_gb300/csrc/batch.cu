@@ -33,8 +33,8 @@ static size_t rowNeedB(int prec, long L, long m, int A, int B)
 
 static size_t outerNeedB(int prec, long L, long m, int tile)
 {
-  size_t f=prec == PREC_F64 ? outerFwdSmem<double>(m,tile) :
-    outerFwdSmem<float>(m,tile);
+  size_t f=prec == PREC_F64 ? outerFwdSmem<double>(L,m,tile) :
+    outerFwdSmem<float>(L,m,tile);
   size_t b=prec == PREC_F64 ? outerBwdSmem<double>(L,m,tile) :
     outerBwdSmem<float>(L,m,tile);
   return std::max(f,b);
@@ -190,7 +190,7 @@ void BatchConv::build()
       RowPlan<T>& R=P.row;
       R.L=(int) L; R.m=(int) m; R.q=(int) q; R.N=(int) (m*q);
       R.cshift=kind == KIND_CENTERED ? (int) (L/2) : 0;
-      R.A=A; R.B=B; R.mult=mult; R.realIO=0;
+      R.A=A; R.B=B; R.mult=mult; R.realIO=0; R.rpc=1;
       R.scale=(T) (1.0/(double) (m*q));
       R.fp=fftPlanPublic(m,prec);
       R.twN=(const Tw *) twiddles(m*q,prec);
@@ -227,7 +227,7 @@ void BatchConv::build()
       for(int b=0; b < B; ++b) G.out[b]=(cplx<T> *) (offsets[i]*e);
       RowPlan<T>& R=P.row;
       R.L=(int) m; R.m=(int) m; R.q=1; R.N=(int) m; R.cshift=0;
-      R.A=A; R.B=B; R.mult=mult; R.realIO=0; R.scale=(T) 1;
+      R.A=A; R.B=B; R.mult=mult; R.realIO=0; R.rpc=1; R.scale=(T) 1;
       R.fp=fftPlanPublic(m,prec);
       R.twN=(const Tw *) twiddles(m,prec);
       R.rowStride=m; R.nrows=qc;

@@ -172,27 +172,43 @@ static const size_t SMEM_MAX=227*1024;
 
 static size_t elem(int prec) {return prec == PREC_F64 ? 16 : 8;}
 
-static size_t rowNeed(int prec, long L, long m, int A, int B)
+static size_t rowNeed(int prec, long L, long m, int A, int B, int rpc=1)
 {
-  return prec == PREC_F64 ? rowSmem<double>(L,m,A,B) : rowSmem<float>(L,m,A,B);
+  return prec == PREC_F64 ? rowSmem<double>(L,m,A,B,rpc) :
+    rowSmem<float>(L,m,A,B,rpc);
 }
 
-static size_t hermNeed(int prec, long H, long Nh, int A)
+static size_t hermNeed(int prec, long H, long Nh, int A, int rpc=1)
 {
-  return prec == PREC_F64 ? hermRowSmem<double>(H,Nh,A) :
-    hermRowSmem<float>(H,Nh,A);
+  return prec == PREC_F64 ? hermRowSmem<double>(H,Nh,A,rpc) :
+    hermRowSmem<float>(H,Nh,A,rpc);
 }
 
 static size_t outerNeed(int prec, long L, long m, int tile)
 {
-  size_t f=prec == PREC_F64 ? outerFwdSmem<double>(m,tile) :
-    outerFwdSmem<float>(m,tile);
+  size_t f=prec == PREC_F64 ? outerFwdSmem<double>(L,m,tile) :
+    outerFwdSmem<float>(L,m,tile);
   size_t b=prec == PREC_F64 ? outerBwdSmem<double>(L,m,tile) :
     outerBwdSmem<float>(L,m,tile);
   return std::max(f,b);
 }
 
 static double fftCost(long m) {return m*std::log2((double) std::max(m,2L));}
+
+static double fftInstr(long n);
+
+// Rows per CTA of a row kernel: enough that a radix-8 stage has >= 512
+// butterflies for 256 threads, at most 8 and at most nrows, within half of
+// the shared memory (two CTAs per SM).
+template<typename F>
+static int pickRpc(long n, int A, long nrows, F smem)
+{
+  long per=std::max(1L,n/8)*A;
+  int rpc=(int) std::min<long>(8,std::max<long>(1,(512+per-1)/per));
+  rpc=(int) std::min<long>(rpc,std::max(1L,nrows));
+  while(rpc > 1 && smem(rpc) > SMEM_MAX/2) --rpc;
+  return rpc;
+}
 
 // Inner (row) axis, complex data: residue block m and residue count q.
 static bool planRowComplex(AxisPlan& a, long mForce, int A, int B, int prec)
@@ -211,7 +227,10 @@ static bool planRowComplex(AxisPlan& a, long mForce, int A, int B, int prec)
       if(m*q < a.M) continue;
       if(rowNeed(prec,a.L,m,A,B) > SMEM_MAX) continue;
       long p=ceilquotient(a.L,m);
-      double cost=q*((A+B)*fftCost(m)+A*p*(double) m+(A+B)*(double) m);
+      // Arithmetic instructions: transforms, the fold (a complex twiddle per
+      // term for residues r > 0) and the post-twiddled accumulation.
+      double cost=q*(A+B)*fftInstr(m)+A*(double) m*(2.0*p+(q-1)*6.0*p)+
+        B*(double) a.L*(2.0+(q-1)*6.0);
       if(cost < best) {best=cost; bm=m; bq=q;}
     }
     if(!bm) return false;
@@ -272,13 +291,15 @@ static double fftInstr(long n)
 static const int NSM=152;
 
 // Largest power-of-two tile <= maxTile whose kernel fits in shared memory
-// and still gives at least three waves of CTAs over the SMs.
+// and gives at least two waves of CTAs over the SMs, but not narrower than
+// one 32-byte sector per row (minTile columns) unless shared memory forces
+// it.
 template<typename F>
-static int pickTile(int maxTile, long C, long factor, F smem)
+static int pickTile(int maxTile, long C, long factor, F smem, int minTile=1)
 {
   int tile=maxTile;
-  while(tile > 1 && (smem(tile) > SMEM_MAX ||
-                     ceilquotient(C,tile)*factor < 3*NSM))
+  while(tile > minTile && (smem(tile) > SMEM_MAX ||
+                           ceilquotient(C,tile)*factor < 2*NSM))
     tile /= 2;
   while(tile > 1 && smem(tile) > SMEM_MAX) tile /= 2;
   return tile;
@@ -288,6 +309,7 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
                       int A, int B)
 {
   int maxTile=prec == PREC_F64 ? 8 : 16;
+  int minTile=prec == PREC_F64 ? 2 : 4;
   if(a.kind == KIND_REAL) {
     a.N=evenSmooth(mForce > 0 ? std::max(a.M,mForce) : a.M);
     a.m=a.N; a.q=1; a.p=1; a.cshift=0;
@@ -297,8 +319,8 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
       return prec == PREC_F64 ? outerRealSmem<double>(a.L,Nh,t) :
         outerRealSmem<float>(a.L,Nh,t);
     };
-    a.tile=pickTile(maxTile,C,nbatch*A,sm);
-    a.tileB=pickTile(maxTile,C,nbatch*B,sm);
+    a.tile=pickTile(maxTile,C,nbatch*A,sm,minTile);
+    a.tileB=pickTile(maxTile,C,nbatch*B,sm,minTile);
     return;
   }
   bool centered=a.kind == KIND_CENTERED;
@@ -332,15 +354,15 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
   a.cshift=centered ? (int) (a.L/2) : 0;
   a.rows=a.N;
   auto smf=[&](int t) {
-    return prec == PREC_F64 ? outerFwdSmem<double>(a.m,t) :
-      outerFwdSmem<float>(a.m,t);
+    return prec == PREC_F64 ? outerFwdSmem<double>(a.L,a.m,t) :
+      outerFwdSmem<float>(a.L,a.m,t);
   };
   auto smb=[&](int t) {
     return prec == PREC_F64 ? outerBwdSmem<double>(a.L,a.m,t) :
       outerBwdSmem<float>(a.L,a.m,t);
   };
-  a.tile=pickTile(maxTile,C,nbatch*a.q*A,smf);
-  a.tileB=pickTile(maxTile,C,nbatch*B,smb);
+  a.tile=pickTile(maxTile,C,nbatch*a.q*A,smf,minTile);
+  a.tileB=pickTile(maxTile,C,nbatch*B,smb,minTile);
   if(smf(a.tile) > SMEM_MAX || smb(a.tileB) > SMEM_MAX)
     throw std::runtime_error("outer axis too long for shared memory");
 }
@@ -374,6 +396,7 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
       throw std::runtime_error("a real axis must be the outermost");
     a.stored=a.kind == KIND_HERMITIAN ? (long) ceilquotient(a.L,2) : a.L;
     a.tile=a.tileB=1;
+    a.rpc=1;
     a.rows=0;
   }
   if(dim > 1 && batch != 1)
@@ -413,6 +436,19 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
     in.tileB=pickTile(prec == PREC_F64 ? 8 : 16,I.rowM,B,sm);
     if(mForce && mForce[0] > 0)
       throw std::runtime_error("forced m not supported on the long path");
+  }
+  // Rows per CTA of the row kernel.
+  long nrows=batch;
+  for(int d=0; d < dim-1; ++d) nrows *= I.axis[d].rows;
+  if(I.longRow) {
+    in.rpc=pickRpc(I.rowM,A,I.rowQ,[&](int r) {
+      return rowNeed(prec,I.rowM,I.rowM,A,B,r);});
+  } else if(in.kind == KIND_HERMITIAN) {
+    in.rpc=pickRpc(in.N/2,A,nrows,[&](int r) {
+      return hermNeed(prec,in.stored,in.N/2,A,r);});
+  } else {
+    in.rpc=pickRpc(in.m,A,nrows,[&](int r) {
+      return rowNeed(prec,in.stored,in.m,A,B,r);});
   }
   allocate();
 }
@@ -518,12 +554,14 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.L=(int) a.stored; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
     P.cshift=a.cshift; P.A=A; P.B=B; P.mult=I.mult;
     P.realIO=a.kind == KIND_REAL && I.dim == 1;
+    P.rpc=I.axis[I.dim-1].rpc;
     P.fp=fftPlan(a.m,I.prec);
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };
   auto hermPlan=[&](HermRowPlan<T>& P, const AxisPlan& a) {
     P.H=(int) a.stored; P.N=(int) a.N; P.Nh=(int) (a.N/2);
     P.A=A; P.B=B; P.mult=I.mult;
+    P.rpc=a.rpc;
     P.fp=fftPlan(a.N/2,I.prec);
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };

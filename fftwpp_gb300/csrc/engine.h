@@ -33,6 +33,7 @@ struct AxisPlan {
   long m, q, N, p;    // residue block length, residues, padded length, folds
   int cshift;         // centred origin offset
   int tile, tileB;    // outer kernels: columns per CTA (forward, backward)
+  int rpc;            // innermost axis: rows per CTA of the row kernel
   long rows;          // outer axis: rows produced (N, or N/2+1 if real)
 };
 

@@ -25,6 +25,21 @@ namespace fgb {
 
 #define FGB_MAXSTAGES 20
 
+// Shared-memory element index with one pad element every 32: the first
+// Stockham stages write with power-of-two strides, which without padding
+// put a whole warp on one bank.
+__host__ __device__ __forceinline__ int sp(int a) {return a+(a >> 5);}
+// Elements to allocate for n logical elements.
+__host__ __device__ __forceinline__ int padded(int n) {return n+(n >> 5)+1;}
+
+// floor(a/b) for 0 <= a < 2^21 through a float reciprocal (exact in that
+// range: the rounded product is within 2^-22 relative of a/b while the
+// nearest integer boundary is at least 1/(2b) away from (a+0.5)/b).
+__device__ __forceinline__ int fdiv(int a, float invb)
+{
+  return __float2int_rz(((float) a+0.5f)*invb);
+}
+
 struct FFTPlanDev {
   int n;
   int nst;
@@ -157,13 +172,15 @@ __device__ __forceinline__ void fftStage(const cplx<T> *__restrict__ x,
   const int nR=n/R;
   const int tstride=n/(Ns*R);
   const int total=nR*ncol;
+  const float invNcol=1.0f/(float) ncol;
+  const float invNs=1.0f/(float) Ns;
   for(int idx=tid; idx < total; idx += nthr) {
-    int j=idx/ncol;
+    int j=fdiv(idx,invNcol);
     int c=idx-j*ncol;
-    int k=j % Ns;
+    int k=j-fdiv(j,invNs)*Ns;
     cplx<T> a[R];
 #pragma unroll
-    for(int r=0; r < R; ++r) a[r]=x[(j+r*nR)*ld+c];
+    for(int r=0; r < R; ++r) a[r]=x[sp((j+r*nR)*ld+c)];
     if(k != 0) {
 #pragma unroll
       for(int r=1; r < R; ++r) a[r]=twmul<S>(a[r],tw[r*k*tstride]);
@@ -171,14 +188,14 @@ __device__ __forceinline__ void fftStage(const cplx<T> *__restrict__ x,
     Codelet<R,S,T>::run(a);
     int base=(j-k)*R+k;
 #pragma unroll
-    for(int r=0; r < R; ++r) y[(base+r*Ns)*ld+c]=a[r];
+    for(int r=0; r < R; ++r) y[sp((base+r*Ns)*ld+c)]=a[r];
   }
 }
 
 // Transform ncol columns (stride ld) of x in place through the ping-pong
-// buffer y.  Every thread of the block must call it; the caller has
-// synchronised after filling x.  Returns the buffer holding the result
-// (x or y) and leaves the block synchronised.
+// buffer y; element (i, c) lives at x[sp(i*ld+c)].  Every thread of the
+// block must call it; the caller has synchronised after filling x.  Returns
+// the buffer holding the result (x or y) and leaves the block synchronised.
 template<typename T, int S>
 __device__ cplx<T> *fftSmem(cplx<T> *x, cplx<T> *y, const FFTPlanDev& p,
                             int ncol, int ld, int tid, int nthr)

@@ -3,6 +3,9 @@
 // kernel.
 #include "kernels.cuh"
 
+#include <algorithm>
+#include <climits>
+
 namespace fgb {
 
 // ---------------------------------------------------------------------------
@@ -97,70 +100,110 @@ __device__ __forceinline__ cplx<float> ldx(const cplx<float> *p)
   return *p;
 }
 
-// One row of the complex row convolution (all residues), using the block's
-// shared memory.  Every thread of the block calls it.
+// Asynchronous global->shared copy of one complex element (cp.async; the
+// 16-byte form bypasses L1).  cpAsyncWait() waits for all of the thread's
+// copies; a __syncthreads() must follow before other threads read them.
+__device__ __forceinline__ void cpAsync(cplx<double> *dst,
+                                        const cplx<double> *src)
+{
+  unsigned s=(unsigned) __cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n"
+               :: "r"(s), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cpAsync(cplx<float> *dst,
+                                        const cplx<float> *src)
+{
+  unsigned s=(unsigned) __cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n"
+               :: "r"(s), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cpAsyncWait()
+{
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// One group of P.rpc rows of the complex row convolution (all residues),
+// using the block's shared memory.  The A x rpc input rows are transformed
+// together as interleaved columns col = a*rpc + rho, so the B x rpc output
+// columns are a contiguous prefix for the inverse transforms.  Every thread
+// of the block calls it.
 template<typename T, bool CG>
-__device__ __forceinline__ void rowConvRow(const RowPlan<T>& P, long long row,
+__device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
+                                           long long group,
                                            unsigned char *smemRaw)
 {
-  const int A=P.A, B=P.B, L=P.L, m=P.m, N=P.N, c=P.cshift;
+  const int A=P.A, B=P.B, L=P.L, m=P.m, N=P.N, c=P.cshift, R=P.rpc;
+  const int ld=A*R, lb=B*R;
   cplx<T> *fin=(cplx<T> *) smemRaw;
-  cplx<T> *acc=fin+A*L;
-  cplx<T> *x=acc+B*L;
-  cplx<T> *y=x+m*A;
+  cplx<T> *acc=fin+ld*L;
+  cplx<T> *x=acc+lb*L;
+  cplx<T> *y=x+padded(m*ld);
   const int tid=threadIdx.x, nthr=blockDim.x;
   const typename TwT<T>::type *tw=P.twN;
+  const float invL=1.0f/(float) L, invLd=1.0f/(float) ld;
+  const float invR=1.0f/(float) R;
+  const long long row0=group*R;
 
-  {
-    long long base=row*P.rowStride;
-    for(int i=tid; i < A*L; i += nthr) {
-      int a=i/L, s=i-a*L;
-      fin[i]=P.realIO ? mk(((const T *) P.in[a])[base+s],(T) 0) :
-        ldx<CG>(P.in[a]+base+s);
+  for(int i=tid; i < ld*L; i += nthr) {
+    int col=fdiv(i,invL), s=i-col*L;
+    int a=fdiv(col,invR);
+    long long row=row0+col-a*R;
+    cplx<T> v=mk((T) 0,(T) 0);
+    if(row < P.nrows) {
+      long long off=row*P.rowStride+s;
+      v=P.realIO ? mk(((const T *) P.in[a])[off],(T) 0) : ldx<CG>(P.in[a]+off);
     }
-    for(int i=tid; i < B*L; i += nthr) acc[i]=mk((T) 0,(T) 0);
+    fin[i]=v;
+  }
+  for(int i=tid; i < lb*L; i += nthr) acc[i]=mk((T) 0,(T) 0);
+  __syncthreads();
+
+  for(int r=0; r < P.q; ++r) {
+    // Fold the data into one length-m block with the residue twiddles.
+    for(int i=tid; i < m*ld; i += nthr) {
+      int t=fdiv(i,invLd), col=i-t*ld;
+      int s0=posmod(t+c,m);
+      cplx<T> sum=mk((T) 0,(T) 0);
+      for(int s=s0; s < L; s += m) {
+        cplx<T> v=fin[col*L+s];
+        if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
+        sum=sum+v;
+      }
+      x[sp(i)]=sum;
+    }
     __syncthreads();
-
-    for(int r=0; r < P.q; ++r) {
-      // Fold the data into one length-m block with the residue twiddles.
-      for(int i=tid; i < m*A; i += nthr) {
-        int t=i/A, a=i-t*A;
-        int s0=posmod(t+c,m);
-        cplx<T> sum=mk((T) 0,(T) 0);
-        for(int s=s0; s < L; s += m) {
-          cplx<T> v=fin[a*L+s];
-          if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
-          sum=sum+v;
-        }
-        x[i]=sum;
-      }
-      __syncthreads();
-      cplx<T> *X=fftSmem<T,1>(x,y,P.fp,A,A,tid,nthr);
-      cplx<T> *Y=X == x ? y : x;
-      for(int j=tid; j < m; j += nthr) {
-        cplx<T> v[FGB_MAXA];
-        for(int a=0; a < A; ++a) v[a]=X[j*A+a];
-        applyMult(P.mult,v,A);
-        for(int b=0; b < B; ++b) X[j*A+b]=v[b];
-      }
-      __syncthreads();
-      cplx<T> *Z=fftSmem<T,-1>(X,Y,P.fp,B,A,tid,nthr);
-      for(int i=tid; i < B*L; i += nthr) {
-        int b=i/L, s=i-b*L;
-        int t=posmod(s-c,m);
-        cplx<T> v=Z[t*A+b];
-        if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
-        acc[i]=acc[i]+v;
-      }
-      __syncthreads();
+    cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
+    cplx<T> *Y=X == x ? y : x;
+    for(int i=tid; i < m*R; i += nthr) {
+      int j=fdiv(i,invR), rho=i-j*R;
+      cplx<T> v[FGB_MAXA];
+      for(int a=0; a < A; ++a) v[a]=X[sp(j*ld+a*R+rho)];
+      applyMult(P.mult,v,A);
+      for(int b=0; b < B; ++b) X[sp(j*ld+b*R+rho)]=v[b];
     }
-    for(int i=tid; i < B*L; i += nthr) {
-      int b=i/L, s=i-b*L;
-      if(P.realIO) ((T *) P.out[b])[base+s]=acc[i].x*P.scale;
-      else P.out[b][base+s]=acc[i]*P.scale;
+    __syncthreads();
+    cplx<T> *Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
+    for(int i=tid; i < lb*L; i += nthr) {
+      int col=fdiv(i,invL), s=i-col*L;
+      int t=posmod(s-c,m);
+      cplx<T> v=Z[sp(t*ld+col)];
+      if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
+      acc[i]=acc[i]+v;
     }
     __syncthreads();
   }
+  for(int i=tid; i < lb*L; i += nthr) {
+    int col=fdiv(i,invL), s=i-col*L;
+    int b=fdiv(col,invR);
+    long long row=row0+col-b*R;
+    if(row >= P.nrows) continue;
+    long long off=row*P.rowStride+s;
+    if(P.realIO) ((T *) P.out[b])[off]=acc[i].x*P.scale;
+    else P.out[b][off]=acc[i]*P.scale;
+  }
+  __syncthreads();
 }
 
 template<typename T>
@@ -168,8 +211,9 @@ __global__ void __launch_bounds__(256)
 rowConvKernel(const RowPlan<T> P)
 {
   extern __shared__ __align__(16) unsigned char smemRaw[];
-  for(long long row=blockIdx.x; row < P.nrows; row += gridDim.x)
-    rowConvRow<T,false>(P,row,smemRaw);
+  const long long groups=(P.nrows+P.rpc-1)/P.rpc;
+  for(long long g=blockIdx.x; g < groups; g += gridDim.x)
+    rowConvRow<T,false>(P,g,smemRaw);
 }
 
 // ---------------------------------------------------------------------------
@@ -184,54 +228,65 @@ __global__ void __launch_bounds__(256)
 hermRowKernel(const HermRowPlan<T> P)
 {
   extern __shared__ __align__(16) unsigned char smemRaw[];
-  const int A=P.A, B=P.B, H=P.H, Nh=P.Nh;
+  const int A=P.A, B=P.B, H=P.H, Nh=P.Nh, R=P.rpc;
+  const int ld=A*R, lb=B*R;
   cplx<T> *zin=(cplx<T> *) smemRaw;
-  cplx<T> *x=zin+A*H;
-  cplx<T> *y=x+Nh*A;
+  cplx<T> *x=zin+ld*H;
+  cplx<T> *y=x+padded(Nh*ld);
   const int tid=threadIdx.x, nthr=blockDim.x;
   const typename TwT<T>::type *tw=P.twN;
   const T half=(T) 0.5;
+  const float invH=1.0f/(float) H, invLd=1.0f/(float) ld;
+  const float invR=1.0f/(float) R;
+  const long long groups=(P.nrows+R-1)/R;
 
-  for(long long row=blockIdx.x; row < P.nrows; row += gridDim.x) {
-    long long base=row*P.rowStride;
-    for(int i=tid; i < A*H; i += nthr) {
-      int a=i/H, k=i-a*H;
-      zin[i]=P.in[a][base+k];
+  // Rows g*R .. g*R+R-1 are transformed together; column col = a*R + rho.
+  for(long long g=blockIdx.x; g < groups; g += gridDim.x) {
+    const long long row0=g*R;
+    for(int i=tid; i < ld*H; i += nthr) {
+      int col=fdiv(i,invH), k=i-col*H;
+      int a=fdiv(col,invR);
+      long long row=row0+col-a*R;
+      zin[i]=row < P.nrows ? P.in[a][row*P.rowStride+k] : mk((T) 0,(T) 0);
     }
     __syncthreads();
     // Y[k] = (Z[k] + conj Z[Nh-k]) + i W_N^k (Z[k] - conj Z[Nh-k])
-    for(int i=tid; i < Nh*A; i += nthr) {
-      int k=i/A, a=i-k*A;
-      cplx<T> zk=k < H ? zin[a*H+k] : mk((T) 0,(T) 0);
+    for(int i=tid; i < Nh*ld; i += nthr) {
+      int k=fdiv(i,invLd), col=i-k*ld;
+      cplx<T> zk=k < H ? zin[col*H+k] : mk((T) 0,(T) 0);
       if(k == 0) zk.y=(T) 0;
       int kk=Nh-k;
-      cplx<T> zc=kk < H ? conjg(zin[a*H+kk]) : mk((T) 0,(T) 0);
+      cplx<T> zc=kk < H ? conjg(zin[col*H+kk]) : mk((T) 0,(T) 0);
       cplx<T> s=zk+zc;
       cplx<T> d=twmul<1>(zk-zc,tw[k]);
-      x[i]=mk(s.x-d.y,s.y+d.x);
+      x[sp(i)]=mk(s.x-d.y,s.y+d.x);
     }
     __syncthreads();
-    cplx<T> *X=fftSmem<T,1>(x,y,P.fp,A,A,tid,nthr);
+    cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
     cplx<T> *Y=X == x ? y : x;
-    for(int t=tid; t < Nh; t += nthr) {
+    for(int i=tid; i < Nh*R; i += nthr) {
+      int t=fdiv(i,invR), rho=i-t*R;
       cplx<T> v[FGB_MAXA];
-      for(int a=0; a < A; ++a) v[a]=X[t*A+a];
+      for(int a=0; a < A; ++a) v[a]=X[sp(t*ld+a*R+rho)];
       applyMult(P.mult,v,A);
-      for(int b=0; b < B; ++b) X[t*A+b]=v[b];
+      for(int b=0; b < B; ++b) X[sp(t*ld+b*R+rho)]=v[b];
     }
     __syncthreads();
-    cplx<T> *Z=fftSmem<T,-1>(X,Y,P.fp,B,A,tid,nthr);
+    cplx<T> *Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
     // V[k] = E[k] + W_N^{-k} O[k],  E=(Zk+conj Zm)/2, O=(Zk-conj Zm)/(2i)
-    for(int i=tid; i < B*H; i += nthr) {
-      int b=i/H, k=i-b*H;
-      cplx<T> zk=Z[k*A+b];
+    for(int i=tid; i < lb*H; i += nthr) {
+      int col=fdiv(i,invH), k=i-col*H;
+      int b=fdiv(col,invR);
+      long long row=row0+col-b*R;
+      if(row >= P.nrows) continue;
+      cplx<T> zk=Z[sp(k*ld+col)];
       int km=k == 0 ? 0 : Nh-k;
-      cplx<T> zm=conjg(Z[km*A+b]);
+      cplx<T> zm=conjg(Z[sp(km*ld+col)]);
       cplx<T> e=(zk+zm)*half;
       cplx<T> dd=zk-zm;
       cplx<T> o=mk(dd.y*half,-dd.x*half);
       cplx<T> v=e+twmul<-1>(o,tw[k]);
-      P.out[b][base+k]=v*P.scale;
+      P.out[b][row*P.rowStride+k]=v*P.scale;
     }
     __syncthreads();
   }
@@ -247,7 +302,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
 {
   const int tile=P.tile, m=P.m, N=P.N, c=P.cshift, L=P.L;
   cplx<T> *x=(cplx<T> *) smemRaw;
-  cplx<T> *y=x+m*tile;
+  cplx<T> *y=x+padded(m*tile);
   const int tid=threadIdx.x, nthr=blockDim.x;
   const int col0=ctile*tile;
   const int a=z % P.count;
@@ -255,30 +310,37 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
   const cplx<T> *src=P.in[a]+batch*P.inBatch;
   cplx<T> *dst=P.out[a]+batch*P.outBatch;
   const typename TwT<T>::type *tw=P.twN;
+  const float invTile=1.0f/(float) tile;
 
-  for(int i=tid; i < m*tile; i += nthr) {
-    int t=i/tile, cc=i-t*tile;
+  // Stage the L x tile input block in y with asynchronous copies (many
+  // loads in flight per thread instead of one dependent load per output).
+  for(int i=tid; i < L*tile; i += nthr) {
+    int s=fdiv(i,invTile), cc=i-s*tile;
     int col=col0+cc;
+    long long off=(long long) s*P.inRow+col;
+    if(col < P.C && off < P.Ltot) cpAsync(y+i,src+off);
+    else y[i]=mk((T) 0,(T) 0);
+  }
+  cpAsyncWait();
+  __syncthreads();
+  for(int i=tid; i < m*tile; i += nthr) {
+    int t=fdiv(i,invTile), cc=i-t*tile;
     cplx<T> sum=mk((T) 0,(T) 0);
-    if(col < P.C) {
-      int s0=posmod(t+c,m);
-      for(int s=s0; s < L; s += m) {
-        long long off=(long long) s*P.inRow+col;
-        if(off >= P.Ltot) break;
-        cplx<T> v=ldx<CG>(src+off);
-        if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
-        sum=sum+v;
-      }
+    int s0=posmod(t+c,m);
+    for(int s=s0; s < L; s += m) {
+      cplx<T> v=y[s*tile+cc];
+      if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
+      sum=sum+v;
     }
-    x[i]=sum;
+    x[sp(i)]=sum;
   }
   __syncthreads();
   cplx<T> *X=fftSmem<T,1>(x,y,P.fp,tile,tile,tid,nthr);
   for(int i=tid; i < m*tile; i += nthr) {
-    int j=i/tile, cc=i-j*tile;
+    int j=fdiv(i,invTile), cc=i-j*tile;
     int col=col0+cc;
     if(col < P.C) {
-      cplx<T> v=X[i];
+      cplx<T> v=X[sp(i)];
       long long k=(long long) r*m+j;
       if(P.twX) {
         unsigned long long e=((unsigned long long) col*(unsigned long long) k)
@@ -307,7 +369,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
   const int tile=P.tile, m=P.m, N=P.N, c=P.cshift, L=P.L;
   cplx<T> *acc=(cplx<T> *) smemRaw;
   cplx<T> *x=acc+L*tile;
-  cplx<T> *y=x+m*tile;
+  cplx<T> *y=x+padded(m*tile);
   const int tid=threadIdx.x, nthr=blockDim.x;
   const int col0=ctile*tile;
   const int b=z % P.count;
@@ -315,37 +377,51 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
   const cplx<T> *src=P.in[b]+batch*P.inBatch;
   cplx<T> *dst=P.out[b]+batch*P.outBatch;
   const typename TwT<T>::type *tw=P.twN;
+  const float invTile=1.0f/(float) tile;
 
   for(int i=tid; i < L*tile; i += nthr) acc[i]=mk((T) 0,(T) 0);
   for(int r=0; r < P.q; ++r) {
-    for(int i=tid; i < m*tile; i += nthr) {
-      int j=i/tile, cc=i-j*tile;
-      int col=col0+cc;
-      cplx<T> v=mk((T) 0,(T) 0);
-      if(col < P.C) {
-        long long k=(long long) r*m+j;
-        v=ldx<CG>(src+k*P.inRow+col);
-        if(P.twX) {
-          unsigned long long e=((unsigned long long) col*(unsigned long long) k)
-            % (unsigned long long) P.NX;
-          v=twmul<-1>(v,P.twX[e]);
-        }
+    if(CG) {
+      // Data written by other CTAs of this launch: L2 loads.
+      for(int i=tid; i < m*tile; i += nthr) {
+        int j=fdiv(i,invTile), cc=i-j*tile;
+        int col=col0+cc;
+        cplx<T> v=mk((T) 0,(T) 0);
+        if(col < P.C) v=ldx<CG>(src+((long long) r*m+j)*P.inRow+col);
+        x[sp(i)]=v;
       }
-      x[i]=v;
+    } else {
+      for(int i=tid; i < m*tile; i += nthr) {
+        int j=fdiv(i,invTile), cc=i-j*tile;
+        int col=col0+cc;
+        if(col < P.C) cpAsync(x+sp(i),src+((long long) r*m+j)*P.inRow+col);
+        else x[sp(i)]=mk((T) 0,(T) 0);
+      }
+      cpAsyncWait();
     }
     __syncthreads();
+    if(P.twX) {
+      for(int i=tid; i < m*tile; i += nthr) {
+        int j=fdiv(i,invTile), cc=i-j*tile;
+        unsigned long long e=((unsigned long long) (col0+cc)*
+                              (unsigned long long) ((long long) r*m+j)) %
+          (unsigned long long) P.NX;
+        x[sp(i)]=twmul<-1>(x[sp(i)],P.twX[e]);
+      }
+      __syncthreads();
+    }
     cplx<T> *X=fftSmem<T,-1>(x,y,P.fp,tile,tile,tid,nthr);
     for(int i=tid; i < L*tile; i += nthr) {
-      int s=i/tile, cc=i-s*tile;
+      int s=fdiv(i,invTile), cc=i-s*tile;
       int t=posmod(s-c,m);
-      cplx<T> v=X[t*tile+cc];
+      cplx<T> v=X[sp(t*tile+cc)];
       if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
       acc[i]=acc[i]+v;
     }
     __syncthreads();
   }
   for(int i=tid; i < L*tile; i += nthr) {
-    int s=i/tile, cc=i-s*tile;
+    int s=fdiv(i,invTile), cc=i-s*tile;
     int col=col0+cc;
     long long off=(long long) s*P.outRow+col;
     if(col < P.C && off < P.Ltot) dst[off]=acc[i]*P.scale;
@@ -372,7 +448,7 @@ outerRealFwdKernel(const OuterPlan<T> P)
   extern __shared__ __align__(16) unsigned char smemRaw[];
   const int tile=P.tile, L=P.L, Nh=P.N/2;
   cplx<T> *x=(cplx<T> *) smemRaw;
-  cplx<T> *y=x+Nh*tile;
+  cplx<T> *y=x+padded(Nh*tile);
   const int tid=threadIdx.x, nthr=blockDim.x;
   const int col0=blockIdx.x*tile;
   const int a=blockIdx.z % P.count;
@@ -381,9 +457,10 @@ outerRealFwdKernel(const OuterPlan<T> P)
   cplx<T> *dst=P.out[a]+batch*P.outBatch;
   const typename TwT<T>::type *tw=P.twN;
   const T half=(T) 0.5;
+  const float invTile=1.0f/(float) tile;
 
   for(int i=tid; i < Nh*tile; i += nthr) {
-    int t=i/tile, cc=i-t*tile;
+    int t=fdiv(i,invTile), cc=i-t*tile;
     int col=col0+cc;
     T re=0, im=0;
     if(col < P.C) {
@@ -391,18 +468,18 @@ outerRealFwdKernel(const OuterPlan<T> P)
       if(s < L) re=src[(long long) s*P.inRow+col];
       if(s+1 < L) im=src[(long long) (s+1)*P.inRow+col];
     }
-    x[i]=mk(re,im);
+    x[sp(i)]=mk(re,im);
   }
   __syncthreads();
   cplx<T> *X=fftSmem<T,1>(x,y,P.fp,tile,tile,tid,nthr);
   for(int i=tid; i < (Nh+1)*tile; i += nthr) {
-    int k=i/tile, cc=i-k*tile;
+    int k=fdiv(i,invTile), cc=i-k*tile;
     int col=col0+cc;
     if(col >= P.C) continue;
     int k0=k == Nh ? 0 : k;
     int km=k == 0 || k == Nh ? 0 : Nh-k;
-    cplx<T> zk=X[k0*tile+cc];
-    cplx<T> zm=conjg(X[km*tile+cc]);
+    cplx<T> zk=X[sp(k0*tile+cc)];
+    cplx<T> zm=conjg(X[sp(km*tile+cc)]);
     cplx<T> e=(zk+zm)*half;
     cplx<T> dd=zk-zm;
     cplx<T> o=mk(dd.y*half,-dd.x*half);
@@ -423,7 +500,7 @@ outerRealBwdKernel(const OuterPlan<T> P)
   extern __shared__ __align__(16) unsigned char smemRaw[];
   const int tile=P.tile, L=P.L, Nh=P.N/2;
   cplx<T> *x=(cplx<T> *) smemRaw;
-  cplx<T> *y=x+Nh*tile;
+  cplx<T> *y=x+padded(Nh*tile);
   const int tid=threadIdx.x, nthr=blockDim.x;
   const int col0=blockIdx.x*tile;
   const int b=blockIdx.z % P.count;
@@ -431,9 +508,10 @@ outerRealBwdKernel(const OuterPlan<T> P)
   const cplx<T> *src=P.in[b]+batch*P.inBatch;
   T *dst=(T *) P.out[b]+batch*P.outBatch;
   const typename TwT<T>::type *tw=P.twN;
+  const float invTile=1.0f/(float) tile;
 
   for(int i=tid; i < Nh*tile; i += nthr) {
-    int k=i/tile, cc=i-k*tile;
+    int k=fdiv(i,invTile), cc=i-k*tile;
     int col=col0+cc;
     cplx<T> v=mk((T) 0,(T) 0);
     if(col < P.C) {
@@ -446,15 +524,15 @@ outerRealBwdKernel(const OuterPlan<T> P)
       cplx<T> d=twmul<-1>(gk-gm,tw[k]);
       v=mk(s.x-d.y,s.y+d.x);
     }
-    x[i]=v;
+    x[sp(i)]=v;
   }
   __syncthreads();
   cplx<T> *X=fftSmem<T,-1>(x,y,P.fp,tile,tile,tid,nthr);
   for(int i=tid; i < Nh*tile; i += nthr) {
-    int t=i/tile, cc=i-t*tile;
+    int t=fdiv(i,invTile), cc=i-t*tile;
     int col=col0+cc;
     if(col >= P.C) continue;
-    cplx<T> v=X[i]*P.scale;
+    cplx<T> v=X[sp(i)]*P.scale;
     int s=2*t;
     if(s < L) dst[(long long) s*P.outRow+col]=v.x;
     if(s+1 < L) dst[(long long) (s+1)*P.outRow+col]=v.y;
@@ -575,25 +653,28 @@ int batchBlocksPerSM(int threads, size_t smem)
 // ---------------------------------------------------------------------------
 // Launchers.
 
-template<typename T> size_t rowSmem(int L, int m, int A, int B)
+// Shared-memory bytes: FFT ping-pong buffers are padded (sp()); the forward
+// outer kernel also stages its L x tile input block in the second buffer.
+template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc)
 {
-  return sizeof(cplx<T>)*((size_t) (A+B)*L+2*(size_t) m*A);
+  return sizeof(cplx<T>)*((size_t) (A+B)*rpc*L+2*(size_t) padded(m*A*rpc));
 }
-template<typename T> size_t hermRowSmem(int H, int Nh, int A)
+template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc)
 {
-  return sizeof(cplx<T>)*((size_t) A*H+2*(size_t) Nh*A);
+  return sizeof(cplx<T>)*((size_t) A*rpc*H+2*(size_t) padded(Nh*A*rpc));
 }
-template<typename T> size_t outerFwdSmem(int m, int tile)
+template<typename T> size_t outerFwdSmem(int L, int m, int tile)
 {
-  return sizeof(cplx<T>)*2*(size_t) m*tile;
+  size_t pm=padded(m*tile);
+  return sizeof(cplx<T>)*(pm+std::max(pm,(size_t) L*tile));
 }
 template<typename T> size_t outerBwdSmem(int L, int m, int tile)
 {
-  return sizeof(cplx<T>)*((size_t) L*tile+2*(size_t) m*tile);
+  return sizeof(cplx<T>)*((size_t) L*tile+2*(size_t) padded(m*tile));
 }
 template<typename T> size_t outerRealSmem(int L, int Nh, int tile)
 {
-  return sizeof(cplx<T>)*2*(size_t) (Nh+1)*tile;
+  return sizeof(cplx<T>)*2*(size_t) padded((Nh+1)*tile);
 }
 
 template<typename K>
@@ -610,9 +691,11 @@ template<typename T>
 cudaError_t launchRow(const RowPlan<T>& P, int threads, long long grid,
                       cudaStream_t s)
 {
-  size_t sm=rowSmem<T>(P.L,P.m,P.A,P.B);
+  size_t sm=rowSmem<T>(P.L,P.m,P.A,P.B,P.rpc);
   cudaError_t e=setSmem(rowConvKernel<T>,sm);
   if(e != cudaSuccess) return e;
+  long long groups=(P.nrows+P.rpc-1)/P.rpc;
+  grid=std::min(std::min(grid,groups),(long long) INT_MAX);
   rowConvKernel<T><<<(unsigned) grid,threads,sm,s>>>(P);
   return cudaGetLastError();
 }
@@ -621,9 +704,11 @@ template<typename T>
 cudaError_t launchHermRow(const HermRowPlan<T>& P, int threads,
                           long long grid, cudaStream_t s)
 {
-  size_t sm=hermRowSmem<T>(P.H,P.Nh,P.A);
+  size_t sm=hermRowSmem<T>(P.H,P.Nh,P.A,P.rpc);
   cudaError_t e=setSmem(hermRowKernel<T>,sm);
   if(e != cudaSuccess) return e;
+  long long groups=(P.nrows+P.rpc-1)/P.rpc;
+  grid=std::min(std::min(grid,groups),(long long) INT_MAX);
   hermRowKernel<T><<<(unsigned) grid,threads,sm,s>>>(P);
   return cudaGetLastError();
 }
@@ -631,7 +716,7 @@ cudaError_t launchHermRow(const HermRowPlan<T>& P, int threads,
 template<typename T>
 cudaError_t launchOuterFwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
 {
-  size_t sm=outerFwdSmem<T>(P.m,P.tile);
+  size_t sm=outerFwdSmem<T>(P.L,P.m,P.tile);
   cudaError_t e=setSmem(outerFwdKernel<T>,sm);
   if(e != cudaSuccess) return e;
   dim3 grid((P.C+P.tile-1)/P.tile,P.q,P.nbatch*P.count);
@@ -681,9 +766,9 @@ cudaError_t launchOuterRealBwd(const OuterPlan<T>& P, int threads,
   template cudaError_t launchOuterBwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
   template cudaError_t launchOuterRealFwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
   template cudaError_t launchOuterRealBwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
-  template size_t rowSmem<T>(int,int,int,int); \
-  template size_t hermRowSmem<T>(int,int,int); \
-  template size_t outerFwdSmem<T>(int,int); \
+  template size_t rowSmem<T>(int,int,int,int,int); \
+  template size_t hermRowSmem<T>(int,int,int,int); \
+  template size_t outerFwdSmem<T>(int,int,int); \
   template size_t outerBwdSmem<T>(int,int,int); \
   template size_t outerRealSmem<T>(int,int,int); \
   template cudaError_t launchBatch<T>(const BatchArgs<T>&,int,int,size_t,cudaStream_t); \

@@ -45,6 +45,7 @@ struct RowPlan {
   int cshift;              // centred origin offset (0 for fftPad)
   int A, B, mult;
   int realIO;              // real data in and out (1D fftPadReal rows)
+  int rpc;                 // rows per CTA (their columns are interleaved)
   T scale;
   FFTPlanDev fp;           // length-m complex FFT
   const typename TwT<T>::type *twN;   // W_N^t, t < N
@@ -59,6 +60,7 @@ struct HermRowPlan {
   int H;                   // stored Hermitian modes (k = 0..H-1)
   int N, Nh;               // real padded length (even) and N/2
   int A, B, mult;
+  int rpc;                 // rows per CTA
   T scale;
   FFTPlanDev fp;           // length-Nh complex FFT
   const typename TwT<T>::type *twN;   // W_N^t, t < N
@@ -148,9 +150,9 @@ template<typename T> cudaError_t launchOuterRealBwd(const OuterPlan<T>& P,
                                                     cudaStream_t s);
 
 // Shared-memory bytes each kernel needs (for plan-time sizing).
-template<typename T> size_t rowSmem(int L, int m, int A, int B);
-template<typename T> size_t hermRowSmem(int H, int Nh, int A);
-template<typename T> size_t outerFwdSmem(int m, int tile);
+template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc=1);
+template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc=1);
+template<typename T> size_t outerFwdSmem(int L, int m, int tile);
 template<typename T> size_t outerBwdSmem(int L, int m, int tile);
 template<typename T> size_t outerRealSmem(int L, int Nh, int tile);
 

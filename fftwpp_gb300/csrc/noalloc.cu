@@ -157,7 +157,7 @@ extern "C" int fgb_hconv2d_convolve_noalloc(const void *f, const void *g,
   auto tileFor=[&](long count, bool bwd) {
     int t=8;
     while(t > 1 && ((bwd ? outerBwdSmem<double>((int) Lx,(int) Nx,t) :
-                     outerFwdSmem<double>((int) Nx,t)) > 227*1024 ||
+                     outerFwdSmem<double>((int) Lx,(int) Nx,t)) > 227*1024 ||
                     ceilquotient(Hy,t)*count < 3*152))
       t /= 2;
     return t;
@@ -179,7 +179,7 @@ extern "C" int fgb_hconv2d_convolve_noalloc(const void *f, const void *g,
 
   HermRowPlan<double> P;
   P.H=(int) Hy; P.N=(int) Ny; P.Nh=(int) Nyh;
-  P.A=2; P.B=1; P.mult=MULT_REALBINARY;
+  P.A=2; P.B=1; P.mult=MULT_REALBINARY; P.rpc=1;
   P.fp=radixPlan(Nyh,tyh);
   P.twN=ty;
   P.in[0]=stage0; P.in[1]=stage1; P.out[0]=stage0;

@@ -80,6 +80,7 @@ class HybridConvolution:
         self.launches = info[24]
         self.staging_bytes = info[25]
         self.long_path = bool(info[26])
+        self.rows_per_cta = info[30]
         self.shape = tuple(ax["stored"] for ax in self.axes)
         if batch > 1:
             self.shape = (batch,) + self.shape
