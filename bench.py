@@ -203,9 +203,10 @@ def cpu_oracle_rate(w, budget_s, max_convs, workers):
     return n * 1.0 / dt, n, dt
 
 
-def traffic_from_profiles(workload, kernel, precision):
-    """DRAM bytes per launch of `kernel` from a committed ncu summary line
-    `TRAFFIC <workload> <precision> <kernel> <bytes>` under profiles/."""
+def profile_figure(tag, workload, kernel, precision):
+    """A per-launch figure from a committed ncu summary line
+    `<tag> <workload> <precision> <kernel> <value>` under profiles/
+    (TRAFFIC: DRAM bytes; DPINST: FP64 instructions)."""
     pdir = os.path.join(ROOT, "profiles")
     if not os.path.isdir(pdir):
         return None
@@ -214,11 +215,25 @@ def traffic_from_profiles(workload, kernel, precision):
             continue
         for line in open(os.path.join(pdir, fn)):
             parts = line.strip().strip("`").split()
-            if (len(parts) == 5 and parts[0] == "TRAFFIC" and
+            if (len(parts) == 5 and parts[0] == tag and
                     parts[1] == workload and parts[2] == precision and
                     parts[3] == kernel):
                 return float(parts[4])
     return None
+
+
+def traffic_from_profiles(workload, kernel, precision):
+    return profile_figure("TRAFFIC", workload, kernel, precision)
+
+
+def measured_fma_rates():
+    """(DFMA/s, FFMA/s) measured on this GPU by the library's probes."""
+    import ctypes
+    from fftwpp_gb300 import _native
+    d, f = ctypes.c_double(), ctypes.c_double()
+    if _native.load().fgb_measure_fma_rate(ctypes.byref(d), ctypes.byref(f)):
+        return None, None
+    return d.value, f.value
 
 
 def run_reference(args, w):
@@ -352,6 +367,30 @@ def run_ours(args, w):
                 "whole_step_frac": abytes / (total_ms / args.steps * 1e-3)
                 / 1e9 / peak}
 
+    # Compute roofline of the FP64 kernels: FP64 instructions per launch
+    # (ncu, committed under profiles/) over the live launch time, against
+    # the DFMA issue rate measured on this GPU.
+    compute = None
+    dfma, ffma = measured_fma_rates()
+    if prec == "f64" and dfma:
+        dp = [profile_figure("DPINST", args.workload, n, prec) for n in names]
+        if dp[dom]:
+            total_dp = sum(x for x in dp if x) if all(dp) else None
+            compute = {
+                "bound": "fp64_issue", "kernel": names[dom],
+                "achieved": dp[dom] / (per_launch[dom] * 1e-3),
+                "peak": dfma, "unit": "FP64 inst/s",
+                "frac": dp[dom] / (per_launch[dom] * 1e-3) / dfma,
+                "whole_step_frac": (total_dp / (total_ms / args.steps * 1e-3)
+                                    / dfma) if total_dp else None,
+                "fp64_tflops_peak_measured": 2 * dfma / 1e12,
+                "fp32_tflops_peak_measured": 2 * ffma / 1e12,
+                "source": "DP instructions per launch from ncu "
+                          "(profiles/), peak from fgb_measure_fma_rate"}
+    elif dfma:
+        compute = {"fp64_tflops_peak_measured": 2 * dfma / 1e12,
+                   "fp32_tflops_peak_measured": 2 * ffma / 1e12}
+
     # Accuracy at full size against the CPU oracle (FP64 restatement), or,
     # for the 256^3 workload, against FP64 direct sums at sampled outputs.
     from oracle import hybrid as H
@@ -454,6 +493,7 @@ def run_ours(args, w):
                    "l2": "flushed (256 MB write) before every timed step",
                    "plan": conv.axes},
         "roofline": roofline,
+        "compute_roofline": compute,
         "kernels_ms_per_step": dict(zip(names, per_launch)),
         "rel_l2_vs_fp64_oracle": err,
         "cpu_baseline": {"value": cpu_rate, "unit": "convs/s",

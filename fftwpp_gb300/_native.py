@@ -53,6 +53,8 @@ def load():
     lib.fgb_timing.argtypes = [vp, ctypes.c_int]
     lib.fgb_timing_collect.restype = ctypes.c_int
     lib.fgb_timing_collect.argtypes = [vp, P(ctypes.c_double), ctypes.c_int]
+    lib.fgb_measure_fma_rate.restype = ctypes.c_int
+    lib.fgb_measure_fma_rate.argtypes = [P(ctypes.c_double), P(ctypes.c_double)]
     lib.fgb_scale_columns_device.restype = ctypes.c_int
     lib.fgb_scale_columns_device.argtypes = [sz, sz, ctypes.c_double,
                                              ctypes.c_double, vp,

@@ -15,7 +15,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib_fftwpp.so")
-SOURCES = ["kernels.cu", "engine.cu", "batch.cu", "capi.cu", "noalloc.cu"]
+# (source, object, extra flags): kernels.cu is compiled once per precision so
+# the two halves of its template instantiations build in parallel.
+UNITS = [("kernels.cu", "kernels_f64.o", ["-DFGB_ONLY_DOUBLE"]),
+         ("kernels.cu", "kernels_f32.o", ["-DFGB_ONLY_FLOAT"]),
+         ("engine.cu", "engine.o", []),
+         ("batch.cu", "batch.o", []),
+         ("capi.cu", "capi.o", []),
+         ("noalloc.cu", "noalloc.o", [])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
          "-I", os.path.join(os.path.dirname(HERE), "include")]
@@ -49,10 +56,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cc = nvcc()
     procs = []
     objs = []
-    for src in SOURCES:
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+    for src, name, extra in UNITS:
+        obj = os.path.join(BUILD, name)
         objs.append(obj)
-        cmd = [cc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src),
+               "-o", obj]
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE,
                                             stderr=subprocess.STDOUT)))
     for cmd, p in procs:

@@ -287,7 +287,7 @@ void BatchConv::build()
   cudaMemcpy(dProbs,probs.data(),pb,cudaMemcpyHostToDevice);
   cudaMemcpy(dTasks,tasks.data(),tb,cudaMemcpyHostToDevice);
   cudaMemset(dCounters,0,sizeof(int)*(2+2*(size_t) n));
-  int per=batchBlocksPerSM<T>(THREADS,smem);
+  int per=batchBlocksPerSM<T>(THREADS,smem,mult,A,B);
   grid=std::min(ntasks,NSM*per);
 }
 
@@ -314,6 +314,9 @@ cudaError_t BatchConv::launch(const void *const *in, void *const *out,
   P.err=(int *) dCounters+1;
   P.done=(int *) dCounters+2;
   P.spinLimit=20000000LL;
+  P.mult=mult;
+  P.A=A;
+  P.B=B;
   for(int a=0; a < FGB_MAXA; ++a) {
     P.inBase[a]=a < A ? (void *) in[a] : NULL;
     P.outBase[a]=a < B ? out[a] : NULL;

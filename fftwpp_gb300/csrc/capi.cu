@@ -178,6 +178,33 @@ __global__ void zeroRowKernel(size_t n, cplx<T> *f)
   if(i < n) f[i]=mk((T) 0,(T) 0);
 }
 
+// Issue-rate probes for the compute roofline: eight independent FMA chains
+// per thread.  The final sum is stored only if impossible, so the chains are
+// kept without writing anything.
+__global__ void dfmaProbe(double *sink, int iters, double b, double c)
+{
+  double a[8];
+  for(int k=0; k < 8; ++k) a[k]=(threadIdx.x+k)*1e-9;
+  for(int i=0; i < iters; ++i)
+#pragma unroll
+    for(int k=0; k < 8; ++k) a[k]=fma(a[k],b,c);
+  double s=0;
+  for(int k=0; k < 8; ++k) s += a[k];
+  if(s == -1.0) sink[0]=s;
+}
+
+__global__ void ffmaProbe(float *sink, int iters, float b, float c)
+{
+  float a[8];
+  for(int k=0; k < 8; ++k) a[k]=(threadIdx.x+k)*1e-6f;
+  for(int i=0; i < iters; ++i)
+#pragma unroll
+    for(int k=0; k < 8; ++k) a[k]=fmaf(a[k],b,c);
+  float s=0;
+  for(int k=0; k < 8; ++k) s += a[k];
+  if(s == -1.0f) sink[0]=s;
+}
+
 // f[i][j] *= (j == 0 ? s0 : s1) on a rows x cols complex array.
 template<typename T>
 __global__ void scaleColumnsKernel(size_t rows, size_t cols, T s0, T s1,
@@ -521,6 +548,44 @@ size_t fgb_index(int kind, size_t m, size_t p, size_t q, size_t n, size_t D,
     r += i/(p*m);
   }
   return q*s+n*u+r;
+}
+
+int fgb_measure_fma_rate(double *dfma_per_s, double *ffma_per_s)
+{
+  int dev=0, nsm=0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm,cudaDevAttrMultiProcessorCount,dev);
+  cudaEvent_t e0, e1;
+  if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return -2;
+  const int blocks=nsm*8, threads=256;
+  const int itd=2048, itf=65536;
+  float ms=0;
+  double *sink=NULL;
+  if(cudaMalloc(&sink,sizeof(double)) != cudaSuccess) return -2;
+  dfmaProbe<<<blocks,threads>>>(sink,itd/8,0.999999,1e-7);   // warm-up
+  cudaEventRecord(e0);
+  dfmaProbe<<<blocks,threads>>>(sink,itd,0.999999,1e-7);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  cudaEventElapsedTime(&ms,e0,e1);
+  if(dfma_per_s) *dfma_per_s=(double) blocks*threads*8.0*itd/(ms*1e-3);
+  ffmaProbe<<<blocks,threads>>>((float *) sink,itf/8,0.9999f,1e-4f);
+  cudaEventRecord(e0);
+  ffmaProbe<<<blocks,threads>>>((float *) sink,itf,0.9999f,1e-4f);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  cudaEventElapsedTime(&ms,e0,e1);
+  if(ffma_per_s) *ffma_per_s=(double) blocks*threads*8.0*itf/(ms*1e-3);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  cudaError_t e=cudaGetLastError();
+  if(e != cudaSuccess) {
+    report("fgb_measure_fma_rate",cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
 }
 
 int fgb_scale_columns_device(size_t rows, size_t cols, double s0, double s1,

@@ -181,7 +181,9 @@ __device__ __forceinline__ void fftStage(const cplx<T> *__restrict__ x,
     cplx<T> a[R];
 #pragma unroll
     for(int r=0; r < R; ++r) a[r]=x[sp((j+r*nR)*ld+c)];
-    if(k != 0) {
+    // Uniform per stage: the first stage has no twiddles; later stages apply
+    // them to every element (W^0 = 1 exactly, so k = 0 needs no branch).
+    if(Ns > 1) {
 #pragma unroll
       for(int r=1; r < R; ++r) a[r]=twmul<S>(a[r],tw[r*k*tstride]);
     }

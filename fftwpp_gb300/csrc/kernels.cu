@@ -58,6 +58,53 @@ __device__ __forceinline__ void applyMult(int kind, cplx<T> *X, int A)
   }
 }
 
+// Compile-time input/output counts of the fixed-arity multipliers; the
+// row kernels are instantiated per multiplier so that the fused multiply is
+// straight-line code on registers (MULT_GENERIC: runtime kind and counts).
+#define MULT_GENERIC (-1)
+template<int K> struct MultArity {static const int A=0, B=0;};
+template<> struct MultArity<MULT_BINARY> {static const int A=2, B=1;};
+template<> struct MultArity<MULT_REALBINARY> {static const int A=2, B=1;};
+template<> struct MultArity<MULT_REALJACOBIAN> {static const int A=4, B=1;};
+template<> struct MultArity<MULT_REALJACADJ> {static const int A=5, B=4;};
+
+// Multiply one transformed slot: the A values at X[sp(base+a*stride)] in,
+// the B results back to X[sp(base+b*stride)].
+template<int K, typename T>
+__device__ __forceinline__ void multiplySlot(cplx<T> *X, int base, int stride,
+                                             int A, int B, int kind)
+{
+  if constexpr(MultArity<K>::A > 0) {
+    constexpr int KA=MultArity<K>::A, KB=MultArity<K>::B;
+    cplx<T> v[KA];
+#pragma unroll
+    for(int a=0; a < KA; ++a) v[a]=X[sp(base+a*stride)];
+    applyMult(K,v,KA);
+#pragma unroll
+    for(int b=0; b < KB; ++b) X[sp(base+b*stride)]=v[b];
+  } else {
+    cplx<T> v[FGB_MAXA];
+    for(int a=0; a < A; ++a) v[a]=X[sp(base+a*stride)];
+    applyMult(kind,v,A);
+    for(int b=0; b < B; ++b) X[sp(base+b*stride)]=v[b];
+  }
+}
+
+// The specialised instantiation serving a (mult, A, B), or MULT_GENERIC.
+static int multVariant(int mult, int A, int B)
+{
+  switch(mult) {
+    case MULT_BINARY: return A == 2 && B == 1 ? MULT_BINARY : MULT_GENERIC;
+    case MULT_REALBINARY:
+      return A == 2 && B == 1 ? MULT_REALBINARY : MULT_GENERIC;
+    case MULT_REALJACOBIAN:
+      return A == 4 && B == 1 ? MULT_REALJACOBIAN : MULT_GENERIC;
+    case MULT_REALJACADJ:
+      return A == 5 && B == 4 ? MULT_REALJACADJ : MULT_GENERIC;
+    default: return MULT_GENERIC;
+  }
+}
+
 // Exponent ((s-c) mod N)*r mod N of a residue twiddle.
 __device__ __forceinline__ int twExp(int s, int c, int r, int N)
 {
@@ -129,7 +176,7 @@ __device__ __forceinline__ void cpAsyncWait()
 // together as interleaved columns col = a*rpc + rho, so the B x rpc output
 // columns are a contiguous prefix for the inverse transforms.  Every thread
 // of the block calls it.
-template<typename T, bool CG>
+template<typename T, bool CG, int K>
 __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
                                            long long group,
                                            unsigned char *smemRaw)
@@ -178,10 +225,7 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
     cplx<T> *Y=X == x ? y : x;
     for(int i=tid; i < m*R; i += nthr) {
       int j=fdiv(i,invR), rho=i-j*R;
-      cplx<T> v[FGB_MAXA];
-      for(int a=0; a < A; ++a) v[a]=X[sp(j*ld+a*R+rho)];
-      applyMult(P.mult,v,A);
-      for(int b=0; b < B; ++b) X[sp(j*ld+b*R+rho)]=v[b];
+      multiplySlot<K>(X,j*ld+rho,R,A,B,P.mult);
     }
     __syncthreads();
     cplx<T> *Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
@@ -206,14 +250,14 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
   __syncthreads();
 }
 
-template<typename T>
+template<typename T, int K>
 __global__ void __launch_bounds__(256)
 rowConvKernel(const RowPlan<T> P)
 {
   extern __shared__ __align__(16) unsigned char smemRaw[];
   const long long groups=(P.nrows+P.rpc-1)/P.rpc;
   for(long long g=blockIdx.x; g < groups; g += gridDim.x)
-    rowConvRow<T,false>(P,g,smemRaw);
+    rowConvRow<T,false,K>(P,g,smemRaw);
 }
 
 // ---------------------------------------------------------------------------
@@ -223,7 +267,7 @@ rowConvKernel(const RowPlan<T> P)
 // physical values as (u[2t], u[2t+1]) pairs; the multiplier acts on those
 // doubles; the sign -1 FFT of the packed product is unpacked into the H
 // output modes (real-to-complex).
-template<typename T>
+template<typename T, int K>
 __global__ void __launch_bounds__(256)
 hermRowKernel(const HermRowPlan<T> P)
 {
@@ -266,10 +310,7 @@ hermRowKernel(const HermRowPlan<T> P)
     cplx<T> *Y=X == x ? y : x;
     for(int i=tid; i < Nh*R; i += nthr) {
       int t=fdiv(i,invR), rho=i-t*R;
-      cplx<T> v[FGB_MAXA];
-      for(int a=0; a < A; ++a) v[a]=X[sp(t*ld+a*R+rho)];
-      applyMult(P.mult,v,A);
-      for(int b=0; b < B; ++b) X[sp(t*ld+b*R+rho)]=v[b];
+      multiplySlot<K>(X,t*ld+rho,R,A,B,P.mult);
     }
     __syncthreads();
     cplx<T> *Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
@@ -555,11 +596,28 @@ __device__ __forceinline__ void rebase(Plan<T>& plan, int count, bool relIn,
   }
 }
 
-template<typename T>
+// Copy a task's plan from the problem table into shared memory (one copy per
+// CTA, read by every thread through broadcast loads) and rebase its pointers
+// there: a per-thread copy would live in local memory.
+template<typename Plan>
+__device__ __forceinline__ Plan& stagePlan(unsigned char *buf, const Plan& src)
+{
+  static_assert(sizeof(Plan) % sizeof(int) == 0, "plan size");
+  int *d=(int *) buf;
+  const int *s=(const int *) &src;
+  for(int i=threadIdx.x; i < (int) (sizeof(Plan)/sizeof(int)); i += blockDim.x)
+    d[i]=s[i];
+  return *(Plan *) buf;
+}
+
+template<typename T, int K>
 __global__ void __launch_bounds__(256)
 batchKernel(const BatchArgs<T> P)
 {
   extern __shared__ __align__(16) unsigned char smemRaw[];
+  constexpr size_t planBytes=sizeof(RowPlan<T>) > sizeof(OuterPlan<T>) ?
+    sizeof(RowPlan<T>) : sizeof(OuterPlan<T>);
+  __shared__ __align__(16) unsigned char planBuf[planBytes];
   __shared__ int slot;
   __shared__ int gaveUp;
   for(;;) {
@@ -589,30 +647,25 @@ batchKernel(const BatchArgs<T> P)
       __syncthreads();
       if(gaveUp) continue;
     }
-    switch(tk.type) {
-      case TASK_SMALL: {
-        RowPlan<T> R=B->row;
-        rebase(R,R.A,B->rel & 1,B->rel & 2,P.inBase,P.outBase);
-        rowConvRow<T,false>(R,tk.i,smemRaw);
-        break;
-      }
-      case TASK_COLFWD: {
-        OuterPlan<T> O=B->fwd;
-        rebase(O,O.count,B->rel & 4,false,P.inBase,P.outBase);
-        outerFwdTile<T,false>(O,tk.i,0,tk.j,smemRaw);
-        break;
-      }
-      case TASK_ROW: {
-        RowPlan<T> R=B->row;
-        rowConvRow<T,true>(R,tk.i,smemRaw);
-        break;
-      }
-      default: {
-        OuterPlan<T> O=B->bwd;
-        rebase(O,O.count,false,B->rel & 8,P.inBase,P.outBase);
-        outerBwdTile<T,true>(O,tk.i,tk.j,smemRaw);
-        break;
-      }
+    const int rel=B->rel;
+    if(tk.type == TASK_SMALL || tk.type == TASK_ROW) {
+      RowPlan<T>& R=stagePlan(planBuf,B->row);
+      __syncthreads();
+      if(threadIdx.x == 0 && tk.type == TASK_SMALL)
+        rebase(R,R.A,rel & 1,rel & 2,P.inBase,P.outBase);
+      __syncthreads();
+      if(tk.type == TASK_SMALL) rowConvRow<T,false,K>(R,tk.i,smemRaw);
+      else rowConvRow<T,true,K>(R,tk.i,smemRaw);
+    } else {
+      const bool fwd=tk.type == TASK_COLFWD;
+      OuterPlan<T>& O=stagePlan(planBuf,fwd ? B->fwd : B->bwd);
+      __syncthreads();
+      if(threadIdx.x == 0)
+        rebase(O,O.count,fwd && (rel & 4),!fwd && (rel & 8),P.inBase,
+               P.outBase);
+      __syncthreads();
+      if(fwd) outerFwdTile<T,false>(O,tk.i,0,tk.j,smemRaw);
+      else outerBwdTile<T,true>(O,tk.i,tk.j,smemRaw);
     }
     if(tk.type == TASK_COLFWD || tk.type == TASK_ROW) {
       __threadfence();
@@ -623,31 +676,53 @@ batchKernel(const BatchArgs<T> P)
   }
 }
 
-template<typename T>
-cudaError_t launchBatch(const BatchArgs<T>& P, int grid, int threads,
-                        size_t smem, cudaStream_t s)
+template<typename T, int K>
+static cudaError_t launchBatchK(const BatchArgs<T>& P, int grid, int threads,
+                                size_t smem, cudaStream_t s)
 {
   if(smem > 48*1024) {
-    cudaError_t e=cudaFuncSetAttribute(batchKernel<T>,
+    cudaError_t e=cudaFuncSetAttribute(batchKernel<T,K>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int) smem);
     if(e != cudaSuccess) return e;
   }
-  batchKernel<T><<<grid,threads,smem,s>>>(P);
+  batchKernel<T,K><<<grid,threads,smem,s>>>(P);
   return cudaGetLastError();
 }
 
 template<typename T>
-int batchBlocksPerSM(int threads, size_t smem)
+cudaError_t launchBatch(const BatchArgs<T>& P, int grid, int threads,
+                        size_t smem, cudaStream_t s)
+{
+  switch(multVariant(P.mult,P.A,P.B)) {
+    case MULT_BINARY: return launchBatchK<T,MULT_BINARY>(P,grid,threads,smem,s);
+    case MULT_REALBINARY:
+      return launchBatchK<T,MULT_REALBINARY>(P,grid,threads,smem,s);
+    default: return launchBatchK<T,MULT_GENERIC>(P,grid,threads,smem,s);
+  }
+}
+
+template<typename T, int K>
+static int batchBlocksK(int threads, size_t smem)
 {
   if(smem > 48*1024)
-    cudaFuncSetAttribute(batchKernel<T>,
+    cudaFuncSetAttribute(batchKernel<T,K>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize,(int) smem);
   int n=0;
-  if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n,batchKernel<T>,threads,
+  if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n,batchKernel<T,K>,threads,
                                                    smem) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
+}
+
+template<typename T>
+int batchBlocksPerSM(int threads, size_t smem, int mult, int A, int B)
+{
+  switch(multVariant(mult,A,B)) {
+    case MULT_BINARY: return batchBlocksK<T,MULT_BINARY>(threads,smem);
+    case MULT_REALBINARY: return batchBlocksK<T,MULT_REALBINARY>(threads,smem);
+    default: return batchBlocksK<T,MULT_GENERIC>(threads,smem);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -692,12 +767,19 @@ cudaError_t launchRow(const RowPlan<T>& P, int threads, long long grid,
                       cudaStream_t s)
 {
   size_t sm=rowSmem<T>(P.L,P.m,P.A,P.B,P.rpc);
-  cudaError_t e=setSmem(rowConvKernel<T>,sm);
-  if(e != cudaSuccess) return e;
   long long groups=(P.nrows+P.rpc-1)/P.rpc;
   grid=std::min(std::min(grid,groups),(long long) INT_MAX);
-  rowConvKernel<T><<<(unsigned) grid,threads,sm,s>>>(P);
-  return cudaGetLastError();
+  auto go=[&](auto kernel) {
+    cudaError_t e=setSmem(kernel,sm);
+    if(e != cudaSuccess) return e;
+    kernel<<<(unsigned) grid,threads,sm,s>>>(P);
+    return cudaGetLastError();
+  };
+  switch(multVariant(P.mult,P.A,P.B)) {
+    case MULT_BINARY: return go(rowConvKernel<T,MULT_BINARY>);
+    case MULT_REALBINARY: return go(rowConvKernel<T,MULT_REALBINARY>);
+    default: return go(rowConvKernel<T,MULT_GENERIC>);
+  }
 }
 
 template<typename T>
@@ -705,12 +787,20 @@ cudaError_t launchHermRow(const HermRowPlan<T>& P, int threads,
                           long long grid, cudaStream_t s)
 {
   size_t sm=hermRowSmem<T>(P.H,P.Nh,P.A,P.rpc);
-  cudaError_t e=setSmem(hermRowKernel<T>,sm);
-  if(e != cudaSuccess) return e;
   long long groups=(P.nrows+P.rpc-1)/P.rpc;
   grid=std::min(std::min(grid,groups),(long long) INT_MAX);
-  hermRowKernel<T><<<(unsigned) grid,threads,sm,s>>>(P);
-  return cudaGetLastError();
+  auto go=[&](auto kernel) {
+    cudaError_t e=setSmem(kernel,sm);
+    if(e != cudaSuccess) return e;
+    kernel<<<(unsigned) grid,threads,sm,s>>>(P);
+    return cudaGetLastError();
+  };
+  switch(multVariant(P.mult,P.A,P.B)) {
+    case MULT_REALBINARY: return go(hermRowKernel<T,MULT_REALBINARY>);
+    case MULT_REALJACOBIAN: return go(hermRowKernel<T,MULT_REALJACOBIAN>);
+    case MULT_REALJACADJ: return go(hermRowKernel<T,MULT_REALJACADJ>);
+    default: return go(hermRowKernel<T,MULT_GENERIC>);
+  }
 }
 
 template<typename T>
@@ -772,9 +862,15 @@ cudaError_t launchOuterRealBwd(const OuterPlan<T>& P, int threads,
   template size_t outerBwdSmem<T>(int,int,int); \
   template size_t outerRealSmem<T>(int,int,int); \
   template cudaError_t launchBatch<T>(const BatchArgs<T>&,int,int,size_t,cudaStream_t); \
-  template int batchBlocksPerSM<T>(int,size_t);
+  template int batchBlocksPerSM<T>(int,size_t,int,int,int);
 
+// Each precision may be compiled as its own translation unit (build.py
+// compiles this file twice, in parallel).
+#ifndef FGB_ONLY_FLOAT
 FGB_INSTANTIATE(double)
+#endif
+#ifndef FGB_ONLY_DOUBLE
 FGB_INSTANTIATE(float)
+#endif
 
 } // namespace fgb

@@ -123,6 +123,7 @@ struct BatchArgs {
   int *done;                // 2 counters per problem (zeroed likewise)
   int *err;                 // set when a wait gave up
   long long spinLimit;
+  int mult, A, B;           // shared by every problem of the batch
   void *inBase[FGB_MAXA];
   void *outBase[FGB_MAXA];
 };
@@ -130,7 +131,8 @@ struct BatchArgs {
 template<typename T> cudaError_t launchBatch(const BatchArgs<T>& P, int grid,
                                              int threads, size_t smem,
                                              cudaStream_t s);
-template<typename T> int batchBlocksPerSM(int threads, size_t smem);
+template<typename T> int batchBlocksPerSM(int threads, size_t smem, int mult,
+                                          int A, int B);
 
 // Host launchers (kernels.cu).
 template<typename T> cudaError_t launchRow(const RowPlan<T>& P, int threads,

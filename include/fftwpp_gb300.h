@@ -151,6 +151,12 @@ size_t fgb_index(int kind, size_t m, size_t p, size_t q, size_t n, size_t D,
 int fgb_hconv2d_convolve_noalloc(const void *f, const void *g, void *h,
                                  size_t Lx, size_t Ly, void *stream);
 
+/* Measured FP64 (DFMA) and FP32 (FFMA) instruction issue rates of the
+ * current GPU, per second, from dependent-chain probes on every SM -- the
+ * denominators of the compute roofline of the FP64-bound kernels (no
+ * reference counterpart). */
+int fgb_measure_fma_rate(double *dfma_per_s, double *ffma_per_s);
+
 /* f[i][j] *= (j == 0 ? s0 : s1) on a rows x cols complex device array: the
  * weight of the k_y = 0 column of half-plane Hermitian data, used by the
  * adjoint of the Hermitian convolutions (no reference counterpart). */
