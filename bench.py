@@ -22,6 +22,7 @@ out of scope); value = all ranks' convolutions / max-over-ranks time.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -119,60 +120,103 @@ def synth_inputs(w, seed=1):
 # Clock sampling during the timed region.
 
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+    """nvidia-smi clock/throttle samples every 50 ms; only samples stamped
+    inside the timed window (begin() .. end()) are summarised.  start()
+    returns once the first sample has arrived, so the sampler is running
+    before the window opens."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,"
               "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    STAMP = "%Y/%m/%d %H:%M:%S.%f"
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}",
                  f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE,
-                stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True, bufsize=1)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        deadline = time.time() + 5.0
+        while not self.lines and time.time() < deadline:
+            time.sleep(0.01)
+
+    def begin(self):
+        self.t0 = datetime.datetime.now()
+
+    def end(self):
+        self.t1 = datetime.datetime.now()
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def _parse(self):
+        out = []
+        for ln in list(self.lines):
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 10:
+                continue
+            try:
+                ts = datetime.datetime.strptime(parts[0], self.STAMP)
+                out.append((ts, float(parts[2]), float(parts[3]), parts[6:10]))
+            except ValueError:
+                continue
+        return out
+
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        # Let the sample that follows the window arrive, then stop.
+        deadline = time.time() + 1.0
+        while time.time() < deadline and self.t1 is not None:
+            s = self._parse()
+            if s and s[-1][0] >= self.t1:
+                break
+            time.sleep(0.02)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.thread.join(timeout=2)
-        sm, smax, reasons = [], [], set()
+        samples = self._parse()
+        t0 = self.t0 or datetime.datetime.min
+        t1 = self.t1 or datetime.datetime.max
+        inside = [x for x in samples if t0 <= x[0] <= t1]
+        window = "timed region"
+        if not inside:
+            # Window shorter than the sampling period: the first sample after
+            # it opened.
+            after = [x for x in samples if x[0] >= t0]
+            inside, window = after[:1], "first sample after the timed region opened"
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
                  "sw_power_cap"]
-        for ln in self.lines:
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-            except ValueError:
-                continue
-            for name, val in zip(names, parts[5:9]):
+        reasons = set()
+        for _, _, _, flags in inside:
+            for name, val in zip(names, flags):
                 if val.lower().startswith("active"):
                     reasons.add(name)
+        sm = [x[1] for x in inside]
+        smax = [x[2] for x in inside]
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "window": window,
+                "window_ms": ((t1 - t0).total_seconds() * 1e3
+                              if self.t0 and self.t1 else None)}
 
 
 # ---------------------------------------------------------------------------
@@ -201,6 +245,62 @@ def cpu_oracle_rate(w, budget_s, max_convs, workers):
             break
     dt = time.perf_counter() - t0
     return n * 1.0 / dt, n, dt
+
+
+def scipy_explicit(fs, w, workers):
+    """Explicit zero-padded convolution with scipy.fft (the textbook method
+    the hybrid scheme replaces): every input goes to a physical grid of at
+    least the padded size, the multiplier is applied pointwise, the product
+    is transformed back and the stored modes are kept.  Unnormalised like
+    the reference's convolve (h_k = sum_p f_p g_{k-p})."""
+    import scipy.fft as sf
+    kinds, L, M = w["kinds"], w["L"], w["M"]
+
+    def combine(us):
+        if w["mult"] in ("binary", "realbinary"):
+            return us[0] * us[1]
+        if w["mult"] == "realjacobian":
+            return us[0] * us[3] - us[1] * us[2]
+        raise ValueError(w["mult"])
+
+    if kinds == [PAD]:
+        n = sf.next_fast_len(M[0])
+        us = [sf.ifft(f, n=n, axis=-1, workers=workers) for f in fs]
+        return sf.fft(combine(us), axis=-1, workers=workers)[..., :L[0]] * n
+    if kinds == [REAL, PAD, PAD]:
+        s = [sf.next_fast_len(m, real=True) for m in M]
+        Fs = [sf.rfftn(f, s=s, workers=workers) for f in fs]
+        h = sf.irfftn(Fs[0] * Fs[1], s=s, workers=workers)
+        return h[:L[0], :L[1], :L[2]]
+    if kinds == [CENTERED, HERMITIAN]:
+        nx = sf.next_fast_len(M[0])
+        ny = sf.next_fast_len(M[1], real=True)
+        ny += ny % 2
+        x0 = L[0] // 2
+        kx = np.arange(L[0]) - x0
+        Hy = fs[0].shape[1]
+        us = []
+        for f in fs:
+            F = np.zeros((nx, ny // 2 + 1), dtype=np.complex128)
+            F[kx % nx, :Hy] = f
+            us.append(sf.irfft2(F, s=(nx, ny), workers=workers))
+        H = sf.rfft2(combine(us), workers=workers) * (nx * ny)
+        return H[kx % nx, :Hy]
+    raise ValueError("no explicit-padding baseline for this workload")
+
+
+def cpu_scipy_rate(w, budget_s, workers, fs, max_convs=64):
+    """Time scipy_explicit on the workload's inputs fs (bounded like the
+    oracle leg); returns (convs/s, n, seconds, result of the last call)."""
+    n, t0, h = 0, time.perf_counter(), None
+    while n < max_convs:
+        h = scipy_explicit(fs, w, workers)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    batch = w.get("batch", 1)
+    return n * batch / dt, n, dt, h
 
 
 def profile_figure(tag, workload, kernel, precision):
@@ -247,22 +347,29 @@ def run_reference(args, w):
     fs = synth_inputs(w, seed=7)
     if w.get("batch", 1) > 1:
         fs = [f[0] for f in fs]
-    for _ in range(args.warmup):
+    # Bound the run: about 20 s of warm-up and 120 s of timed work at most.
+    t0 = time.perf_counter()
+    H.convolve(fs, w["kinds"], w["L"], w["M"], mult=w["mult"],
+               workers=workers)
+    est = time.perf_counter() - t0
+    nwarm = min(args.warmup, max(1, int(20.0 / est))) - 1
+    ntimed = min(args.steps, max(1, int(120.0 / est)))
+    for _ in range(nwarm):
         H.convolve(fs, w["kinds"], w["L"], w["M"], mult=w["mult"],
                    workers=workers)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(ntimed):
         H.convolve(fs, w["kinds"], w["L"], w["M"], mult=w["mult"],
                    workers=workers)
     dt = time.perf_counter() - t0
-    value = args.steps / dt
-    sample = (f"{args.steps} timed single convolutions of the workload "
+    value = ntimed / dt
+    sample = (f"{ntimed} timed single convolutions of the workload "
               f"(numpy/scipy.fft restatement of FFTW++'s hybrid convolution, "
               f"scipy workers={workers})")
     line = {
         "impl": "reference", "metric": METRIC, "value": value,
         "unit": "convs/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "warmup": args.warmup, "ms_per_step": dt / ntimed * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": w["desc"], "parallelism": "cpu"},
@@ -275,13 +382,28 @@ def run_reference(args, w):
     return 0
 
 
-def time_device(conv, ts, steps, warmup, flush, timing=True):
-    """Per-step CUDA-event timing on the current stream; returns total ms."""
+def barrier_sync(world):
+    """Barrier across ranks (when there are several) and a device sync."""
+    import torch
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+
+def time_device(conv, ts, steps, warmup, flush, timing=True, clocks=None,
+                world=1):
+    """Per-step CUDA-event timing on the current stream; returns total ms.
+    The timed loop is bracketed by a barrier and a device sync on both
+    sides; `clocks` (a started ClockSampler) is told when it opens and
+    closes."""
     import torch
     stream = torch.cuda.current_stream()
     for _ in range(warmup):
         conv.convolve(*ts)
-    torch.cuda.synchronize()
+    barrier_sync(world)
+    if clocks:
+        clocks.begin()
     if timing:
         conv.enable_timing(True)
     total = 0.0
@@ -297,6 +419,9 @@ def time_device(conv, ts, steps, warmup, flush, timing=True):
         total += start.elapsed_time(stop)
         if timing:
             conv.collect_timing()
+    barrier_sync(world)
+    if clocks:
+        clocks.end()
     if timing:
         conv.enable_timing(False)
     return total, outs
@@ -323,19 +448,18 @@ def run_ours(args, w):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
     clocks = ClockSampler(local) if rank == 0 else None
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
     if clocks:
         clocks.start()
-    total_ms, outs = time_device(conv, ts, args.steps, args.warmup, flush)
+    total_ms, outs = time_device(conv, ts, args.steps, args.warmup, flush,
+                                 clocks=clocks, world=world)
     clk = clocks.stop() if clocks else None
     if world > 1:
         t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
         torch.distributed.barrier()
-    value = world * args.steps / (total_ms * 1e-3)
+    nb = w.get("batch", 1)          # convolutions per step
+    value = world * nb * args.steps / (total_ms * 1e-3)
 
     names = conv.launch_names()
     kms = conv.kernel_ms()
@@ -424,7 +548,7 @@ def run_ours(args, w):
                              n=12)
         else:
             e32 = None
-        extra["fp32_compensated"] = {"value": args.steps / (ms32 * 1e-3),
+        extra["fp32_compensated"] = {"value": nb * args.steps / (ms32 * 1e-3),
                                      "unit": "convs/s",
                                      "rel_l2_vs_fp64_oracle": e32,
                                      "speedup_vs_fp64": (args.steps / ms32) /
@@ -453,7 +577,7 @@ def run_ours(args, w):
             lib.fftwpp_hconv2d_convolve(h, pa, pb)
             tot += time.perf_counter() - t0
         e2e_err = rel_l2(A_.view(np.complex128).reshape(fs[0].shape), want)
-        e2e = {"value": args.steps / tot, "unit": "convs/s",
+        e2e = {"value": nb * args.steps / tot, "unit": "convs/s",
                "h2d_bytes_per_step": 2 * n * 16, "d2h_bytes_per_step": n * 16,
                "api": "fftwpp_hconv2d_convolve (host pointers)",
                "rel_l2_vs_oracle": e2e_err}
@@ -471,17 +595,26 @@ def run_ours(args, w):
             t0 = time.perf_counter()
             conv.convolve_host(*hs)
             tot += time.perf_counter() - t0
-        nb = host[0].nbytes
-        e2e = {"value": args.steps / tot, "unit": "convs/s",
-               "h2d_bytes_per_step": w["A"] * nb,
-               "d2h_bytes_per_step": w["B"] * nb,
+        nbytes = host[0].nbytes
+        e2e = {"value": nb * args.steps / tot, "unit": "convs/s",
+               "h2d_bytes_per_step": w["A"] * nbytes,
+               "d2h_bytes_per_step": w["B"] * nbytes,
                "api": "fgb_convolve_host (host pointers)"}
 
-    if big:
-        cpu_rate, cpu_n, cpu_dt = None, 0, 0.0
-    else:
-        cpu_rate, cpu_n, cpu_dt = cpu_oracle_rate(w, args.cpu_budget, 64,
-                                                  os.cpu_count() or 1)
+    cpu_rate, cpu_n, cpu_dt = cpu_oracle_rate(w, args.cpu_budget, 64,
+                                              os.cpu_count() or 1)
+    sp_rate, sp_n, sp_dt, sp_h = cpu_scipy_rate(w, args.cpu_budget,
+                                                os.cpu_count() or 1, fs)
+    sp_first = sp_h[0] if w.get("batch", 1) > 1 else sp_h
+    ours_first = (outs[0][0] if w.get("batch", 1) > 1 else outs[0])
+    scipy_point = {
+        "value": sp_rate, "unit": "convs/s", "cores": os.cpu_count() or 1,
+        "label": "scipy explicit-padding CPU",
+        "sample": f"{sp_n} calls in {sp_dt:.1f} s (scipy.fft, zero-padded "
+                  f"physical grids, workers={os.cpu_count() or 1})",
+        "rel_l2_gpu_vs_scipy": rel_l2(
+            ours_first.cpu().numpy().astype(np.result_type(sp_first)),
+            sp_first)}
     line = {
         "metric": METRIC, "value": value, "unit": "convs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -501,6 +634,7 @@ def run_ours(args, w):
                          "sample": f"{cpu_n} single convolutions of the same "
                                    f"workload in {cpu_dt:.1f} s (numpy/scipy.fft "
                                    f"restatement of FFTW++'s hybrid convolution)"},
+        "cpu_scipy_explicit": scipy_point,
         "e2e": e2e,
         "gpu_launches": conv.launches * args.steps,
         "clocks": clk,
@@ -519,31 +653,124 @@ def batched_lengths(n=512, lo=64, hi=65536, seed=2024):
             rng.uniform(np.log(lo), np.log(hi), n)]
 
 
+def batched_job(world):
+    """The whole batched job at `world` ranks: one 512-problem batch per rank
+    (seeds 2024, 2025, ...), so per-rank work stays fixed as ranks are added.
+    Returns the lengths and the packed inputs f, g (iid U[-1,1])."""
+    Ls = []
+    for s in range(world):
+        Ls += batched_lengths(seed=2024 + s)
+    rng = np.random.default_rng(3)
+    tot = sum(Ls)
+    f = rng.uniform(-1, 1, tot) + 1j * rng.uniform(-1, 1, tot)
+    g = rng.uniform(-1, 1, tot) + 1j * rng.uniform(-1, 1, tot)
+    return Ls, f, g
+
+
+BATCHED_DESC = ("512 independent 1D complex binary convolutions per GPU, L "
+                "log-uniform in [64, 65536] (seed 2024 + shard), M=2L-1, "
+                "sharded across ranks by cost (L log L), one persistent launch "
+                "per step replayed from a CUDA graph, autotuned plans")
+
+
+def oracle_batch_rate(Ls, f, g, budget_s, workers, stride=None):
+    """Time the CPU restatement over a bounded, evenly strided sample of the
+    batch's problems; returns (convs/s, problems timed, seconds, stride).
+    Without a stride, one is chosen from a calibration pass over every 16th
+    problem so that the sample takes about budget_s."""
+    from oracle import hybrid as H
+    from fftwpp_gb300.sharding import offsets
+    off = offsets(Ls)
+    if stride is None:
+        t0 = time.perf_counter()
+        for i in range(0, len(Ls), 16):
+            o, L = off[i], Ls[i]
+            H.convolve([f[o:o + L], g[o:o + L]], [H.PAD], [L], [2 * L - 1],
+                       workers=workers)
+        per = (time.perf_counter() - t0) / len(range(0, len(Ls), 16))
+        stride = max(1, int(np.ceil(per * len(Ls) / max(budget_s, 1e-3))))
+    idx = list(range(0, len(Ls), stride))
+    t0 = time.perf_counter()
+    for i in idx:
+        o, L = off[i], Ls[i]
+        H.convolve([f[o:o + L], g[o:o + L]], [H.PAD], [L], [2 * L - 1],
+                   workers=workers)
+    dt = time.perf_counter() - t0
+    return len(idx) / dt, len(idx), dt, stride
+
+
+def run_reference_batched(args):
+    """--impl reference for the batched workload: the CPU restatement over
+    the same problem distribution, one bounded strided sample per step."""
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    workers = os.cpu_count() or 1
+    Ls, f, g = batched_job(1)
+    budget = max(1.0, 120.0 / max(args.steps + args.warmup, 1))
+    n = 0
+    dt = 0.0
+    stride = None
+    for it in range(args.warmup + args.steps):
+        rate, k, t, stride = oracle_batch_rate(Ls, f, g, budget, workers,
+                                               stride)
+        if it >= args.warmup:
+            n += k
+            dt += t
+    value = n / dt
+    sample = (f"a stride-{stride} sample of the 512 problems per step "
+              f"(numpy/scipy.fft restatement of FFTW++'s hybrid convolution, "
+              f"scipy workers={workers})")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value,
+        "unit": "convs/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": BATCHED_DESC, "parallelism": "cpu"},
+        "cpu_baseline": {"value": value, "unit": "convs/s", "cores": workers,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "convs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_batched(args):
     """Batched uneven 1D complex binary convolutions: one persistent launch
-    replayed from a CUDA graph, against the same problems launched one plain
-    convolution at a time."""
+    per rank replayed from a CUDA graph, against the same problems launched
+    one plain convolution at a time."""
     import torch
-    torch.cuda.set_device(0)
-    from fftwpp_gb300.gpu import BatchedConvolution, HybridConvolution
-    Ls = batched_lengths()
+    world, rank, local = dist_setup()
+    if world > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from fftwpp_gb300.gpu import HybridConvolution
+    from fftwpp_gb300.sharding import ShardedBatch
+    Lall, fall, gall = batched_job(world)
     prec = args.precision
-    conv = BatchedConvolution(Ls, precision=prec, tune=True)
-    rng = np.random.default_rng(3)
-    f = rng.uniform(-1, 1, conv.total) + 1j * rng.uniform(-1, 1, conv.total)
-    g = rng.uniform(-1, 1, conv.total) + 1j * rng.uniform(-1, 1, conv.total)
+    shard = ShardedBatch(Lall, rank, world, precision=prec, tune=True)
+    conv = shard.conv
+    Ls = shard.local_lengths
+    f, g = shard.local(fall), shard.local(gall)
     tf = torch.from_numpy(f).to(conv.dtype).cuda()
     tg = torch.from_numpy(g).to(conv.dtype).cuda()
     out = [torch.empty_like(tf)]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
+    clocks = ClockSampler(local) if rank == 0 else None
+    if clocks:
+        clocks.start()
     for _ in range(args.warmup):
         conv.convolve(tf, tg, out=out, graph=True)
-    torch.cuda.synchronize()
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler(0)
-    clocks.start()
+    barrier_sync(world)
+    if clocks:
+        clocks.begin()
     total = 0.0
     for _ in range(args.steps):
         flush.zero_()
@@ -552,11 +779,48 @@ def run_batched(args):
         stop.record(stream)
         stop.synchronize()
         total += start.elapsed_time(stop)
-    clk = clocks.stop()
-    assert conv.error() == 0
-    value = len(Ls) * args.steps / (total * 1e-3)
+    barrier_sync(world)
+    if clocks:
+        clocks.end()
+    clk = clocks.stop() if clocks else None
+    if conv.error() != 0:
+        raise RuntimeError("a wait of the persistent kernel gave up")
+    if world > 1:
+        t = torch.tensor([total], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total = float(t.item())
+    value = len(Lall) * args.steps / (total * 1e-3)
 
-    # Accuracy on a sample of problems against the FP64 oracle.
+    # End to end through the public API: page-locked host inputs copied in,
+    # one graph-replayed launch, the outputs copied back, every step.
+    hf = torch.from_numpy(f).to(conv.dtype).pin_memory()
+    hg = torch.from_numpy(g).to(conv.dtype).pin_memory()
+    ho = torch.empty_like(hf).pin_memory()
+    barrier_sync(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        tf.copy_(hf, non_blocking=True)
+        tg.copy_(hg, non_blocking=True)
+        conv.convolve(tf, tg, out=out, graph=True)
+        ho.copy_(out[0], non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_dt = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_dt], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_dt = float(t.item())
+    elem = 16 if prec == "f64" else 8
+    e2e = {"value": len(Lall) * args.steps / e2e_dt, "unit": "convs/s",
+           "h2d_bytes_per_step": 2 * elem * shard.local_total,
+           "d2h_bytes_per_step": elem * shard.local_total,
+           "api": "fftwpp_gb300.sharding.ShardedBatch / BatchedConvolution "
+                  "on page-locked host tensors (copies inside the timed loop)"}
+
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return 0
+
+    # Accuracy on a sample of this rank's problems against the FP64 oracle.
     from oracle import hybrid as H
     from oracle.direct import rel_l2
     h = out[0].cpu().numpy()
@@ -579,7 +843,7 @@ def run_batched(args):
             p.convolve(a, b, out=[c])
         torch.cuda.synchronize()
         t = 0.0
-        reps = max(1, args.steps // 5)
+        reps = max(1, min(args.steps // 5, 20))
         for _ in range(reps):
             flush.zero_()
             start.record(stream)
@@ -592,47 +856,65 @@ def run_batched(args):
 
     sep_same, sep_launches = separate(prec)
     sep_f64, _ = separate("f64") if prec != "f64" else (sep_same, None)
-    elem = 16 if prec == "f64" else 8
-    abytes = 3 * elem * conv.total
+    abytes = 3 * elem * shard.local_total
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    peak = peaks.get("hbm_gbs", 6800.0)
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured"
+    if not peak:
+        peak, peak_src = 6800.0, "fallback"
     achieved = abytes / (total / args.steps * 1e-3) / 1e9
+    cpu = None
+    if world == 1:
+        rate, k, dt, stride = oracle_batch_rate(Ls, f, g, args.cpu_budget,
+                                                os.cpu_count() or 1)
+        cpu = {"value": rate, "unit": "convs/s", "cores": os.cpu_count() or 1,
+               "kind": "port",
+               "sample": f"a stride-{stride} sample of the 512 problems ({k} "
+                         f"convolutions, {dt:.1f} s; numpy/scipy.fft "
+                         f"restatement of FFTW++'s hybrid convolution)"}
     line = {
-        "metric": METRIC, "value": value, "unit": "convs/s", "n_gpus": 1,
+        "metric": METRIC, "value": value, "unit": "convs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": prec,
         "data": "synthetic (seeded)",
-        "config": {"workload": "512 independent 1D complex binary convolutions,"
-                               " L log-uniform in [64, 65536] (seed 2024), "
-                               "M=2L-1, one persistent launch per step "
-                               "replayed from a CUDA graph, autotuned plans",
+        "config": {"workload": BATCHED_DESC,
+                   "parallelism": f"shards x{world} (no data-path collective)",
                    "l2": "flushed (256 MB write) before every timed step",
-                   "total_length": conv.total, "tasks": conv.tasks,
-                   "grid": conv.grid, "short_problems": conv.short_problems,
+                   "problems": len(Lall), "rank0_problems": len(Ls),
+                   "rank0_total_length": shard.local_total,
+                   "tasks": conv.tasks, "grid": conv.grid,
+                   "short_problems": conv.short_problems,
                    "long_problems": conv.long_problems},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                     "kernel": "batchKernel",
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic_from_profiles("batched1d", "batch",
+                                                      prec),
+                     "kernel": "batchKernel", "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": abytes},
         "rel_l2_vs_fp64_oracle_max_sample": max(errs),
         "separate_plain_launches": {"value": sep_same, "unit": "convs/s",
                                     "launches_per_step": sep_launches,
-                                    "batched_speedup": value / sep_same},
+                                    "batched_speedup": value / world / sep_same},
         "plain_fp64_separate_launches": {"value": sep_f64, "unit": "convs/s",
-                                         "batched_speedup": value / sep_f64},
+                                         "batched_speedup":
+                                         value / world / sep_f64},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
         "gpu_launches": args.steps,
         "clocks": clk,
     }
     print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
     return 0
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hconv2d",
@@ -646,10 +928,7 @@ def main():
         args.warmup = 3
     if args.workload == "batched1d":
         if args.impl == "reference":
-            return run_reference(args, dict(
-                kinds=[PAD], L=[4096], M=[8191], mult="binary", A=2, B=1,
-                desc="one 1D complex binary convolution L=4096 (a sample of "
-                     "the batched workload)"))
+            return run_reference_batched(args)
         return run_batched(args)
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
