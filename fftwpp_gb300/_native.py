@@ -15,7 +15,8 @@ LIB_PATH = os.path.join(HERE, "lib_fftwpp.so")
 PAD, CENTERED, HERMITIAN, REAL = 0, 1, 2, 3
 F64, F32 = 0, 1
 MULT = {"none": 0, "binary": 1, "realbinary": 2, "correlation": 3,
-        "realjacobian": 4, "jacobian": 5, "realjacadj": 6, "dot": 7}
+        "realjacobian": 4, "jacobian": 5, "realjacadj": 6, "dot": 7,
+        "realdot": 8}
 
 _lib = None
 
@@ -76,6 +77,18 @@ def load():
     lib.fgb_batch_error.argtypes = [vp]
     lib.fgb_batch_destroy.restype = None
     lib.fgb_batch_destroy.argtypes = [vp]
+    lib.fgb_pad_create.restype = vp
+    lib.fgb_pad_create.argtypes = [ctypes.c_int, sz, sz, sz, sz, ctypes.c_int]
+    lib.fgb_pad_forward_device.restype = ctypes.c_int
+    lib.fgb_pad_forward_device.argtypes = [vp, vp, vp, vp]
+    lib.fgb_pad_backward_device.restype = ctypes.c_int
+    lib.fgb_pad_backward_device.argtypes = [vp, vp, vp, vp]
+    lib.fgb_pad_info.restype = ctypes.c_int
+    lib.fgb_pad_info.argtypes = [vp, P(ctypes.c_long)]
+    lib.fgb_pad_index.restype = sz
+    lib.fgb_pad_index.argtypes = [vp, sz, sz]
+    lib.fgb_pad_destroy.restype = None
+    lib.fgb_pad_destroy.argtypes = [vp]
     lib.fgb_destroy.restype = None
     lib.fgb_destroy.argtypes = [vp]
     lib.fgb_last_error.restype = ctypes.c_char_p
@@ -103,6 +116,28 @@ def load():
         delete = getattr(lib, f"fftwpp_{name}_delete")
         delete.restype = None
         delete.argtypes = [vp]
+        # Dot-product and work-array forms (declared in FFTW++'s header).
+        cdot = getattr(lib, f"fftwpp_create_{name}_dot")
+        cdot.restype = vp
+        cdot.argtypes = [sz] * dims + [sz]
+        nwork = {"conv1d": 2, "hconv1d": 3, "conv2d": 4, "hconv2d": 5,
+                 "conv3d": 6, "hconv3d": 7}[name]
+        cwork = getattr(lib, f"fftwpp_create_{name}_work")
+        cwork.restype = vp
+        cwork.argtypes = [sz] * dims + [vp] * nwork
+        if name != "conv3d":
+            cwd = getattr(lib, f"fftwpp_create_{name}_work_dot")
+            cwd.restype = vp
+            cwd.argtypes = [sz] * dims + [vp] * nwork + [sz]
+        dot = getattr(lib, f"fftwpp_{name}_convolve_dot")
+        dot.restype = None
+        dot.argtypes = [vp, P(vp), P(vp)]
+        if name != "hconv3d":
+            dotf = getattr(lib, f"fftwpp_{name}_convolve_dotf")
+            dotf.restype = None
+            dotf.argtypes = [vp, vp, vp]
+    lib.create_doublealign.restype = vp
+    lib.create_doublealign.argtypes = [sz]
     lib.fftwpp_HermitianSymmetrize.argtypes = [vp]
     lib.fftwpp_HermitianSymmetrizeX.argtypes = [sz, sz, sz, vp]
     lib.fftwpp_HermitianSymmetrizeXY.argtypes = [sz, sz, sz, sz, sz, vp]

@@ -16,9 +16,19 @@
 
 using namespace fgb;
 
+struct fgb_pad {
+  std::unique_ptr<PadTransform> t;
+};
+
 struct fgb_conv {
   std::unique_ptr<Conv> conv;
   cudaStream_t stream;
+  // Dot-product handles (the *_dot entry points): products summed per call;
+  // 0 for a plain handle.  Sums of more than FGB_MAXA/2 products run in
+  // chunks of the plan's A/2 pairs, accumulated on the device.
+  size_t pairs=0;
+  std::vector<void *> dotBuf;     // device: A chunk inputs, accumulator, temp
+  ~fgb_conv() {for(void *p : dotBuf) cudaFree(p);}
 };
 
 namespace {
@@ -104,6 +114,105 @@ int convolveHost(fgb_conv *c, void *a, void *b, const char *where)
     return -2;
   }
   return 0;
+}
+
+__global__ void accumulateKernel(double *acc, const double *t, size_t n)
+{
+  for(size_t i=blockIdx.x*(size_t) blockDim.x+threadIdx.x; i < n;
+      i += (size_t) gridDim.x*blockDim.x)
+    acc[i] += t[i];
+}
+
+// A handle summing `pairs` binary products (realdot: lane-wise on doubles,
+// for Hermitian data).  The old FFTW++ C interface declares these entry
+// points without defining them (wrappers/cfftw++.h:30-47, 53-71, 77-99,
+// 104-129, 136-153, 161-188); the sum of products is the convolution of
+// the dot product, h = sum_k a_k * b_k.
+long defaultM(int kind, long L);
+
+fgb_conv *makeDot(int dim, const int *kinds, const long *L, size_t pairs,
+                  bool hermitian, const char *where)
+{
+  if(pairs < 1) {report(where,"the number of products must be positive");
+    return NULL;}
+  long Ms[3];
+  for(int d=0; d < dim; ++d) Ms[d]=defaultM(kinds[d],L[d]);
+  int K=(int) std::min<size_t>(pairs,FGB_MAXA/2);
+  fgb_conv *c=make(dim,kinds,L,Ms,NULL,2*K,1,
+                   hermitian ? MULT_REALDOT : MULT_DOT,PREC_F64,1,where);
+  if(c) c->pairs=pairs;
+  return c;
+}
+
+// a[k], b[k] (k < pairs): host arrays of the stored layout; the sum of the
+// pairs' convolutions overwrites a[0].
+int convolveDot(fgb_conv *c, void *const *a, void *const *b,
+                const char *where)
+{
+  if(!c) {report(where,"null handle"); return -1;}
+  if(c->pairs == 0) return convolveHost(c,a[0],b[0],where);
+  Conv& C=*c->conv;
+  const int K=C.info().A/2;
+  const size_t bytes=C.elements()*C.elemBytes();
+  cudaStream_t s=c->stream;
+  cudaError_t e=cudaSuccess;
+  if(c->dotBuf.empty()) {
+    c->dotBuf.assign(2*K+2,NULL);
+    for(void *&p : c->dotBuf)
+      if(e == cudaSuccess) e=cudaMalloc(&p,bytes);
+    if(e != cudaSuccess) {
+      for(void *&p : c->dotBuf) {if(p) cudaFree(p); p=NULL;}
+      c->dotBuf.clear();
+      report(where,cudaGetErrorString(e));
+      return -2;
+    }
+  }
+  void **in=c->dotBuf.data();
+  void *acc=c->dotBuf[2*K], *tmp=c->dotBuf[2*K+1];
+  for(size_t c0=0; c0 < c->pairs && e == cudaSuccess; c0 += K) {
+    for(int k=0; k < K && e == cudaSuccess; ++k) {
+      if(c0+k < c->pairs) {
+        e=cudaMemcpyAsync(in[k],a[c0+k],bytes,cudaMemcpyHostToDevice,s);
+        if(e == cudaSuccess)
+          e=cudaMemcpyAsync(in[K+k],b[c0+k],bytes,cudaMemcpyHostToDevice,s);
+      } else {        // a short last chunk: zero pairs add nothing
+        e=cudaMemsetAsync(in[k],0,bytes,s);
+        if(e == cudaSuccess) e=cudaMemsetAsync(in[K+k],0,bytes,s);
+      }
+    }
+    if(e != cudaSuccess) break;
+    void *out[1]={c0 == 0 ? acc : tmp};
+    e=C.run(in,out,s);
+    if(e == cudaSuccess && c0 > 0) {
+      size_t n=bytes/sizeof(double);
+      unsigned grid=(unsigned) std::min<size_t>((n+255)/256,4096);
+      accumulateKernel<<<grid,256,0,s>>>((double *) acc,(const double *) tmp,
+                                         n);
+      e=cudaGetLastError();
+    }
+  }
+  if(e == cudaSuccess)
+    e=cudaMemcpyAsync(a[0],acc,bytes,cudaMemcpyDeviceToHost,s);
+  if(e == cudaSuccess) e=cudaStreamSynchronize(s);
+  if(e != cudaSuccess) {
+    report(where,cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
+// *_dotf: the pairs' arrays back to back in one flat array each.
+int convolveDotFlat(fgb_conv *c, void *a, void *b, const char *where)
+{
+  if(!c) {report(where,"null handle"); return -1;}
+  size_t P=c->pairs ? c->pairs : 1;
+  size_t bytes=c->conv->elements()*c->conv->elemBytes();
+  std::vector<void *> pa(P), pb(P);
+  for(size_t k=0; k < P; ++k) {
+    pa[k]=(char *) a+k*bytes;
+    pb[k]=(char *) b+k*bytes;
+  }
+  return convolveDot(c,pa.data(),pb.data(),where);
 }
 
 long defaultM(int kind, long L)
@@ -333,6 +442,155 @@ void fftwpp_hconv3d_convolve(void *c, void *a, void *b)
 }
 
 // ---------------------------------------------------------------------------
+// Dot-product and work-array forms declared by the old FFTW++ C interface
+// (wrappers/cfftw++.h).  m: data length per axis as in the plain forms;
+// M: number of products summed.  The work arrays u, v, w were host scratch
+// of the CPU implementation; device scratch is allocated internally, so
+// they are accepted and not used.
+
+double *create_doublealign(size_t n) {return create_doubleAlign(n);}
+
+void *fftwpp_create_conv1d_dot(size_t m, size_t M)
+{
+  int k[]={KIND_PAD};
+  long Ls[]={(long) m};
+  return makeDot(1,k,Ls,M,false,"fftwpp_create_conv1d_dot");
+}
+void *fftwpp_create_conv1d_work(size_t m, void *, void *)
+{
+  return fftwpp_create_conv1d(m);
+}
+void *fftwpp_create_conv1d_work_dot(size_t m, void *, void *, size_t M)
+{
+  return fftwpp_create_conv1d_dot(m,M);
+}
+void fftwpp_conv1d_convolve_dot(void *c, void **a, void **b)
+{
+  convolveDot((fgb_conv *) c,a,b,"fftwpp_conv1d_convolve_dot");
+}
+void fftwpp_conv1d_convolve_dotf(void *c, void *a, void *b)
+{
+  convolveDotFlat((fgb_conv *) c,a,b,"fftwpp_conv1d_convolve_dotf");
+}
+
+void *fftwpp_create_hconv1d_dot(size_t m, size_t M)
+{
+  int k[]={KIND_HERMITIAN};
+  long Ls[]={(long) m};
+  return makeDot(1,k,Ls,M,true,"fftwpp_create_hconv1d_dot");
+}
+void *fftwpp_create_hconv1d_work(size_t m, void *, void *, void *)
+{
+  return fftwpp_create_hconv1d(m);
+}
+void *fftwpp_create_hconv1d_work_dot(size_t m, void *, void *, void *,
+                                     size_t M)
+{
+  return fftwpp_create_hconv1d_dot(m,M);
+}
+void fftwpp_hconv1d_convolve_dot(void *c, void **a, void **b)
+{
+  convolveDot((fgb_conv *) c,a,b,"fftwpp_hconv1d_convolve_dot");
+}
+void fftwpp_hconv1d_convolve_dotf(void *c, void *a, void *b)
+{
+  convolveDotFlat((fgb_conv *) c,a,b,"fftwpp_hconv1d_convolve_dotf");
+}
+
+void *fftwpp_create_conv2d_dot(size_t mx, size_t my, size_t M)
+{
+  int k[]={KIND_PAD,KIND_PAD};
+  long Ls[]={(long) mx,(long) my};
+  return makeDot(2,k,Ls,M,false,"fftwpp_create_conv2d_dot");
+}
+void *fftwpp_create_conv2d_work(size_t mx, size_t my, void *, void *, void *,
+                                void *)
+{
+  return fftwpp_create_conv2d(mx,my);
+}
+void *fftwpp_create_conv2d_work_dot(size_t mx, size_t my, void *, void *,
+                                    void *, void *, size_t M)
+{
+  return fftwpp_create_conv2d_dot(mx,my,M);
+}
+void fftwpp_conv2d_convolve_dot(void *c, void **a, void **b)
+{
+  convolveDot((fgb_conv *) c,a,b,"fftwpp_conv2d_convolve_dot");
+}
+void fftwpp_conv2d_convolve_dotf(void *c, void *a, void *b)
+{
+  convolveDotFlat((fgb_conv *) c,a,b,"fftwpp_conv2d_convolve_dotf");
+}
+
+void *fftwpp_create_hconv2d_dot(size_t mx, size_t my, size_t M)
+{
+  int k[]={KIND_CENTERED,KIND_HERMITIAN};
+  long Ls[]={(long) mx,(long) my};
+  return makeDot(2,k,Ls,M,true,"fftwpp_create_hconv2d_dot");
+}
+void *fftwpp_create_hconv2d_work(size_t mx, size_t my, void *, void *, void *,
+                                 void *, void *)
+{
+  return fftwpp_create_hconv2d(mx,my);
+}
+void *fftwpp_create_hconv2d_work_dot(size_t mx, size_t my, void *, void *,
+                                     void *, void *, void *, size_t M)
+{
+  return fftwpp_create_hconv2d_dot(mx,my,M);
+}
+void fftwpp_hconv2d_convolve_dot(void *c, void **a, void **b)
+{
+  convolveDot((fgb_conv *) c,a,b,"fftwpp_hconv2d_convolve_dot");
+}
+void fftwpp_hconv2d_convolve_dotf(void *c, void *a, void *b)
+{
+  convolveDotFlat((fgb_conv *) c,a,b,"fftwpp_hconv2d_convolve_dotf");
+}
+
+void *fftwpp_create_conv3d_dot(size_t mx, size_t my, size_t mz, size_t M)
+{
+  int k[]={KIND_PAD,KIND_PAD,KIND_PAD};
+  long Ls[]={(long) mx,(long) my,(long) mz};
+  return makeDot(3,k,Ls,M,false,"fftwpp_create_conv3d_dot");
+}
+void *fftwpp_create_conv3d_work(size_t mx, size_t my, size_t mz, void *,
+                                void *, void *, void *, void *, void *)
+{
+  return fftwpp_create_conv3d(mx,my,mz);
+}
+void fftwpp_conv3d_convolve_dot(void *c, void **a, void **b)
+{
+  convolveDot((fgb_conv *) c,a,b,"fftwpp_conv3d_convolve_dot");
+}
+void fftwpp_conv3d_convolve_dotf(void *c, void *a, void *b)
+{
+  convolveDotFlat((fgb_conv *) c,a,b,"fftwpp_conv3d_convolve_dotf");
+}
+
+void *fftwpp_create_hconv3d_dot(size_t mx, size_t my, size_t mz, size_t M)
+{
+  int k[]={KIND_CENTERED,KIND_CENTERED,KIND_HERMITIAN};
+  long Ls[]={(long) mx,(long) my,(long) mz};
+  return makeDot(3,k,Ls,M,true,"fftwpp_create_hconv3d_dot");
+}
+void *fftwpp_create_hconv3d_work(size_t mx, size_t my, size_t mz, void *,
+                                 void *, void *, void *, void *, void *,
+                                 void *)
+{
+  return fftwpp_create_hconv3d(mx,my,mz);
+}
+void *fftwpp_create_hconv3d_work_dot(size_t mx, size_t my, size_t mz, void *,
+                                     void *, void *, void *, void *, void *,
+                                     void *, size_t M)
+{
+  return fftwpp_create_hconv3d_dot(mx,my,mz,M);
+}
+void fftwpp_hconv3d_convolve_dot(void *c, void **a, void **b)
+{
+  convolveDot((fgb_conv *) c,a,b,"fftwpp_hconv3d_convolve_dot");
+}
+
+// ---------------------------------------------------------------------------
 // Device-pointer API (include/fftwpp_gb300.h).
 
 fgb_conv *fgb_create(int dim, const int *kinds, const size_t *L,
@@ -480,6 +738,64 @@ int fgb_batch_error(fgb_batch *h)
 }
 
 void fgb_batch_destroy(fgb_batch *h) {delete h;}
+
+// Standalone padded transforms (engine.h, class PadTransform).
+fgb_pad *fgb_pad_create(int kind, size_t L, size_t M, size_t C, size_t m,
+                        int precision)
+{
+  try {
+    fgb_pad *h=new fgb_pad;
+    h->t.reset(new PadTransform(kind,(long) L,(long) M,(long) C,(long) m,
+                                precision));
+    return h;
+  } catch(std::exception& e) {
+    report("fgb_pad_create",e.what());
+    return NULL;
+  }
+}
+
+int fgb_pad_forward_device(fgb_pad *h, const void *f, void *F, void *stream)
+{
+  if(!h || !f || !F) {report("fgb_pad_forward_device","null argument");
+    return -1;}
+  cudaError_t e=h->t->forward(f,F,(cudaStream_t) stream);
+  if(e != cudaSuccess) {
+    report("fgb_pad_forward_device",cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
+int fgb_pad_backward_device(fgb_pad *h, const void *F, void *f, void *stream)
+{
+  if(!h || !f || !F) {report("fgb_pad_backward_device","null argument");
+    return -1;}
+  cudaError_t e=h->t->backward(F,f,(cudaStream_t) stream);
+  if(e != cudaSuccess) {
+    report("fgb_pad_backward_device",cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
+int fgb_pad_info(const fgb_pad *h, long *info)
+{
+  if(!h || !info) {report("fgb_pad_info","null argument"); return -1;}
+  const AxisPlan& a=h->t->plan();
+  long v[10]={a.m,a.p,a.q,a.N,a.L,h->t->columns(),a.rows,a.cshift,a.tile,
+              a.tileB};
+  for(int i=0; i < 10; ++i) info[i]=v[i];
+  return 0;
+}
+
+size_t fgb_pad_index(const fgb_pad *h, size_t r, size_t j)
+{
+  if(!h) return 0;
+  const AxisPlan& a=h->t->plan();
+  return a.kind == KIND_REAL ? j : a.q*j+r;
+}
+
+void fgb_pad_destroy(fgb_pad *h) {delete h;}
 
 const char *fgb_last_error(void)
 {

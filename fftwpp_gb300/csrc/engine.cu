@@ -2,6 +2,7 @@
 #include "engine.h"
 #include "kernels.cuh"
 
+#include <climits>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -378,6 +379,25 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
   if(prec != PREC_F64 && prec != PREC_F32)
     throw std::runtime_error("unknown precision");
   if(batch < 1) throw std::runtime_error("batch must be positive");
+  switch(mult) {
+    case MULT_NONE: break;
+    case MULT_BINARY: case MULT_REALBINARY: case MULT_CORRELATION:
+      if(A < 2) throw std::runtime_error("a binary multiplier needs A >= 2");
+      break;
+    case MULT_REALJACOBIAN: case MULT_JACOBIAN:
+      if(A < 4) throw std::runtime_error("a Jacobian multiplier needs A >= 4");
+      break;
+    case MULT_REALJACADJ:
+      if(A != 5 || B != 4)
+        throw std::runtime_error("the Jacobian adjoint needs A = 5, B = 4");
+      break;
+    case MULT_DOT: case MULT_REALDOT:
+      if(A % 2 || B != 1)
+        throw std::runtime_error("a dot-product multiplier needs an even A "
+                                 "and B = 1");
+      break;
+    default: throw std::runtime_error("unknown multiplier");
+  }
   I.dim=dim; I.A=A; I.B=B; I.mult=mult; I.prec=prec;
   I.longRow=false; I.rowM=I.rowQ=0;
   for(int d=0; d < dim; ++d) {
@@ -769,6 +789,65 @@ cudaError_t Conv::runHost(const void *const *in, void *const *out,
     if(e != cudaSuccess) return e;
   }
   return cudaStreamSynchronize(s);
+}
+
+// ---------------------------------------------------------------------------
+// Standalone padded transform (engine.h).
+
+PadTransform::PadTransform(int kind, long L, long M, long C, long mForce,
+                           int prec) : C(C), prec(prec)
+{
+  if(kind != KIND_PAD && kind != KIND_CENTERED && kind != KIND_REAL)
+    throw std::runtime_error("standalone padded transforms take fftPad, "
+                             "fftPadCentered or fftPadReal data");
+  if(prec != PREC_F64 && prec != PREC_F32)
+    throw std::runtime_error("unknown precision");
+  if(L < 1 || C < 1) throw std::runtime_error("L and C must be positive");
+  if(L > M)
+    throw std::runtime_error("L="+std::to_string(L)+" is greater than M="+
+                             std::to_string(M));
+  if(L*C > (long) INT_MAX || M*C > (long) INT_MAX)
+    throw std::runtime_error("transform too large");
+  a.kind=kind; a.L=L; a.M=M; a.stored=L; a.tile=a.tileB=1; a.rpc=1;
+  a.rows=0;
+  planOuter(a,mForce,prec,C,1,1,1);
+}
+
+size_t PadTransform::outElements() const {return (size_t) a.rows*C;}
+
+template<typename T>
+cudaError_t PadTransform::runT(const void *in, void *out, bool fwd,
+                               cudaStream_t s)
+{
+  typedef cplx<T> Cx;
+  OuterPlan<T> P;
+  P.L=(int) a.L; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
+  P.cshift=a.cshift; P.tile=fwd ? a.tile : a.tileB;
+  P.fp=fftPlan(a.kind == KIND_REAL ? a.N/2 : a.m,prec);
+  P.twN=(const typename TwT<T>::type *) twiddles(a.N,prec);
+  P.twX=NULL; P.NX=1;
+  P.count=1; P.nbatch=1; P.inBatch=P.outBatch=0;
+  P.inRow=C; P.outRow=C; P.C=(int) C; P.Ltot=(long long) a.L*C;
+  P.scale=(T) 1;
+  P.in[0]=(const Cx *) in;
+  P.out[0]=(Cx *) out;
+  const int threads=256;
+  if(a.kind == KIND_REAL)
+    return fwd ? launchOuterRealFwd<T>(P,threads,s) :
+      launchOuterRealBwd<T>(P,threads,s);
+  return fwd ? launchOuterFwd<T>(P,threads,s) : launchOuterBwd<T>(P,threads,s);
+}
+
+cudaError_t PadTransform::forward(const void *f, void *F, cudaStream_t s)
+{
+  return prec == PREC_F64 ? runT<double>(f,F,true,s) :
+    runT<float>(f,F,true,s);
+}
+
+cudaError_t PadTransform::backward(const void *F, void *f, cudaStream_t s)
+{
+  return prec == PREC_F64 ? runT<double>(F,f,false,s) :
+    runT<float>(F,f,false,s);
 }
 
 } // namespace fgb

@@ -97,6 +97,37 @@ private:
 // Twiddle table W_n^t = exp(2 pi i t/n), t < n, on the current device,
 // cached for the life of the process.  prec selects double2 or the float4
 // (hi, lo) split.
+// Standalone padded transform along one axis of C interleaved columns: the
+// forward and backward transforms of fftPad / fftPadCentered / fftPadReal
+// as a public device API (convolve.h:515-536, 623-646, 855-877; the
+// reference's tests/hybrid.cc drives them the same way).
+//   complex kinds: f is L x C complex (element (s, c) at s*C + c); F is
+//     N x C complex with row k = r*m + j holding residue r, entry j, the
+//     padded DFT (sign +1) at transformed index q*j + r:
+//       F[r*m+j][c] = sum_s f[s][c] exp(+2 pi i (s - cshift)(q j + r) / N);
+//     backward is the unnormalised adjoint, accumulated over residues:
+//       f[s][c] = sum_{r,j} F[r*m+j][c] exp(-2 pi i (s - cshift)(q j + r)/N).
+//   real kind: f is L x C real; F is (N/2+1) x C complex in natural order
+//     (row k: frequency k); backward is the matching complex-to-real sum.
+// backward(forward(f)) = N f.
+class PadTransform {
+public:
+  PadTransform(int kind, long L, long M, long C, long mForce, int prec);
+  cudaError_t forward(const void *f, void *F, cudaStream_t s);
+  cudaError_t backward(const void *F, void *f, cudaStream_t s);
+  const AxisPlan& plan() const {return a;}
+  long columns() const {return C;}
+  int precision() const {return prec;}
+  size_t inElements() const {return (size_t) a.L*C;}
+  size_t outElements() const;
+private:
+  AxisPlan a;
+  long C;
+  int prec;
+  template<typename T> cudaError_t runT(const void *in, void *out, bool fwd,
+                                        cudaStream_t s);
+};
+
 const void *twiddles(long n, int prec);
 
 std::string lastError();

@@ -53,6 +53,15 @@ __device__ __forceinline__ void applyMult(int kind, cplx<T> *X, int A)
       X[0]=s;
       break;
     }
+    case MULT_REALDOT: {
+      // The same on real data (two doubles per complex slot).
+      int K=A/2;
+      cplx<T> s=mk(X[0].x*X[K].x,X[0].y*X[K].y);
+      for(int k=1; k < K; ++k)
+        s=mk(fma(X[k].x,X[K+k].x,s.x),fma(X[k].y,X[K+k].y,s.y));
+      X[0]=s;
+      break;
+    }
     default:
       break;
   }

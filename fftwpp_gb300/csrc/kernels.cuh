@@ -31,7 +31,8 @@ namespace fgb {
 
 enum MultKind {
   MULT_NONE=0, MULT_BINARY=1, MULT_REALBINARY=2, MULT_CORRELATION=3,
-  MULT_REALJACOBIAN=4, MULT_JACOBIAN=5, MULT_REALJACADJ=6, MULT_DOT=7
+  MULT_REALJACOBIAN=4, MULT_JACOBIAN=5, MULT_REALJACADJ=6, MULT_DOT=7,
+  MULT_REALDOT=8
 };
 
 template<typename T>

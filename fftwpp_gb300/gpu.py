@@ -19,8 +19,8 @@ from typing import Sequence
 from . import _native
 from ._native import CENTERED, F32, F64, HERMITIAN, MULT, PAD, REAL
 
-__all__ = ["HybridConvolution", "BatchedConvolution", "PAD", "CENTERED",
-           "HERMITIAN", "REAL", "default_M"]
+__all__ = ["HybridConvolution", "BatchedConvolution", "PaddedTransform",
+           "PAD", "CENTERED", "HERMITIAN", "REAL", "default_M"]
 
 
 def default_M(kind: int, L: int, A: int = 2) -> int:
@@ -270,3 +270,94 @@ class BatchedConvolution:
             except Exception:
                 pass
             self.handle = None
+
+
+class PaddedTransform:
+    """Standalone forward/backward padded transform along one axis of C
+    interleaved columns (fftPad / fftPadCentered / fftPadReal,
+    convolve.h:515-536, 623-646, 855-877), for work in padded space.
+
+    Complex kinds: f has shape (L, C) (or (L,) for C = 1); forward returns
+    F of shape (N, C) whose row r*m + j is the padded DFT (sign +1) at
+    transformed index q*j + r (index(r, j)); backward is the unnormalised
+    adjoint, so backward(forward(f)) = N f.  Real kind: f real (L, C), F
+    complex (N/2 + 1, C) in natural frequency order.
+    """
+
+    def __init__(self, kind: int, L: int, M: int | None = None, *, C: int = 1,
+                 m: int = 0, precision: str = "f64"):
+        import torch
+        self.lib = _native.load()
+        self.kind, self.L, self.C = kind, int(L), int(C)
+        self.M = int(M) if M is not None else default_M(kind, L)
+        self.precision = precision
+        self.prec = F64 if precision == "f64" else F32
+        torch.cuda.current_device()
+        self.handle = self.lib.fgb_pad_create(kind, self.L, self.M, self.C,
+                                              int(m), self.prec)
+        if not self.handle:
+            raise ValueError(_native.last_error())
+        info = (ctypes.c_long * 10)()
+        self.lib.fgb_pad_info(self.handle, info)
+        (self.m, self.p, self.q, self.N, _, _, self.rows,
+         self.cshift) = list(info)[:8]
+
+    @property
+    def cdtype(self):
+        import torch
+        return torch.complex128 if self.prec == F64 else torch.complex64
+
+    @property
+    def idtype(self):
+        """Element type of the data side f."""
+        import torch
+        if self.kind == REAL:
+            return torch.float64 if self.prec == F64 else torch.float32
+        return self.cdtype
+
+    def index(self, r: int, j: int) -> int:
+        return self.lib.fgb_pad_index(self.handle, r, j)
+
+    def _check(self, t, rows, dtype, what):
+        if (not t.is_cuda or t.dtype != dtype or not t.is_contiguous() or
+                t.numel() != rows * self.C):
+            raise ValueError(f"{what} must be a contiguous CUDA tensor of "
+                             f"{rows} x {self.C} {dtype}")
+
+    def forward(self, f, out=None, stream=None):
+        import torch
+        self._check(f, self.L, self.idtype, "f")
+        if out is None:
+            out = torch.empty((self.rows, self.C), dtype=self.cdtype,
+                              device=f.device)
+        self._check(out, self.rows, self.cdtype, "out")
+        s = stream if stream is not None else torch.cuda.current_stream()
+        rc = self.lib.fgb_pad_forward_device(
+            self.handle, ctypes.c_void_p(f.data_ptr()),
+            ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(s.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(_native.last_error())
+        return out
+
+    def backward(self, F, out=None, stream=None):
+        import torch
+        self._check(F, self.rows, self.cdtype, "F")
+        if out is None:
+            out = torch.empty((self.L, self.C), dtype=self.idtype,
+                              device=F.device)
+        self._check(out, self.L, self.idtype, "out")
+        s = stream if stream is not None else torch.cuda.current_stream()
+        rc = self.lib.fgb_pad_backward_device(
+            self.handle, ctypes.c_void_p(F.data_ptr()),
+            ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(s.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(_native.last_error())
+        return out
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            try:
+                self.lib.fgb_pad_destroy(h)
+            except Exception:
+                pass

@@ -94,6 +94,93 @@ void fftwpp_hconv3d_delete(HybridConvolutionHermitian3 *conv); /* cfftw++.cc:155
 void fftwpp_hconv3d_convolve(HybridConvolutionHermitian3 *conv,
                              FFTWPP_C128 *a, FFTWPP_C128 *b);  /* cfftw++.cc:159 */
 
+/* Dot-product and work-array forms.  FFTW++'s header declares these but
+ * its wrapper never defines them (cfftw++.h:18, 30-47, 53-71, 77-99,
+ * 104-129, 136-153, 161-188); here they are defined with the meaning their
+ * signatures carry:
+ *   m (mx, my, mz): data lengths, as L of the plain forms;
+ *   M: number of products; the result is sum_{k<M} a_k * b_k (Hermitian
+ *      forms: lane-wise real products, like realMultBinary), normalised
+ *      like the plain forms and written over a[0] (dotf: the first block);
+ *   _dot(a, b): arrays of M host pointers; _dotf(a, b): M arrays back to
+ *      back in one host array each;
+ *   _work(..., u, v, w, ...): the caller's host scratch of the CPU code;
+ *      the GPU allocates its own device scratch, so these are ignored.
+ * A plain handle passed to a _dot call computes one product (M = 1). */
+double *create_doublealign(size_t n);                     /* cfftw++.h:18 */
+
+HybridConvolution *fftwpp_create_conv1d_dot(size_t m, size_t M);  /* cfftw++.h:30 */
+HybridConvolution *fftwpp_create_conv1d_work(size_t m, FFTWPP_C128 *u,
+                                             FFTWPP_C128 *v);     /* cfftw++.h:32 */
+HybridConvolution *fftwpp_create_conv1d_work_dot(size_t m, FFTWPP_C128 *u,
+                                                 FFTWPP_C128 *v,
+                                                 size_t M);       /* cfftw++.h:35 */
+void fftwpp_conv1d_convolve_dot(HybridConvolution *conv, FFTWPP_C128 **a,
+                                FFTWPP_C128 **b);                 /* cfftw++.h:42 */
+void fftwpp_conv1d_convolve_dotf(HybridConvolution *conv, FFTWPP_C128 *a,
+                                 FFTWPP_C128 *b);                 /* cfftw++.h:45 */
+
+HybridConvolutionHermitian *fftwpp_create_hconv1d_dot(size_t m,
+                                                      size_t M);  /* cfftw++.h:53 */
+HybridConvolutionHermitian *fftwpp_create_hconv1d_work(size_t m,
+    FFTWPP_C128 *u, FFTWPP_C128 *v, FFTWPP_C128 *w);              /* cfftw++.h:55 */
+HybridConvolutionHermitian *fftwpp_create_hconv1d_work_dot(size_t m,
+    FFTWPP_C128 *u, FFTWPP_C128 *v, FFTWPP_C128 *w, size_t M);    /* cfftw++.h:59 */
+void fftwpp_hconv1d_convolve_dot(HybridConvolutionHermitian *conv,
+                                 FFTWPP_C128 **a, FFTWPP_C128 **b); /* cfftw++.h:66 */
+void fftwpp_hconv1d_convolve_dotf(HybridConvolutionHermitian *conv,
+                                  FFTWPP_C128 *a, FFTWPP_C128 *b); /* cfftw++.h:69 */
+
+HybridConvolution2 *fftwpp_create_conv2d_dot(size_t mx, size_t my,
+                                             size_t M);           /* cfftw++.h:77 */
+HybridConvolution2 *fftwpp_create_conv2d_work(size_t mx, size_t my,
+    FFTWPP_C128 *u1, FFTWPP_C128 *v1, FFTWPP_C128 *u2,
+    FFTWPP_C128 *v2);                                             /* cfftw++.h:79 */
+HybridConvolution2 *fftwpp_create_conv2d_work_dot(size_t mx, size_t my,
+    FFTWPP_C128 *u1, FFTWPP_C128 *v1, FFTWPP_C128 *u2,
+    FFTWPP_C128 *v2, size_t M);                                   /* cfftw++.h:85 */
+void fftwpp_conv2d_convolve_dot(HybridConvolution2 *conv, FFTWPP_C128 **a,
+                                FFTWPP_C128 **b);                 /* cfftw++.h:95 */
+void fftwpp_conv2d_convolve_dotf(HybridConvolution2 *conv, FFTWPP_C128 *a,
+                                 FFTWPP_C128 *b);                 /* cfftw++.h:97 */
+
+HybridConvolutionHermitian2 *fftwpp_create_hconv2d_dot(size_t mx, size_t my,
+                                                       size_t M); /* cfftw++.h:104 */
+HybridConvolutionHermitian2 *fftwpp_create_hconv2d_work(size_t mx, size_t my,
+    FFTWPP_C128 *u1, FFTWPP_C128 *v1, FFTWPP_C128 *w1, FFTWPP_C128 *u2,
+    FFTWPP_C128 *v2);                                             /* cfftw++.h:107 */
+HybridConvolutionHermitian2 *fftwpp_create_hconv2d_work_dot(size_t mx,
+    size_t my, FFTWPP_C128 *u1, FFTWPP_C128 *v1, FFTWPP_C128 *w1,
+    FFTWPP_C128 *u2, FFTWPP_C128 *v2, size_t M);                  /* cfftw++.h:114 */
+void fftwpp_hconv2d_convolve_dot(HybridConvolutionHermitian2 *conv,
+                                 FFTWPP_C128 **a, FFTWPP_C128 **b); /* cfftw++.h:124 */
+void fftwpp_hconv2d_convolve_dotf(HybridConvolutionHermitian2 *conv,
+                                  FFTWPP_C128 *a, FFTWPP_C128 *b); /* cfftw++.h:127 */
+
+HybridConvolution3 *fftwpp_create_conv3d_work(size_t mx, size_t my,
+    size_t mz, FFTWPP_C128 *u1, FFTWPP_C128 *v1, FFTWPP_C128 *u2,
+    FFTWPP_C128 *v2, FFTWPP_C128 *u3, FFTWPP_C128 *v3);           /* cfftw++.h:136 */
+HybridConvolution3 *fftwpp_create_conv3d_dot(size_t mx, size_t my,
+                                             size_t mz, size_t M); /* cfftw++.h:145 */
+void fftwpp_conv3d_convolve_dot(HybridConvolution3 *conv, FFTWPP_C128 **a,
+                                FFTWPP_C128 **b);                 /* cfftw++.h:151 */
+void fftwpp_conv3d_convolve_dotf(HybridConvolution3 *conv, FFTWPP_C128 *a,
+                                 FFTWPP_C128 *b);                 /* cfftw++.h:153 */
+
+HybridConvolutionHermitian3 *fftwpp_create_hconv3d_dot(size_t mx, size_t my,
+                                                       size_t mz,
+                                                       size_t M); /* cfftw++.h:161 */
+HybridConvolutionHermitian3 *fftwpp_create_hconv3d_work(size_t mx, size_t my,
+    size_t mz, FFTWPP_C128 *u1, FFTWPP_C128 *v1, FFTWPP_C128 *w1,
+    FFTWPP_C128 *u2, FFTWPP_C128 *v2, FFTWPP_C128 *u3,
+    FFTWPP_C128 *v3);                                             /* cfftw++.h:165 */
+HybridConvolutionHermitian3 *fftwpp_create_hconv3d_work_dot(size_t mx,
+    size_t my, size_t mz, FFTWPP_C128 *u1, FFTWPP_C128 *v1,
+    FFTWPP_C128 *w1, FFTWPP_C128 *u2, FFTWPP_C128 *v2, FFTWPP_C128 *u3,
+    FFTWPP_C128 *v3, size_t M);                                   /* cfftw++.h:175 */
+void fftwpp_hconv3d_convolve_dot(HybridConvolutionHermitian3 *conv,
+                                 FFTWPP_C128 **a, FFTWPP_C128 **b); /* cfftw++.h:188 */
+
 #ifdef __cplusplus
 }
 #endif

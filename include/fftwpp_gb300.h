@@ -38,6 +38,7 @@ extern "C" {
 #define FGB_MULT_JACOBIAN 5        /* same on complex data */
 #define FGB_MULT_REALJACADJ 6      /* adjoint of FGB_MULT_REALJACOBIAN */
 #define FGB_MULT_DOT 7             /* F0 = sum_k F_k F_{A/2+k} */
+#define FGB_MULT_REALDOT 8         /* the same, lane-wise on doubles */
 
 #define FGB_F64 0
 #define FGB_F32 1                  /* FP32 data, split hi+lo twiddles */
@@ -114,6 +115,33 @@ long fgb_batch_choice(const fgb_batch *b, int i);
 /* Nonzero if a bounded in-kernel wait gave up since the last call. */
 int fgb_batch_error(fgb_batch *b);
 void fgb_batch_destroy(fgb_batch *b);
+
+/* Standalone padded transforms: the forward and backward transforms of
+ * fftPad / fftPadCentered / fftPadReal (convolve.h:515-536, 623-646,
+ * 855-877; driven stand-alone by the reference's tests/hybrid.cc and
+ * tests/hybridr.cc), for callers that work in padded space themselves.
+ * kind: FGB_PAD, FGB_CENTERED or FGB_REAL; L data length, M
+ * minimum padded length, C interleaved columns (element (s, c) at s*C + c),
+ * m forced residue block length (0: planner's choice).
+ * Complex kinds: F is N x C complex, row r*m + j holding residue r, entry j,
+ *   the padded DFT (sign +1) at transformed index fgb_pad_index(r, j) =
+ *   q*j + r, measured from the centred origin floor(L/2) for
+ *   FGB_CENTERED.  Real kind: f is L x C real, F is (N/2+1) x C
+ *   complex in natural frequency order (fgb_pad_index(0, k) = k).
+ * backward is the unnormalised adjoint (sign -1) accumulated over residues,
+ * so backward(forward(f)) = N f.  Device pointers, asynchronous on stream.
+ * The Hermitian kind (fftPadHermitian) is fused into the convolution's row
+ * kernel and has no standalone form. */
+typedef struct fgb_pad fgb_pad;
+fgb_pad *fgb_pad_create(int kind, size_t L, size_t M, size_t C, size_t m,
+                        int precision);
+int fgb_pad_forward_device(fgb_pad *t, const void *f, void *F, void *stream);
+int fgb_pad_backward_device(fgb_pad *t, const void *F, void *f, void *stream);
+/* info[0] m, [1] p, [2] q, [3] N, [4] L, [5] C, [6] rows of F, [7] centred
+ * origin offset, [8] forward columns per CTA, [9] backward columns per CTA. */
+int fgb_pad_info(const fgb_pad *t, long *info);
+size_t fgb_pad_index(const fgb_pad *t, size_t r, size_t j);
+void fgb_pad_destroy(fgb_pad *t);
 
 /* Text of the last error on this thread. */
 const char *fgb_last_error(void);

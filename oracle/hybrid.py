@@ -352,7 +352,24 @@ def mult_realjacadj(F):
             (-g * R[1]).astype(np.complex128), (g * R[0]).astype(np.complex128)]
 
 
+def mult_dot(F):
+    """Sum of A/2 binary products F_k F_{A/2+k}: the convolution of a dot
+    product, declared (not defined) by the old C interface's *_dot entry
+    points (wrappers/cfftw++.h:30-47)."""
+    K = len(F) // 2
+    return [sum(F[k] * F[K + k] for k in range(K))]
+
+
+def mult_realdot(F):
+    """mult_dot on real data (realMultBinary per pair, convolve.cc:60-83)."""
+    K = len(F) // 2
+    return [sum(F[k].real * F[K + k].real for k in range(K))
+            .astype(np.complex128)]
+
+
 MULTIPLIERS: dict[str, Callable] = {
+    "dot": mult_dot,
+    "realdot": mult_realdot,
     "realjacadj": mult_realjacadj,
     "binary": mult_binary,
     "realbinary": mult_realbinary,

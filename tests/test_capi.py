@@ -114,3 +114,34 @@ def test_missing_library_is_loud(tmp_path, monkeypatch):
     monkeypatch.setattr(_native, "_lib", None)
     with pytest.raises(_native.NativeLibraryMissing):
         _native.load()
+
+
+def test_padded_transform_plans(native_lib):
+    """Standalone padded-transform plans (host-side planning only)."""
+    from fftwpp_gb300 import _native
+    lib = native_lib
+    info = (ctypes.c_long * 10)()
+    for kind, L, M, C, m in [(0, 1000, 1999, 4, 0), (1, 63, 94, 3, 0),
+                             (0, 64, 127, 1, 16), (1, 31, 46, 2, 8),
+                             (3, 100, 199, 5, 0)]:
+        h = lib.fgb_pad_create(kind, L, M, C, m, 0)
+        assert h, _native.last_error()
+        try:
+            assert lib.fgb_pad_info(h, info) == 0
+            mm, p, q, N, LL, CC, rows, c = list(info)[:8]
+            assert (LL, CC) == (L, C) and N >= M
+            if kind == 3:
+                assert rows == N // 2 + 1 and q == 1
+                assert lib.fgb_pad_index(h, 0, 7) == 7
+            else:
+                assert mm * q == N and rows == N and p == -(-L // mm)
+                if m:
+                    assert mm == m
+                assert c == (L // 2 if kind == 1 else 0)
+                assert lib.fgb_pad_index(h, 1, 5) == q * 5 + 1
+        finally:
+            lib.fgb_pad_destroy(h)
+    assert not lib.fgb_pad_create(2, 16, 24, 1, 0, 0)
+    assert "fftPadReal" in _native.last_error()
+    assert not lib.fgb_pad_create(0, 16, 8, 1, 0, 0)
+    assert "greater than M" in _native.last_error()

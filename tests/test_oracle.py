@@ -179,3 +179,29 @@ def test_layout_values_are_padded_dft():
         k = lay["idx"]
         full = np.exp(2j * np.pi * (np.outer(k, s - c) % N) / N) @ f
         assert Dr.rel_l2(lay["F"], full) < 1e-12, lay["key"]
+
+
+@pytest.mark.parametrize("kinds,L,mult,single", [
+    ([H.PAD], [23], "dot", "binary"),
+    ([H.CENTERED, H.HERMITIAN], [15, 15], "realdot", "realbinary"),
+    ([H.PAD, H.PAD], [6, 7], "dot", "binary"),
+])
+def test_dot_multiplier_is_sum_of_products(kinds, L, mult, single):
+    """The dot-product multiplier equals the sum of the pairs' binary
+    convolutions (linearity); checks the restated *_dot semantics."""
+    rng = np.random.default_rng(4)
+    shape = list(L)
+    if kinds[-1] == H.HERMITIAN:
+        shape[-1] = (L[-1] + 1) // 2
+    K = 3
+    fs = []
+    for _ in range(2 * K):
+        f = rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+        if kinds[-1] == H.HERMITIAN:
+            H.hermitian_symmetrize_x(f, (L[0] + 1) // 2, shape[1], L[0] // 2)
+        fs.append(f)
+    M = [H.default_M(k, l) for k, l in zip(kinds, L)]
+    got = H.convolve(fs, kinds, L, M, mult=mult)[0]
+    want = sum(H.convolve([fs[k], fs[K + k]], kinds, L, M, mult=single)[0]
+               for k in range(K))
+    assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
