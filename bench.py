@@ -465,7 +465,7 @@ def run_ours(args, w):
     kms = conv.kernel_ms()
     per_launch = [k / args.steps for k in kms]
     dom = int(np.argmax(per_launch))
-    elem = (8 if conv.real else 16) if prec == "f64" else (4 if conv.real else 8)
+    elem = (8 if conv.real else 16) if prec != "f32" else (4 if conv.real else 8)
     abytes = algorithmic_bytes(w, elem)
 
     if rank != 0:
@@ -534,25 +534,25 @@ def run_ours(args, w):
 
     extra = {}
     if not args.quick and prec == "f64":
-        # FP32 compensated mode on the same workload.
-        c32 = HybridConvolution(w["kinds"], w["L"], w["M"], A=w["A"], B=w["B"],
-                                mult=w["mult"], precision="f32",
-                                batch=w.get("batch", 1))
-        t32 = [torch.from_numpy(f).to(c32.dtype).cuda() for f in fs]
-        ms32, o32 = time_device(c32, t32, args.steps, args.warmup, flush,
-                                timing=False)
-        if want is not None:
-            e32 = rel_l2(o32[0].cpu().numpy(), want)
-        elif big:
-            e32 = spot_check(fs, o32[0].cpu().numpy().astype(got0.dtype), w,
-                             n=12)
-        else:
-            e32 = None
-        extra["fp32_compensated"] = {"value": nb * args.steps / (ms32 * 1e-3),
-                                     "unit": "convs/s",
-                                     "rel_l2_vs_fp64_oracle": e32,
-                                     "speedup_vs_fp64": (args.steps / ms32) /
-                                     (args.steps / total_ms)}
+        # The FP32-compensated and float-float modes on the same workload.
+        for other, key in (("f32", "fp32_compensated"), ("ff", "float_float")):
+            co = HybridConvolution(w["kinds"], w["L"], w["M"], A=w["A"],
+                                   B=w["B"], mult=w["mult"], precision=other,
+                                   batch=w.get("batch", 1))
+            to = [torch.from_numpy(f).to(co.dtype).cuda() for f in fs]
+            mso, oo = time_device(co, to, args.steps, args.warmup, flush,
+                                  timing=False)
+            if want is not None:
+                eo = rel_l2(oo[0].cpu().numpy(), want)
+            elif big:
+                eo = spot_check(fs, oo[0].cpu().numpy().astype(got0.dtype), w,
+                                n=12)
+            else:
+                eo = None
+            extra[key] = {"value": nb * args.steps / (mso * 1e-3),
+                          "unit": "convs/s", "rel_l2_vs_fp64_oracle": eo,
+                          "speedup_vs_fp64": total_ms / mso}
+            del co, to, oo
 
     # End to end through the reference-facing C ABI on host buffers.
     e2e = None
@@ -586,9 +586,9 @@ def run_ours(args, w):
         lib.delete_complexAlign(pb)
     else:
         # Host-pointer entry of the device-API plan.
-        host = [f.astype(np.complex128 if not conv.real else np.float64)
-                if prec == "f64" else f.astype(np.complex64 if not conv.real
-                                               else np.float32) for f in fs]
+        host = [f.astype(np.complex64 if not conv.real else np.float32)
+                if prec == "f32" else f.astype(np.complex128 if not conv.real
+                                               else np.float64) for f in fs]
         tot = 0.0
         for _ in range(args.steps):
             hs = [x.copy() for x in host]
@@ -919,7 +919,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hconv2d",
                     choices=sorted(WORKLOADS) + ["batched1d"])
-    ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "ff"])
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--quick", action="store_true",
                     help="skip the FP32 comparison leg")

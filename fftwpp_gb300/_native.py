@@ -13,7 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib_fftwpp.so")
 
 PAD, CENTERED, HERMITIAN, REAL = 0, 1, 2, 3
-F64, F32 = 0, 1
+F64, F32, FF = 0, 1, 2
+PRECISIONS = {"f64": F64, "f32": F32, "ff": FF}
 MULT = {"none": 0, "binary": 1, "realbinary": 2, "correlation": 3,
         "realjacobian": 4, "jacobian": 5, "realjacadj": 6, "dot": 7,
         "realdot": 8}

@@ -19,6 +19,7 @@ LIB = os.path.join(HERE, "lib_fftwpp.so")
 # the two halves of its template instantiations build in parallel.
 UNITS = [("kernels.cu", "kernels_f64.o", ["-DFGB_ONLY_DOUBLE"]),
          ("kernels.cu", "kernels_f32.o", ["-DFGB_ONLY_FLOAT"]),
+         ("kernels.cu", "kernels_ff.o", ["-DFGB_ONLY_FF"]),
          ("engine.cu", "engine.o", []),
          ("batch.cu", "batch.o", []),
          ("capi.cu", "capi.o", []),

@@ -91,6 +91,8 @@ BatchConv::BatchConv(int nprob, const long *L, const long *M,
     throw std::runtime_error("need 1 <= B <= A <= 8");
   if(kind != KIND_PAD && kind != KIND_CENTERED)
     throw std::runtime_error("batched problems are fftPad or fftPadCentered");
+  if(prec != PREC_F64 && prec != PREC_F32)
+    throw std::runtime_error("batched problems run in FP64 or FP32");
   budget=72*1024;
   Ls.assign(L,L+nprob);
   Ms.assign(M,M+nprob);

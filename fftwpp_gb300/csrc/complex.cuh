@@ -1,11 +1,13 @@
 // complex.cuh -- complex arithmetic and twiddle types for the GB300 engine.
 //
-// Two arithmetic types are supported:
+// Three arithmetic types are supported:
 //   double : FP64 drop-in mode, twiddles stored as double2;
 //   float  : FP32 compensated mode, every twiddle stored as an unevaluated
 //            sum hi+lo of two floats derived from the FP64 value, so a
 //            twiddle multiply a*(hi+lo) keeps ~2^-48 relative twiddle
-//            accuracy while the butterfly data stays FP32.
+//            accuracy while the butterfly data stays FP32;
+//   ff     : float-float mode, data and arithmetic both hi+lo pairs (FP64
+//            data at the interface, FP64-grade accuracy on the FP32 pipe).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -13,11 +15,96 @@
 
 namespace fgb {
 
+// The CUDA fma overloads (double, float) stay visible next to the
+// float-float one below.
+using ::fma;
+
+// ---------------------------------------------------------------------------
+// Float-float arithmetic: a real number held as the unevaluated sum hi + lo
+// of two floats with |lo| <= ulp(hi)/2, about 48 significant bits.  GB300
+// issues FP32 instructions at 64 times its FP64 rate, so transforms in this
+// type keep FP64-grade normwise accuracy at a fraction of the FP64 cost.
+// The operations are the error-free transformations of Knuth (TwoSum),
+// Dekker (FastTwoSum) and the FMA-based TwoProduct; the addition is the
+// "sloppy" double-word sum, whose error is bounded by 2^-46 (|a| + |b|),
+// which is the normwise bound an FFT needs.  The _rn intrinsics keep the
+// compiler from fusing the error terms into multiply-adds.
+struct ff {
+  float hi, lo;
+  ff() = default;
+  __host__ __device__ constexpr ff(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr explicit ff(double d)
+    : hi((float) d), lo((float) (d-(double) (float) d)) {}
+};
+
+__device__ __forceinline__ ff ffTwoSum(float a, float b)
+{
+  float s=__fadd_rn(a,b);
+  float bb=__fsub_rn(s,a);
+  float e=__fadd_rn(__fsub_rn(a,__fsub_rn(s,bb)),__fsub_rn(b,bb));
+  return ff(s,e);
+}
+
+// Renormalise s + e for |s| >= |e|.
+__device__ __forceinline__ ff ffFast(float s, float e)
+{
+  float t=__fadd_rn(s,e);
+  return ff(t,__fsub_rn(e,__fsub_rn(t,s)));
+}
+
+__device__ __forceinline__ ff operator+(ff a, ff b)
+{
+  ff s=ffTwoSum(a.hi,b.hi);
+  return ffFast(s.hi,__fadd_rn(s.lo,__fadd_rn(a.lo,b.lo)));
+}
+__device__ __forceinline__ ff operator-(ff a) {return ff(-a.hi,-a.lo);}
+__device__ __forceinline__ ff operator-(ff a, ff b) {return a+(-b);}
+
+__device__ __forceinline__ ff operator*(ff a, ff b)
+{
+  float p=__fmul_rn(a.hi,b.hi);
+  float e=fmaf(a.hi,b.hi,-p);
+  e=fmaf(a.hi,b.lo,e);
+  e=fmaf(a.lo,b.hi,e);
+  return ffFast(p,e);
+}
+
+// a*b + c.
+__device__ __forceinline__ ff fma(ff a, ff b, ff c)
+{
+  float p=__fmul_rn(a.hi,b.hi);
+  float e=fmaf(a.hi,b.hi,-p);
+  ff s=ffTwoSum(p,c.hi);
+  float l=__fadd_rn(__fadd_rn(s.lo,e),c.lo);
+  l=fmaf(a.hi,b.lo,l);
+  l=fmaf(a.lo,b.hi,l);
+  return ffFast(s.hi,l);
+}
+
+// a*b + c*d with one renormalisation (complex multiplies).
+__device__ __forceinline__ ff ffDot2(ff a, ff b, ff c, ff d)
+{
+  float p1=__fmul_rn(a.hi,b.hi);
+  float e1=fmaf(a.hi,b.hi,-p1);
+  float p2=__fmul_rn(c.hi,d.hi);
+  float e2=fmaf(c.hi,d.hi,-p2);
+  ff s=ffTwoSum(p1,p2);
+  float l=__fadd_rn(s.lo,__fadd_rn(e1,e2));
+  l=fmaf(a.hi,b.lo,l);
+  l=fmaf(a.lo,b.hi,l);
+  l=fmaf(c.hi,d.lo,l);
+  l=fmaf(c.lo,d.hi,l);
+  return ffFast(s.hi,l);
+}
+
 template<typename T> struct cplx { T x, y; };
+// Float-float complex values move as one 16-byte vector.
+template<> struct __align__(16) cplx<ff> { ff x, y; };
 
 template<typename T> struct TwT;
 template<> struct TwT<double> { typedef double2 type; };
 template<> struct TwT<float>  { typedef float4 type; };   // (hi.x, hi.y, lo.x, lo.y)
+template<> struct TwT<ff>     { typedef float4 type; };   // the same split
 
 template<typename T>
 __host__ __device__ __forceinline__ cplx<T> mk(T a, T b) { cplx<T> r; r.x=a; r.y=b; return r; }
@@ -39,6 +126,16 @@ template<typename T>
 __device__ __forceinline__ cplx<T> cmulconj(cplx<T> a, cplx<T> b)   // a*conj(b)
 {
   return mk(fma(a.x,b.x,a.y*b.y),fma(a.y,b.x,-a.x*b.y));
+}
+
+__device__ __forceinline__ cplx<ff> cmul(cplx<ff> a, cplx<ff> b)
+{
+  return mk(ffDot2(a.x,b.x,-a.y,b.y),ffDot2(a.x,b.y,a.y,b.x));
+}
+
+__device__ __forceinline__ cplx<ff> cmulconj(cplx<ff> a, cplx<ff> b)
+{
+  return mk(ffDot2(a.x,b.x,a.y,b.y),ffDot2(a.y,b.x,-a.x,b.y));
 }
 
 template<typename T>
@@ -72,17 +169,12 @@ __device__ __forceinline__ cplx<float> twmul(cplx<float> a, float4 w)
   return mk(rx,ry);
 }
 
-// Runtime-sign variants.
-__device__ __forceinline__ cplx<double> twmulr(cplx<double> a, double2 w, int s)
+template<int S>
+__device__ __forceinline__ cplx<ff> twmul(cplx<ff> a, float4 w)
 {
-  return s > 0 ? twmul<1>(a,w) : twmul<-1>(a,w);
+  ff wx(w.x,w.z);
+  ff wy=S > 0 ? ff(w.y,w.w) : ff(-w.y,-w.w);
+  return mk(ffDot2(a.x,wx,-a.y,wy),ffDot2(a.x,wy,a.y,wx));
 }
-__device__ __forceinline__ cplx<float> twmulr(cplx<float> a, float4 w, int s)
-{
-  return s > 0 ? twmul<1>(a,w) : twmul<-1>(a,w);
-}
-
-__device__ __forceinline__ cplx<double> twval(double2 w) { return mk(w.x,w.y); }
-__device__ __forceinline__ cplx<float> twval(float4 w) { return mk(w.x,w.y); }
 
 } // namespace fgb

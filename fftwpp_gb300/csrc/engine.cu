@@ -87,6 +87,7 @@ void setLastError(const std::string& s) {errorText=s;}
 
 const void *twiddles(long n, int prec)
 {
+  if(prec == PREC_FF) prec=PREC_F32;        // the same hi+lo float4 table
   static std::mutex mu;
   static std::map<std::tuple<int,long,int>,void *> cache;
   int dev=0;
@@ -171,25 +172,27 @@ FFTPlanDev fftPlanPublic(long n, int prec) {return fftPlan(n,prec);}
 
 static const size_t SMEM_MAX=227*1024;
 
-static size_t elem(int prec) {return prec == PREC_F64 ? 16 : 8;}
+// 16-byte complex elements (FP64 and float-float) or 8-byte ones (FP32).
+static bool wide(int prec) {return prec != PREC_F32;}
+static size_t elem(int prec) {return wide(prec) ? 16 : 8;}
 
 static size_t rowNeed(int prec, long L, long m, int A, int B, int rpc=1)
 {
-  return prec == PREC_F64 ? rowSmem<double>(L,m,A,B,rpc) :
+  return wide(prec) ? rowSmem<double>(L,m,A,B,rpc) :
     rowSmem<float>(L,m,A,B,rpc);
 }
 
 static size_t hermNeed(int prec, long H, long Nh, int A, int rpc=1)
 {
-  return prec == PREC_F64 ? hermRowSmem<double>(H,Nh,A,rpc) :
+  return wide(prec) ? hermRowSmem<double>(H,Nh,A,rpc) :
     hermRowSmem<float>(H,Nh,A,rpc);
 }
 
 static size_t outerNeed(int prec, long L, long m, int tile)
 {
-  size_t f=prec == PREC_F64 ? outerFwdSmem<double>(L,m,tile) :
+  size_t f=wide(prec) ? outerFwdSmem<double>(L,m,tile) :
     outerFwdSmem<float>(L,m,tile);
-  size_t b=prec == PREC_F64 ? outerBwdSmem<double>(L,m,tile) :
+  size_t b=wide(prec) ? outerBwdSmem<double>(L,m,tile) :
     outerBwdSmem<float>(L,m,tile);
   return std::max(f,b);
 }
@@ -309,15 +312,15 @@ static int pickTile(int maxTile, long C, long factor, F smem, int minTile=1)
 static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
                       int A, int B)
 {
-  int maxTile=prec == PREC_F64 ? 8 : 16;
-  int minTile=prec == PREC_F64 ? 2 : 4;
+  int maxTile=wide(prec) ? 8 : 16;
+  int minTile=wide(prec) ? 2 : 4;
   if(a.kind == KIND_REAL) {
     a.N=evenSmooth(mForce > 0 ? std::max(a.M,mForce) : a.M);
     a.m=a.N; a.q=1; a.p=1; a.cshift=0;
     a.rows=a.N/2+1;
     long Nh=a.N/2;
     auto sm=[&](int t) {
-      return prec == PREC_F64 ? outerRealSmem<double>(a.L,Nh,t) :
+      return wide(prec) ? outerRealSmem<double>(a.L,Nh,t) :
         outerRealSmem<float>(a.L,Nh,t);
     };
     a.tile=pickTile(maxTile,C,nbatch*A,sm,minTile);
@@ -355,11 +358,11 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
   a.cshift=centered ? (int) (a.L/2) : 0;
   a.rows=a.N;
   auto smf=[&](int t) {
-    return prec == PREC_F64 ? outerFwdSmem<double>(a.L,a.m,t) :
+    return wide(prec) ? outerFwdSmem<double>(a.L,a.m,t) :
       outerFwdSmem<float>(a.L,a.m,t);
   };
   auto smb=[&](int t) {
-    return prec == PREC_F64 ? outerBwdSmem<double>(a.L,a.m,t) :
+    return wide(prec) ? outerBwdSmem<double>(a.L,a.m,t) :
       outerBwdSmem<float>(a.L,a.m,t);
   };
   a.tile=pickTile(maxTile,C,nbatch*a.q*A,smf,minTile);
@@ -376,7 +379,7 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
   if(dim < 1 || dim > 3) throw std::runtime_error("dimension must be 1, 2 or 3");
   if(A < 1 || A > FGB_MAXA || B < 1 || B > A)
     throw std::runtime_error("need 1 <= B <= A <= 8");
-  if(prec != PREC_F64 && prec != PREC_F32)
+  if(prec != PREC_F64 && prec != PREC_F32 && prec != PREC_FF)
     throw std::runtime_error("unknown precision");
   if(batch < 1) throw std::runtime_error("batch must be positive");
   switch(mult) {
@@ -452,8 +455,8 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
     in.N=N; in.m=best; in.q=N/best; in.p=ceilquotient(in.L,best);
     in.cshift=0;
     auto sm=[&](int t) {return outerNeed(prec,in.p,I.rowQ,t);};
-    in.tile=pickTile(prec == PREC_F64 ? 8 : 16,I.rowM,A,sm);
-    in.tileB=pickTile(prec == PREC_F64 ? 8 : 16,I.rowM,B,sm);
+    in.tile=pickTile(wide(prec) ? 8 : 16,I.rowM,A,sm);
+    in.tileB=pickTile(wide(prec) ? 8 : 16,I.rowM,B,sm);
     if(mForce && mForce[0] > 0)
       throw std::runtime_error("forced m not supported on the long path");
   }
@@ -477,11 +480,12 @@ Conv::~Conv()
 {
   for(cudaEvent_t ev : events) cudaEventDestroy(ev);
   for(void *p : bufs) cudaFree(p);
+  for(void *p : ffBufs) cudaFree(p);
   if(hostIn) cudaFree(hostIn);
   if(hostOut) cudaFree(hostOut);
 }
 
-size_t Conv::elemBytes() const
+size_t Conv::elemBytes() const   // user-facing element (FP64 in ff mode)
 {
   if(I.axis[0].kind == KIND_REAL) return elem(I.prec)/2;
   return elem(I.prec);
@@ -520,6 +524,20 @@ void Conv::allocate()
     for(int a=0; a < A; ++a) get(e*rx*Ly*nz);
     for(int a=0; a < A; ++a) get(e*rx*ry*nz);
     nlaunch=5;
+  }
+  if(I.prec == PREC_FF) {
+    // The A converted inputs and B outputs in float-float form (the same
+    // size as the FP64 arrays), and a conversion launch on either side.
+    size_t bytes=elements()*elemBytes();
+    for(int a=0; a < A+I.B; ++a) {
+      void *p=NULL;
+      if(cudaMalloc(&p,bytes) != cudaSuccess)
+        throw std::runtime_error("device allocation of "+
+                                 std::to_string(bytes)+" bytes failed");
+      ffBufs.push_back(p);
+      staging += bytes;
+    }
+    nlaunch += 2;
   }
 }
 
@@ -567,9 +585,6 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   double scale=1.0;
   if(normalize)
     for(int d=0; d < I.dim; ++d) scale /= (double) I.axis[d].N;
-  marks=0;
-  tick(s);
-
   auto rowPlan=[&](RowPlan<T>& P, const AxisPlan& a) {
     P.L=(int) a.stored; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
     P.cshift=a.cshift; P.A=A; P.B=B; P.mult=I.mult;
@@ -763,8 +778,30 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
 
 cudaError_t Conv::run(const void *const *in, void *const *out, cudaStream_t s)
 {
+  marks=0;
+  tick(s);
   if(I.prec == PREC_F64) return runT<double>(in,out,s);
-  return runT<float>(in,out,s);
+  if(I.prec == PREC_F32) return runT<float>(in,out,s);
+  // Float-float: convert the FP64 inputs, convolve, convert the outputs.
+  const int A=I.A, B=I.B;
+  const size_t reals=elements()*elemBytes()/sizeof(double);
+  ConvertArgs C;
+  C.count=A; C.n=reals;
+  for(int a=0; a < A; ++a) {C.src[a]=in[a]; C.dst[a]=ffBufs[a];}
+  cudaError_t e=launchConvert(C,true,s);
+  tick(s);
+  if(e != cudaSuccess) return e;
+  std::vector<const void *> fin(A);
+  std::vector<void *> fout(B);
+  for(int a=0; a < A; ++a) fin[a]=ffBufs[a];
+  for(int b=0; b < B; ++b) fout[b]=ffBufs[A+b];
+  e=runT<ff>(fin.data(),fout.data(),s);
+  if(e != cudaSuccess) return e;
+  C.count=B;
+  for(int b=0; b < B; ++b) {C.src[b]=ffBufs[A+b]; C.dst[b]=out[b];}
+  e=launchConvert(C,false,s);
+  tick(s);
+  return e;
 }
 
 cudaError_t Conv::runHost(const void *const *in, void *const *out,
@@ -801,7 +838,8 @@ PadTransform::PadTransform(int kind, long L, long M, long C, long mForce,
     throw std::runtime_error("standalone padded transforms take fftPad, "
                              "fftPadCentered or fftPadReal data");
   if(prec != PREC_F64 && prec != PREC_F32)
-    throw std::runtime_error("unknown precision");
+    throw std::runtime_error("standalone padded transforms run in FP64 or "
+                             "FP32");
   if(L < 1 || C < 1) throw std::runtime_error("L and C must be positive");
   if(L > M)
     throw std::runtime_error("L="+std::to_string(L)+" is greater than M="+

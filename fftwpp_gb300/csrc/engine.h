@@ -15,7 +15,8 @@
 namespace fgb {
 
 enum AxisKind {KIND_PAD=0, KIND_CENTERED=1, KIND_HERMITIAN=2, KIND_REAL=3};
-enum Precision {PREC_F64=0, PREC_F32=1};
+// PREC_FF: FP64 data at the interface, float-float arithmetic inside.
+enum Precision {PREC_F64=0, PREC_F32=1, PREC_FF=2};
 
 // Integer rules shared with the reference (convolve.cc:114-175, 403-410).
 size_t ceilquotient(size_t a, size_t b);
@@ -81,6 +82,8 @@ private:
   ConvInfo I;
   long batch;
   std::vector<void *> bufs;        // device staging buffers
+  std::vector<void *> ffBufs;      // float-float mode: converted A inputs,
+                                   // then B outputs
   size_t staging;
   void *hostIn, *hostOut;          // device copies for runHost
   int nlaunch;

@@ -91,9 +91,14 @@ template<int S, typename T> struct Codelet<8,S,T> {
     Codelet<4,S,T>::run(o);
     // o[k] *= W_8^{S k}
     cplx<T> o1=o[1], o3=o[3];
-    o[1]=mk((o1.x-(T) S*o1.y)*h,(o1.y+(T) S*o1.x)*h);          // (1+Si)/sqrt2
+    if(S > 0) {
+      o[1]=mk((o1.x-o1.y)*h,(o1.y+o1.x)*h);                     // (1+i)/sqrt2
+      o[3]=mk((-o3.x-o3.y)*h,(o3.x-o3.y)*h);                    // (-1+i)/sqrt2
+    } else {
+      o[1]=mk((o1.x+o1.y)*h,(o1.y-o1.x)*h);                     // (1-i)/sqrt2
+      o[3]=mk((o3.y-o3.x)*h,(-o3.y-o3.x)*h);                    // (-1-i)/sqrt2
+    }
     o[2]=mulI<S>(o[2]);
-    o[3]=mk((-o3.x-(T) S*o3.y)*h,(-o3.y+(T) S*o3.x)*h);        // (-1+Si)/sqrt2
 #pragma unroll
     for(int k=0; k < 4; ++k) {
       a[k]=e[k]+o[k];
@@ -105,7 +110,7 @@ template<int S, typename T> struct Codelet<8,S,T> {
 template<int S, typename T> struct Codelet<3,S,T> {
   static __device__ __forceinline__ void run(cplx<T> *a) {
     const T c=(T) -0.5;
-    const T s=(T) S*(T) FGB_SQRT3_2;
+    const T s=(T) (S*FGB_SQRT3_2);
     cplx<T> t=a[1]+a[2];
     cplx<T> d=a[1]-a[2];
     cplx<T> b=mk(fma(c,t.x,a[0].x),fma(c,t.y,a[0].y));
@@ -119,7 +124,7 @@ template<int S, typename T> struct Codelet<3,S,T> {
 template<int S, typename T> struct Codelet<5,S,T> {
   static __device__ __forceinline__ void run(cplx<T> *a) {
     const T c1=(T) FGB_C51, c2=(T) FGB_C52;
-    const T s1=(T) S*(T) FGB_S51, s2=(T) S*(T) FGB_S52;
+    const T s1=(T) (S*FGB_S51), s2=(T) (S*FGB_S52);
     cplx<T> t1=a[1]+a[4], d1=a[1]-a[4];
     cplx<T> t2=a[2]+a[3], d2=a[2]-a[3];
     cplx<T> x0=a[0];
@@ -140,7 +145,7 @@ template<int S, typename T> struct Codelet<5,S,T> {
 template<int S, typename T> struct Codelet<7,S,T> {
   static __device__ __forceinline__ void run(cplx<T> *a) {
     const T C1=(T) FGB_C71, C2=(T) FGB_C72, C3=(T) FGB_C73;
-    const T S1=(T) S*(T) FGB_S71, S2=(T) S*(T) FGB_S72, S3=(T) S*(T) FGB_S73;
+    const T S1=(T) (S*FGB_S71), S2=(T) (S*FGB_S72), S3=(T) (S*FGB_S73);
     cplx<T> t1=a[1]+a[6], d1=a[1]-a[6];
     cplx<T> t2=a[2]+a[5], d2=a[2]-a[5];
     cplx<T> t3=a[3]+a[4], d3=a[3]-a[4];

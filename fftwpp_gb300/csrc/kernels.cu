@@ -156,11 +156,28 @@ __device__ __forceinline__ cplx<float> ldx(const cplx<float> *p)
   return *p;
 }
 
+template<bool CG>
+__device__ __forceinline__ cplx<ff> ldx(const cplx<ff> *p)
+{
+  if(CG) {
+    float4 v=__ldcg((const float4 *) p);
+    return mk(ff(v.x,v.y),ff(v.z,v.w));
+  }
+  return *p;
+}
+
 // Asynchronous global->shared copy of one complex element (cp.async; the
 // 16-byte form bypasses L1).  cpAsyncWait() waits for all of the thread's
 // copies; a __syncthreads() must follow before other threads read them.
 __device__ __forceinline__ void cpAsync(cplx<double> *dst,
                                         const cplx<double> *src)
+{
+  unsigned s=(unsigned) __cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n"
+               :: "r"(s), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cpAsync(cplx<ff> *dst, const cplx<ff> *src)
 {
   unsigned s=(unsigned) __cvta_generic_to_shared(dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n"
@@ -512,7 +529,7 @@ outerRealFwdKernel(const OuterPlan<T> P)
   for(int i=tid; i < Nh*tile; i += nthr) {
     int t=fdiv(i,invTile), cc=i-t*tile;
     int col=col0+cc;
-    T re=0, im=0;
+    T re=(T) 0, im=(T) 0;
     if(col < P.C) {
       int s=2*t;
       if(s < L) re=src[(long long) s*P.inRow+col];
@@ -874,12 +891,57 @@ cudaError_t launchOuterRealBwd(const OuterPlan<T>& P, int threads,
   template int batchBlocksPerSM<T>(int,size_t,int,int,int);
 
 // Each precision may be compiled as its own translation unit (build.py
-// compiles this file twice, in parallel).
-#ifndef FGB_ONLY_FLOAT
+// compiles this file once per precision, in parallel): FGB_ONLY_<P> keeps
+// one of DOUBLE, FLOAT and FF.
+#if !defined(FGB_ONLY_FLOAT) && !defined(FGB_ONLY_FF)
 FGB_INSTANTIATE(double)
 #endif
-#ifndef FGB_ONLY_DOUBLE
+#if !defined(FGB_ONLY_DOUBLE) && !defined(FGB_ONLY_FF)
 FGB_INSTANTIATE(float)
+#endif
+#if !defined(FGB_ONLY_DOUBLE) && !defined(FGB_ONLY_FLOAT)
+FGB_INSTANTIATE(ff)
+
+// ---------------------------------------------------------------------------
+// FP64 <-> float-float conversion at the boundary of the float-float mode:
+// hi is the float nearest to x and lo the float nearest to x - hi, so
+// hi + lo carries x to 2^-48 relative; the way back sums them in FP64.
+
+__global__ void __launch_bounds__(256) toFFKernel(ConvertArgs P)
+{
+  const size_t total=P.n*(size_t) P.count;
+  for(size_t i=blockIdx.x*(size_t) blockDim.x+threadIdx.x; i < total;
+      i += (size_t) gridDim.x*blockDim.x) {
+    int a=(int) (i/P.n);
+    size_t k=i-(size_t) a*P.n;
+    double x=((const double *) P.src[a])[k];
+    float hi=__double2float_rn(x);
+    float lo=__double2float_rn(x-(double) hi);
+    ((float2 *) P.dst[a])[k]=make_float2(hi,lo);
+  }
+}
+
+__global__ void __launch_bounds__(256) fromFFKernel(ConvertArgs P)
+{
+  const size_t total=P.n*(size_t) P.count;
+  for(size_t i=blockIdx.x*(size_t) blockDim.x+threadIdx.x; i < total;
+      i += (size_t) gridDim.x*blockDim.x) {
+    int a=(int) (i/P.n);
+    size_t k=i-(size_t) a*P.n;
+    float2 v=((const float2 *) P.src[a])[k];
+    ((double *) P.dst[a])[k]=(double) v.x+(double) v.y;
+  }
+}
+
+cudaError_t launchConvert(const ConvertArgs& P, bool toFF, cudaStream_t s)
+{
+  size_t total=P.n*(size_t) P.count;
+  if(total == 0) return cudaSuccess;
+  unsigned grid=(unsigned) std::min<size_t>((total+255)/256,152*16);
+  if(toFF) toFFKernel<<<grid,256,0,s>>>(P);
+  else fromFFKernel<<<grid,256,0,s>>>(P);
+  return cudaGetLastError();
+}
 #endif
 
 } // namespace fgb

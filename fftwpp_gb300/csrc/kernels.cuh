@@ -152,6 +152,16 @@ template<typename T> cudaError_t launchOuterRealBwd(const OuterPlan<T>& P,
                                                     int threads,
                                                     cudaStream_t s);
 
+// FP64 <-> float-float conversion of `count` arrays of n real values each
+// (complex data counts two reals per element).
+struct ConvertArgs {
+  const void *src[FGB_MAXA];
+  void *dst[FGB_MAXA];
+  int count;
+  size_t n;
+};
+cudaError_t launchConvert(const ConvertArgs& P, bool toFF, cudaStream_t s);
+
 // Shared-memory bytes each kernel needs (for plan-time sizing).
 template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc=1);
 template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc=1);

@@ -17,7 +17,8 @@ import ctypes
 from typing import Sequence
 
 from . import _native
-from ._native import CENTERED, F32, F64, HERMITIAN, MULT, PAD, REAL
+from ._native import (CENTERED, F32, F64, FF, HERMITIAN, MULT, PAD,
+                      PRECISIONS, REAL)
 
 __all__ = ["HybridConvolution", "BatchedConvolution", "PaddedTransform",
            "PAD", "CENTERED", "HERMITIAN", "REAL", "default_M"]
@@ -36,7 +37,8 @@ class HybridConvolution:
 
     kinds, L, M: per axis, outermost first.  m: optional forced residue
     block lengths (the reference's Application m).  precision: "f64" (the
-    drop-in mode) or "f32" (FP32 data with split hi+lo twiddles).
+    drop-in mode), "f32" (FP32 data with split hi+lo twiddles) or "ff"
+    (FP64 data, float-float arithmetic on the FP32 pipe).
     batch: independent 1D problems stored back to back.
     """
 
@@ -55,7 +57,9 @@ class HybridConvolution:
         self.A, self.B = A, B
         self.mult = mult
         self.precision = precision
-        self.prec = F64 if precision == "f64" else F32
+        if precision not in PRECISIONS:
+            raise ValueError(f"unknown precision {precision!r}")
+        self.prec = PRECISIONS[precision]
         self.batch = batch
         self.real = self.kinds[0] == REAL
         sz = ctypes.c_size_t
@@ -90,8 +94,8 @@ class HybridConvolution:
     def dtype(self):
         import torch
         if self.real:
-            return torch.float64 if self.prec == F64 else torch.float32
-        return torch.complex128 if self.prec == F64 else torch.complex64
+            return torch.float32 if self.prec == F32 else torch.float64
+        return torch.complex64 if self.prec == F32 else torch.complex128
 
     @property
     def normalization(self) -> int:
@@ -138,9 +142,16 @@ class HybridConvolution:
         import numpy as np
         if len(arrays) != self.A:
             raise ValueError(f"expected {self.A} inputs")
+        want = {"torch.float64": np.float64, "torch.float32": np.float32,
+                "torch.complex128": np.complex128,
+                "torch.complex64": np.complex64}[str(self.dtype)]
         for a in arrays:
             if not (isinstance(a, np.ndarray) and a.flags["C_CONTIGUOUS"]):
                 raise TypeError("host inputs must be C-contiguous numpy arrays")
+            # The library copies exactly this many bytes in and out.
+            if a.dtype != want or tuple(a.shape) != tuple(self.shape):
+                raise TypeError(f"host inputs must be {np.dtype(want).name} "
+                                f"arrays of shape {self.shape}")
         ptrs = (ctypes.c_void_p * self.A)(*[a.ctypes.data for a in arrays])
         rc = self.lib.fgb_convolve_host(self.handle, ptrs, ptrs)
         if rc != 0:
@@ -151,16 +162,19 @@ class HybridConvolution:
     def launch_names(self) -> list[str]:
         """Kernel launched at each position of one convolve call."""
         k = self.kinds
-        if self.dim == 1:
-            if self.long_path:
-                return ["outer_fwd_cols", "row_conv", "outer_bwd_cols"]
-            return ["herm_row" if k[0] == HERMITIAN else "row_conv"]
         inner = "herm_row" if k[-1] == HERMITIAN else "row_conv"
         x = "real" if k[0] == REAL else ""
-        if self.dim == 2:
-            return [f"outer{x}_fwd_x", inner, f"outer{x}_bwd_x"]
-        return [f"outer{x}_fwd_x", "outer_fwd_y", inner, "outer_bwd_y",
-                f"outer{x}_bwd_x"]
+        if self.dim == 1:
+            names = (["outer_fwd_cols", "row_conv", "outer_bwd_cols"]
+                     if self.long_path else [inner])
+        elif self.dim == 2:
+            names = [f"outer{x}_fwd_x", inner, f"outer{x}_bwd_x"]
+        else:
+            names = [f"outer{x}_fwd_x", "outer_fwd_y", inner, "outer_bwd_y",
+                     f"outer{x}_bwd_x"]
+        if self.prec == FF:
+            names = ["to_ff"] + names + ["from_ff"]
+        return names
 
     def enable_timing(self, on: bool = True) -> None:
         if self.lib.fgb_timing(self.handle, int(on)) != 0:
@@ -208,6 +222,9 @@ class BatchedConvolution:
                                    [2 * l - 1 for l in self.L])]
         self.n = len(self.L)
         self.A, self.B = A, B
+        if precision not in ("f64", "f32"):
+            raise ValueError(f"precision must be 'f64' or 'f32', not "
+                             f"{precision!r}")
         self.prec = F64 if precision == "f64" else F32
         sz = ctypes.c_size_t
         torch.cuda.current_device()
@@ -291,6 +308,9 @@ class PaddedTransform:
         self.kind, self.L, self.C = kind, int(L), int(C)
         self.M = int(M) if M is not None else default_M(kind, L)
         self.precision = precision
+        if precision not in ("f64", "f32"):
+            raise ValueError(f"precision must be 'f64' or 'f32', not "
+                             f"{precision!r}")
         self.prec = F64 if precision == "f64" else F32
         torch.cuda.current_device()
         self.handle = self.lib.fgb_pad_create(kind, self.L, self.M, self.C,

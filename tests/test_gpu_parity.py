@@ -3,7 +3,8 @@ against the CPU oracle (numpy restatement of FFTW++'s hybrid convolution,
 pinned to the compiled reference) on seeded inputs.
 
 Tolerances (relative L2, as the reference's tests measure it,
-tests/hybridconv.cc:118-129): 1e-13 in FP64, 2e-6 in FP32-compensated mode.
+tests/hybridconv.cc:118-129): 1e-13 in FP64 and in the float-float mode
+(FP64 data, hi+lo float arithmetic), 2e-6 in FP32-compensated mode.
 """
 import numpy as np
 import pytest
@@ -13,7 +14,7 @@ from oracle.direct import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"f64": 1e-13, "f32": 2e-6}
+TOL = {"f64": 1e-13, "ff": 1e-13, "f32": 2e-6}
 
 
 def _rand(rng, shape, real):
@@ -95,7 +96,7 @@ def _ids():
             + "-" + c[3] for c in CASES]
 
 
-@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("precision", ["f64", "ff", "f32"])
 @pytest.mark.parametrize("case", CASES, ids=_ids())
 def test_parity(case, precision, native_lib):
     kinds, L, M, mult = case
@@ -118,14 +119,27 @@ def test_forced_m(m, native_lib):
     assert rel_l2(got[0], want) <= 1e-13
 
 
-def test_long_1d(native_lib):
+@pytest.mark.parametrize("precision", ["f64", "ff"])
+def test_long_1d(native_lib, precision):
     """1D data too long for one CTA takes the column/row/column path."""
     kinds, L, M = [H.PAD], [20000], [39999]
     fs = _inputs(kinds, L, 2, seed=11)
     want = H.convolve(fs, kinds, L, M)[0]
-    got, conv = run_gpu(kinds, L, M, fs, "binary", "f64")
+    got, conv = run_gpu(kinds, L, M, fs, "binary", precision)
     assert conv.long_path
     assert rel_l2(got[0], want) <= 1e-13
+
+
+def test_float_float_large_2d(native_lib):
+    """The float-float mode on the 2D centred-Hermitian workload's full
+    size (1023 x 512 modes) against the FP64 GPU path, whose parity with
+    the oracle the tests above establish."""
+    kinds, L, M = [H.CENTERED, H.HERMITIAN], [1023, 1023], [1534, 1534]
+    fs = _inputs(kinds, L, 2, seed=21)
+    g64, _ = run_gpu(kinds, L, M, fs, "realbinary", "f64")
+    gff, conv = run_gpu(kinds, L, M, fs, "realbinary", "ff")
+    assert conv.launch_names()[0] == "to_ff"
+    assert rel_l2(gff[0], g64[0]) <= 1e-13
 
 
 def test_jacobian_2d(native_lib):
@@ -133,6 +147,27 @@ def test_jacobian_2d(native_lib):
     kinds, L, M = [H.CENTERED, H.HERMITIAN], [15, 15], [22, 22]
     fs = _inputs(kinds, L, 4, seed=5)
     want = H.convolve(fs, kinds, L, M, mult="realjacobian")[0]
-    for prec in ("f64", "f32"):
+    for prec in ("f64", "ff", "f32"):
         got, _ = run_gpu(kinds, L, M, fs, "realjacobian", prec)
         assert rel_l2(got[0], want) <= TOL[prec]
+
+
+@pytest.mark.parametrize("precision", ["f64", "ff", "f32"])
+def test_host_pointer_entry(native_lib, precision):
+    """fgb_convolve_host (copies inside the call) in every mode; host arrays
+    of the wrong type or shape are refused before any copy."""
+    from fftwpp_gb300.gpu import HybridConvolution
+    kinds, L, M = [H.CENTERED, H.HERMITIAN], [31, 31], [46, 46]
+    fs = _inputs(kinds, L, 2, seed=9)
+    want = H.convolve(fs, kinds, L, M, mult="realbinary")[0]
+    conv = HybridConvolution(kinds, L, M, mult="realbinary",
+                             precision=precision)
+    dt = np.complex64 if precision == "f32" else np.complex128
+    hs = [f.astype(dt) for f in fs]
+    conv.convolve_host(*hs)
+    assert rel_l2(hs[0], want) <= TOL[precision]
+    with pytest.raises(TypeError):
+        conv.convolve_host(*[f.astype(np.complex64 if dt == np.complex128
+                                      else np.complex128) for f in fs])
+    with pytest.raises(TypeError):
+        conv.convolve_host(*[f[:-1].copy().astype(dt) for f in fs])
