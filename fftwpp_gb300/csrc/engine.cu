@@ -8,6 +8,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <tuple>
+#include <type_traits>
 
 namespace fgb {
 
@@ -480,7 +481,6 @@ Conv::~Conv()
 {
   for(cudaEvent_t ev : events) cudaEventDestroy(ev);
   for(void *p : bufs) cudaFree(p);
-  for(void *p : ffBufs) cudaFree(p);
   if(hostIn) cudaFree(hostIn);
   if(hostOut) cudaFree(hostOut);
 }
@@ -524,20 +524,6 @@ void Conv::allocate()
     for(int a=0; a < A; ++a) get(e*rx*Ly*nz);
     for(int a=0; a < A; ++a) get(e*rx*ry*nz);
     nlaunch=5;
-  }
-  if(I.prec == PREC_FF) {
-    // The A converted inputs and B outputs in float-float form (the same
-    // size as the FP64 arrays), and a conversion launch on either side.
-    size_t bytes=elements()*elemBytes();
-    for(int a=0; a < A+I.B; ++a) {
-      void *p=NULL;
-      if(cudaMalloc(&p,bytes) != cudaSuccess)
-        throw std::runtime_error("device allocation of "+
-                                 std::to_string(bytes)+" bytes failed");
-      ffBufs.push_back(p);
-      staging += bytes;
-    }
-    nlaunch += 2;
   }
 }
 
@@ -590,6 +576,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.cshift=a.cshift; P.A=A; P.B=B; P.mult=I.mult;
     P.realIO=a.kind == KIND_REAL && I.dim == 1;
     P.rpc=I.axis[I.dim-1].rpc;
+    P.io64=0;
     P.fp=fftPlan(a.m,I.prec);
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };
@@ -597,6 +584,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.H=(int) a.stored; P.N=(int) a.N; P.Nh=(int) (a.N/2);
     P.A=A; P.B=B; P.mult=I.mult;
     P.rpc=a.rpc;
+    P.io64=0;
     P.fp=fftPlan(a.N/2,I.prec);
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };
@@ -606,7 +594,11 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.fp=fftPlan(a.kind == KIND_REAL ? a.N/2 : a.m,I.prec);
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
     P.twX=NULL; P.NX=1;
+    P.io64=0;
   };
+  // Float-float mode: the first launch reads the caller's FP64 arrays and
+  // the last one writes them.
+  const int IN64=std::is_same<T,ff>::value ? 1 : 0, OUT64=2*IN64;
 
   if(I.dim == 1 && !I.longRow) {
     const AxisPlan& a=I.axis[0];
@@ -616,6 +608,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
       for(int i=0; i < A; ++i) P.in[i]=(const Cx *) in[i];
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
       P.rowStride=a.stored; P.nrows=batch; P.scale=(T) scale;
+      P.io64=IN64 | OUT64;
       e=launchHermRow<T>(P,threads,batch,s);
       tick(s);
       return e;
@@ -625,6 +618,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) in[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
     P.rowStride=a.stored; P.nrows=batch; P.scale=(T) scale;
+    P.io64=IN64 | OUT64;
     e=launchRow<T>(P,threads,batch,s);
     tick(s);
     return e;
@@ -643,6 +637,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.count=A; O.nbatch=1; O.inBatch=O.outBatch=0;
     O.inRow=m; O.outRow=m; O.C=(int) m; O.Ltot=a.L;
     O.scale=(T) 1;
+    O.io64=IN64;
     for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) bufs[i];}
     e=launchOuterFwd<T>(O,threads,s);
     tick(s);
@@ -661,6 +656,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.tile=a.tileB;
     O.Ltot=a.L;
     O.scale=(T) scale;
+    O.io64=OUT64;
     for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) bufs[i]; O.out[i]=(Cx *) out[i];}
     e=launchOuterBwd<T>(O,threads,s);
     tick(s);
@@ -676,6 +672,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.count=A; O.nbatch=1; O.inBatch=O.outBatch=0;
     O.inRow=C; O.outRow=C; O.C=(int) C; O.Ltot=(long long) ax.L*C;
     O.scale=(T) 1;
+    O.io64=IN64;
     for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) bufs[i];}
     e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(O,threads,s) :
       launchOuterFwd<T>(O,threads,s);
@@ -701,6 +698,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.count=B;
     O.tile=ax.tileB;
     O.scale=(T) scale;
+    O.io64=OUT64;
     for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) bufs[i]; O.out[i]=(Cx *) out[i];}
     e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(O,threads,s) :
       launchOuterBwd<T>(O,threads,s);
@@ -722,6 +720,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   X.count=A; X.nbatch=1; X.inBatch=X.outBatch=0;
   X.inRow=Cx_; X.outRow=Cx_; X.C=(int) Cx_; X.Ltot=(long long) ax.L*Cx_;
   X.scale=(T) 1;
+  X.io64=IN64;
   for(int i=0; i < A; ++i) {X.in[i]=(const Cx *) in[i]; X.out[i]=(Cx *) bx[i];}
   e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(X,threads,s) :
     launchOuterFwd<T>(X,threads,s);
@@ -769,6 +768,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   X.count=B;
   X.tile=ax.tileB;
   X.scale=(T) scale;
+  X.io64=OUT64;
   for(int i=0; i < B; ++i) {X.in[i]=(const Cx *) bx[i]; X.out[i]=(Cx *) out[i];}
   e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(X,threads,s) :
     launchOuterBwd<T>(X,threads,s);
@@ -782,26 +782,7 @@ cudaError_t Conv::run(const void *const *in, void *const *out, cudaStream_t s)
   tick(s);
   if(I.prec == PREC_F64) return runT<double>(in,out,s);
   if(I.prec == PREC_F32) return runT<float>(in,out,s);
-  // Float-float: convert the FP64 inputs, convolve, convert the outputs.
-  const int A=I.A, B=I.B;
-  const size_t reals=elements()*elemBytes()/sizeof(double);
-  ConvertArgs C;
-  C.count=A; C.n=reals;
-  for(int a=0; a < A; ++a) {C.src[a]=in[a]; C.dst[a]=ffBufs[a];}
-  cudaError_t e=launchConvert(C,true,s);
-  tick(s);
-  if(e != cudaSuccess) return e;
-  std::vector<const void *> fin(A);
-  std::vector<void *> fout(B);
-  for(int a=0; a < A; ++a) fin[a]=ffBufs[a];
-  for(int b=0; b < B; ++b) fout[b]=ffBufs[A+b];
-  e=runT<ff>(fin.data(),fout.data(),s);
-  if(e != cudaSuccess) return e;
-  C.count=B;
-  for(int b=0; b < B; ++b) {C.src[b]=ffBufs[A+b]; C.dst[b]=out[b];}
-  e=launchConvert(C,false,s);
-  tick(s);
-  return e;
+  return runT<ff>(in,out,s);        // float-float, FP64 at the interface
 }
 
 cudaError_t Conv::runHost(const void *const *in, void *const *out,

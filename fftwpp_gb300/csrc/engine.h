@@ -82,8 +82,6 @@ private:
   ConvInfo I;
   long batch;
   std::vector<void *> bufs;        // device staging buffers
-  std::vector<void *> ffBufs;      // float-float mode: converted A inputs,
-                                   // then B outputs
   size_t staging;
   void *hostIn, *hostOut;          // device copies for runHost
   int nlaunch;

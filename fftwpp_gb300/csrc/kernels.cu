@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <type_traits>
 
 namespace fgb {
 
@@ -111,6 +112,92 @@ static int multVariant(int mult, int A, int B)
     case MULT_REALJACADJ:
       return A == 5 && B == 4 ? MULT_REALJACADJ : MULT_GENERIC;
     default: return MULT_GENERIC;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 values at the interface of the float-float mode.  The first kernel of
+// a convolution reads the caller's FP64 arrays and the last one writes them
+// (RowPlan::io64); complex FP64 and float-float elements are both 16 bytes,
+// so offsets are unchanged.  The split avoids the FP64 pipe: hi keeps the
+// leading 24 significand bits of x, lo the float nearest to the remaining
+// 29, so hi + lo = x to 2^-48 relative; values outside [2^-70, 2^101)
+// (zero, subnormals, huge values) take the FP64 conversion.
+
+__device__ __forceinline__ ff toFF(double x)
+{
+  unsigned long long b=(unsigned long long) __double_as_longlong(x);
+  int e=(int) ((b >> 52) & 0x7ff)-1023;
+  if(e < -70 || e > 100) {          // keep 2^(e-52) a normal float
+    float h=__double2float_rn(x);
+    return ff(h,__double2float_rn(x-(double) h));
+  }
+  unsigned sign=(unsigned) (b >> 32) & 0x80000000u;
+  float hi=__uint_as_float(sign | ((unsigned) (e+127) << 23) |
+                           (unsigned) ((b >> 29) & 0x7fffffu));
+  float lo=__uint2float_rn((unsigned) (b & 0x1fffffffull));    // < 2^29
+  lo=__fmul_rn(lo,__uint_as_float((unsigned) (e-52+127) << 23)); // * 2^(e-52)
+  lo=__uint_as_float(__float_as_uint(lo) | sign);
+  return ffFast(hi,lo);
+}
+
+__device__ __forceinline__ double fromFF(ff v)
+{
+  return (double) v.hi+(double) v.lo;
+}
+
+template<typename T>
+__device__ __forceinline__ cplx<T> loadIO(const cplx<T> *p, bool f64)
+{
+  if constexpr(std::is_same<T,ff>::value) {
+    if(f64) {
+      double2 d=*(const double2 *) p;
+      return mk(toFF(d.x),toFF(d.y));
+    }
+  }
+  return *p;
+}
+
+template<typename T>
+__device__ __forceinline__ T loadIOr(const T *p, bool f64)
+{
+  if constexpr(std::is_same<T,ff>::value)
+    if(f64) return toFF(*(const double *) p);
+  return *p;
+}
+
+template<typename T>
+__device__ __forceinline__ void storeIO(cplx<T> *p, cplx<T> v, bool f64)
+{
+  if constexpr(std::is_same<T,ff>::value) {
+    if(f64) {
+      *(double2 *) p=make_double2(fromFF(v.x),fromFF(v.y));
+      return;
+    }
+  }
+  *p=v;
+}
+
+template<typename T>
+__device__ __forceinline__ void storeIOr(T *p, T v, bool f64)
+{
+  if constexpr(std::is_same<T,ff>::value) {
+    if(f64) {
+      *(double *) p=fromFF(v);
+      return;
+    }
+  }
+  *p=v;
+}
+
+// Convert n elements staged in shared memory as FP64 (by cp.async) to
+// float-float in place; each thread converts the elements it copied.
+template<typename T>
+__device__ __forceinline__ void convertStaged(cplx<T> *y, int i)
+{
+  if constexpr(std::is_same<T,ff>::value) {
+    double2 d=*(double2 *) (y+i);
+    y[i]=mk(toFF(d.x),toFF(d.y));
   }
 }
 
@@ -226,7 +313,9 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
     cplx<T> v=mk((T) 0,(T) 0);
     if(row < P.nrows) {
       long long off=row*P.rowStride+s;
-      v=P.realIO ? mk(((const T *) P.in[a])[off],(T) 0) : ldx<CG>(P.in[a]+off);
+      if(P.realIO) v=mk(loadIOr((const T *) P.in[a]+off,P.io64 & 1),(T) 0);
+      else if(P.io64 & 1) v=loadIO(P.in[a]+off,true);
+      else v=ldx<CG>(P.in[a]+off);
     }
     fin[i]=v;
   }
@@ -270,8 +359,8 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
     long long row=row0+col-b*R;
     if(row >= P.nrows) continue;
     long long off=row*P.rowStride+s;
-    if(P.realIO) ((T *) P.out[b])[off]=acc[i].x*P.scale;
-    else P.out[b][off]=acc[i]*P.scale;
+    if(P.realIO) storeIOr((T *) P.out[b]+off,acc[i].x*P.scale,P.io64 & 2);
+    else storeIO(P.out[b]+off,acc[i]*P.scale,P.io64 & 2);
   }
   __syncthreads();
 }
@@ -317,7 +406,8 @@ hermRowKernel(const HermRowPlan<T> P)
       int col=fdiv(i,invH), k=i-col*H;
       int a=fdiv(col,invR);
       long long row=row0+col-a*R;
-      zin[i]=row < P.nrows ? P.in[a][row*P.rowStride+k] : mk((T) 0,(T) 0);
+      zin[i]=row < P.nrows ? loadIO(P.in[a]+row*P.rowStride+k,P.io64 & 1) :
+        mk((T) 0,(T) 0);
     }
     __syncthreads();
     // Y[k] = (Z[k] + conj Z[Nh-k]) + i W_N^k (Z[k] - conj Z[Nh-k])
@@ -353,7 +443,7 @@ hermRowKernel(const HermRowPlan<T> P)
       cplx<T> dd=zk-zm;
       cplx<T> o=mk(dd.y*half,-dd.x*half);
       cplx<T> v=e+twmul<-1>(o,tw[k]);
-      P.out[b][row*P.rowStride+k]=v*P.scale;
+      storeIO(P.out[b]+row*P.rowStride+k,v*P.scale,P.io64 & 2);
     }
     __syncthreads();
   }
@@ -389,6 +479,15 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
     else y[i]=mk((T) 0,(T) 0);
   }
   cpAsyncWait();
+  if(std::is_same<T,ff>::value && (P.io64 & 1)) {
+    // The caller's FP64 values were staged as they are: convert them.
+    for(int i=tid; i < L*tile; i += nthr) {
+      int s=fdiv(i,invTile), cc=i-s*tile;
+      int col=col0+cc;
+      long long off=(long long) s*P.inRow+col;
+      if(col < P.C && off < P.Ltot) convertStaged(y,i);
+    }
+  }
   __syncthreads();
   for(int i=tid; i < m*tile; i += nthr) {
     int t=fdiv(i,invTile), cc=i-t*tile;
@@ -491,7 +590,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
     int s=fdiv(i,invTile), cc=i-s*tile;
     int col=col0+cc;
     long long off=(long long) s*P.outRow+col;
-    if(col < P.C && off < P.Ltot) dst[off]=acc[i]*P.scale;
+    if(col < P.C && off < P.Ltot) storeIO(dst+off,acc[i]*P.scale,P.io64 & 2);
   }
   __syncthreads();
 }
@@ -532,8 +631,8 @@ outerRealFwdKernel(const OuterPlan<T> P)
     T re=(T) 0, im=(T) 0;
     if(col < P.C) {
       int s=2*t;
-      if(s < L) re=src[(long long) s*P.inRow+col];
-      if(s+1 < L) im=src[(long long) (s+1)*P.inRow+col];
+      if(s < L) re=loadIOr(src+(long long) s*P.inRow+col,P.io64 & 1);
+      if(s+1 < L) im=loadIOr(src+(long long) (s+1)*P.inRow+col,P.io64 & 1);
     }
     x[sp(i)]=mk(re,im);
   }
@@ -601,8 +700,8 @@ outerRealBwdKernel(const OuterPlan<T> P)
     if(col >= P.C) continue;
     cplx<T> v=X[sp(i)]*P.scale;
     int s=2*t;
-    if(s < L) dst[(long long) s*P.outRow+col]=v.x;
-    if(s+1 < L) dst[(long long) (s+1)*P.outRow+col]=v.y;
+    if(s < L) storeIOr(dst+(long long) s*P.outRow+col,v.x,P.io64 & 2);
+    if(s+1 < L) storeIOr(dst+(long long) (s+1)*P.outRow+col,v.y,P.io64 & 2);
   }
 }
 
@@ -902,46 +1001,6 @@ FGB_INSTANTIATE(float)
 #if !defined(FGB_ONLY_DOUBLE) && !defined(FGB_ONLY_FLOAT)
 FGB_INSTANTIATE(ff)
 
-// ---------------------------------------------------------------------------
-// FP64 <-> float-float conversion at the boundary of the float-float mode:
-// hi is the float nearest to x and lo the float nearest to x - hi, so
-// hi + lo carries x to 2^-48 relative; the way back sums them in FP64.
-
-__global__ void __launch_bounds__(256) toFFKernel(ConvertArgs P)
-{
-  const size_t total=P.n*(size_t) P.count;
-  for(size_t i=blockIdx.x*(size_t) blockDim.x+threadIdx.x; i < total;
-      i += (size_t) gridDim.x*blockDim.x) {
-    int a=(int) (i/P.n);
-    size_t k=i-(size_t) a*P.n;
-    double x=((const double *) P.src[a])[k];
-    float hi=__double2float_rn(x);
-    float lo=__double2float_rn(x-(double) hi);
-    ((float2 *) P.dst[a])[k]=make_float2(hi,lo);
-  }
-}
-
-__global__ void __launch_bounds__(256) fromFFKernel(ConvertArgs P)
-{
-  const size_t total=P.n*(size_t) P.count;
-  for(size_t i=blockIdx.x*(size_t) blockDim.x+threadIdx.x; i < total;
-      i += (size_t) gridDim.x*blockDim.x) {
-    int a=(int) (i/P.n);
-    size_t k=i-(size_t) a*P.n;
-    float2 v=((const float2 *) P.src[a])[k];
-    ((double *) P.dst[a])[k]=(double) v.x+(double) v.y;
-  }
-}
-
-cudaError_t launchConvert(const ConvertArgs& P, bool toFF, cudaStream_t s)
-{
-  size_t total=P.n*(size_t) P.count;
-  if(total == 0) return cudaSuccess;
-  unsigned grid=(unsigned) std::min<size_t>((total+255)/256,152*16);
-  if(toFF) toFFKernel<<<grid,256,0,s>>>(P);
-  else fromFFKernel<<<grid,256,0,s>>>(P);
-  return cudaGetLastError();
-}
 #endif
 
 } // namespace fgb

@@ -47,6 +47,8 @@ struct RowPlan {
   int A, B, mult;
   int realIO;              // real data in and out (1D fftPadReal rows)
   int rpc;                 // rows per CTA (their columns are interleaved)
+  int io64;                // float-float mode: bit 0, in[] holds FP64
+                           // values; bit 1, out[] takes FP64 values
   T scale;
   FFTPlanDev fp;           // length-m complex FFT
   const typename TwT<T>::type *twN;   // W_N^t, t < N
@@ -62,6 +64,7 @@ struct HermRowPlan {
   int N, Nh;               // real padded length (even) and N/2
   int A, B, mult;
   int rpc;                 // rows per CTA
+  int io64;                // as RowPlan::io64
   T scale;
   FFTPlanDev fp;           // length-Nh complex FFT
   const typename TwT<T>::type *twN;   // W_N^t, t < N
@@ -80,6 +83,7 @@ struct OuterPlan {
                            // s*dataRow + c < Ltot
   int L, m, q, N, cshift;
   int tile;
+  int io64;                // as RowPlan::io64
   T scale;
   FFTPlanDev fp;           // length-m (complex) or length-N/2 (real) FFT
   const typename TwT<T>::type *twN;
@@ -151,16 +155,6 @@ template<typename T> cudaError_t launchOuterRealFwd(const OuterPlan<T>& P,
 template<typename T> cudaError_t launchOuterRealBwd(const OuterPlan<T>& P,
                                                     int threads,
                                                     cudaStream_t s);
-
-// FP64 <-> float-float conversion of `count` arrays of n real values each
-// (complex data counts two reals per element).
-struct ConvertArgs {
-  const void *src[FGB_MAXA];
-  void *dst[FGB_MAXA];
-  int count;
-  size_t n;
-};
-cudaError_t launchConvert(const ConvertArgs& P, bool toFF, cudaStream_t s);
 
 // Shared-memory bytes each kernel needs (for plan-time sizing).
 template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc=1);

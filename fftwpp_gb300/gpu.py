@@ -172,8 +172,6 @@ class HybridConvolution:
         else:
             names = [f"outer{x}_fwd_x", "outer_fwd_y", inner, "outer_bwd_y",
                      f"outer{x}_bwd_x"]
-        if self.prec == FF:
-            names = ["to_ff"] + names + ["from_ff"]
         return names
 
     def enable_timing(self, on: bool = True) -> None:

@@ -138,7 +138,7 @@ def test_float_float_large_2d(native_lib):
     fs = _inputs(kinds, L, 2, seed=21)
     g64, _ = run_gpu(kinds, L, M, fs, "realbinary", "f64")
     gff, conv = run_gpu(kinds, L, M, fs, "realbinary", "ff")
-    assert conv.launch_names()[0] == "to_ff"
+    assert conv.launches == 3
     assert rel_l2(gff[0], g64[0]) <= 1e-13
 
 
@@ -171,3 +171,21 @@ def test_host_pointer_entry(native_lib, precision):
                                       else np.complex128) for f in fs])
     with pytest.raises(TypeError):
         conv.convolve_host(*[f[:-1].copy().astype(dt) for f in fs])
+
+
+@pytest.mark.parametrize("scales", [(1e-25, 1e30), (1e20, 1e-18), (1.0, 0.0),
+                                    (2.0 ** -69, 2.0 ** 69)])
+def test_float_float_scales(native_lib, scales):
+    """FP64 inputs far from 1 (both sides of the fast split's range, and
+    zero) in the float-float mode."""
+    kinds, L, M = [H.CENTERED, H.HERMITIAN], [31, 31], [46, 46]
+    fs = _inputs(kinds, L, 2, seed=13)
+    fs = [fs[0] * scales[0], fs[1] * scales[1]]
+    # A spread of magnitudes inside one array as well.
+    fs[0][::3] *= 1e-12
+    want = H.convolve(fs, kinds, L, M, mult="realbinary")[0]
+    got, _ = run_gpu(kinds, L, M, fs, "realbinary", "ff")
+    if not np.any(want):
+        assert not np.any(got[0])
+    else:
+        assert rel_l2(got[0], want) <= 1e-13
