@@ -90,6 +90,8 @@ def load():
     lib.fgb_pad_index.argtypes = [vp, sz, sz]
     lib.fgb_pad_destroy.restype = None
     lib.fgb_pad_destroy.argtypes = [vp]
+    lib.fgb_set_autotune.restype = None
+    lib.fgb_set_autotune.argtypes = [ctypes.c_int]
     lib.fgb_destroy.restype = None
     lib.fgb_destroy.argtypes = [vp]
     lib.fgb_last_error.restype = ctypes.c_char_p

@@ -652,6 +652,8 @@ int fgb_info(const fgb_conv *c, long *info)
   return 0;
 }
 
+void fgb_set_autotune(int on) {Conv::setAutotune(on != 0);}
+
 int fgb_set_normalize(fgb_conv *c, int normalize)
 {
   if(!c) return -1;

@@ -363,8 +363,8 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
       outerFwdSmem<float>(a.L,a.m,t);
   };
   auto smb=[&](int t) {
-    return wide(prec) ? outerBwdSmem<double>(a.L,a.m,t) :
-      outerBwdSmem<float>(a.L,a.m,t);
+    return wide(prec) ? outerBwdSmem<double>(a.L,a.m,t,(int) a.q) :
+      outerBwdSmem<float>(a.L,a.m,t,(int) a.q);
   };
   a.tile=pickTile(maxTile,C,nbatch*a.q*A,smf,minTile);
   a.tileB=pickTile(maxTile,C,nbatch*B,smb,minTile);
@@ -475,6 +475,115 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
       return rowNeed(prec,in.stored,in.m,A,B,r);});
   }
   allocate();
+  if(autotune) tune();
+}
+
+bool Conv::autotune=true;
+void Conv::setAutotune(bool on) {autotune=on;}
+
+void Conv::tune()
+{
+  struct Tunable {int *param; std::vector<int> cands; int launch;};
+  std::vector<Tunable> tn;
+  const int dim=I.dim, prec=I.prec, A=I.A, B=I.B;
+  AxisPlan& in=I.axis[dim-1];
+  long nrows=batch;
+  for(int d=0; d < dim-1; ++d) nrows *= I.axis[d].rows;
+
+  // Rows per CTA of the innermost-axis kernel.
+  {
+    Tunable t;
+    t.param=&in.rpc;
+    t.launch=I.longRow ? 1 : dim-1;
+    long avail=I.longRow ? I.rowQ : nrows;
+    for(int r : {1,2,3,4,6,8}) {
+      if(r > avail) break;
+      size_t need=I.longRow ? rowNeed(prec,I.rowM,I.rowM,A,B,r) :
+        in.kind == KIND_HERMITIAN ? hermNeed(prec,in.stored,in.N/2,A,r) :
+        rowNeed(prec,in.stored,in.m,A,B,r);
+      if(need <= SMEM_MAX) t.cands.push_back(r);
+    }
+    if(t.cands.size() > 1) tn.push_back(t);
+  }
+  // Column tiles of the outer-axis kernels (forward and backward).
+  if(!I.longRow) {
+    for(int d=0; d < dim-1; ++d) {
+      AxisPlan& a=I.axis[d];
+      long C=1;
+      for(int e=d+1; e < dim; ++e) C *= I.axis[e].stored;
+      Tunable f, b;
+      f.param=&a.tile;
+      b.param=&a.tileB;
+      f.launch=d;
+      b.launch=2*(dim-1)-d;
+      for(int t=1; t <= (wide(prec) ? 8 : 16) && t <= C; t *= 2) {
+        size_t sf, sb;
+        if(a.kind == KIND_REAL) {
+          sf=sb=wide(prec) ? outerRealSmem<double>(a.L,a.N/2,t) :
+            outerRealSmem<float>(a.L,a.N/2,t);
+        } else {
+          sf=wide(prec) ? outerFwdSmem<double>(a.L,a.m,t) :
+            outerFwdSmem<float>(a.L,a.m,t);
+          sb=wide(prec) ? outerBwdSmem<double>(a.L,a.m,t,(int) a.q) :
+            outerBwdSmem<float>(a.L,a.m,t,(int) a.q);
+        }
+        if(sf <= SMEM_MAX) f.cands.push_back(t);
+        if(sb <= SMEM_MAX) b.cands.push_back(t);
+      }
+      if(f.cands.size() > 1) tn.push_back(f);
+      if(b.cands.size() > 1) tn.push_back(b);
+    }
+  }
+  if(tn.empty()) return;
+
+  // Scratch arrays (zeros: the kernels' timing does not depend on values).
+  const size_t bytes=elements()*elemBytes();
+  std::vector<void *> tin(A,NULL), tout(B,NULL);
+  cudaStream_t s=NULL;
+  bool ok=cudaStreamCreateWithFlags(&s,cudaStreamNonBlocking) == cudaSuccess;
+  for(auto& p : tin)
+    ok=ok && cudaMalloc(&p,bytes) == cudaSuccess &&
+      cudaMemsetAsync(p,0,bytes,s) == cudaSuccess;
+  for(auto& p : tout) ok=ok && cudaMalloc(&p,bytes) == cudaSuccess;
+  const bool wasTiming=timing;
+  ok=ok && enableTiming(true) == cudaSuccess;
+  std::vector<int> keep;
+  for(auto& t : tn) keep.push_back(*t.param);
+  if(ok) {
+    size_t K=0;
+    for(auto& t : tn) K=std::max(K,t.cands.size());
+    std::vector<std::vector<double>> ms(tn.size(),
+                                        std::vector<double>(K,1e300));
+    std::vector<double> lt(nlaunch);
+    for(size_t k=0; k < K && ok; ++k) {
+      for(auto& t : tn) *t.param=t.cands[std::min(k,t.cands.size()-1)];
+      for(int rep=0; rep < 3 && ok; ++rep) {
+        ok=run(tin.data(),tout.data(),s) == cudaSuccess &&
+          cudaStreamSynchronize(s) == cudaSuccess;
+        if(!ok || rep == 0) continue;
+        std::fill(lt.begin(),lt.end(),0.0);
+        collect(lt.data(),nlaunch);
+        for(size_t i=0; i < tn.size(); ++i)
+          if(k < tn[i].cands.size())
+            ms[i][k]=std::min(ms[i][k],lt[tn[i].launch]);
+      }
+    }
+    if(ok)
+      for(size_t i=0; i < tn.size(); ++i) {
+        size_t bk=0;
+        for(size_t k=1; k < tn[i].cands.size(); ++k)
+          if(ms[i][k] < ms[i][bk]) bk=k;
+        keep[i]=tn[i].cands[bk];
+      }
+  }
+  // The planner's choice stays wherever timing failed.
+  for(size_t i=0; i < tn.size(); ++i) *tn[i].param=keep[i];
+  timing=wasTiming;
+  cudaGetLastError();
+  if(s) cudaStreamSynchronize(s);
+  for(void *p : tin) if(p) cudaFree(p);
+  for(void *p : tout) if(p) cudaFree(p);
+  if(s) cudaStreamDestroy(s);
 }
 
 Conv::~Conv()

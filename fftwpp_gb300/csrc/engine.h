@@ -78,6 +78,14 @@ public:
   // Normalise by 1/prod(N) (Convolution::convolve) or not (convolveRaw).
   void setNormalize(bool on) {normalize=on;}
 
+  // Plan-time autotuning (the GPU counterpart of FFTW++'s optimiser,
+  // convolve.cc:177-470): rows per CTA of the innermost-axis kernel and the
+  // column tiles of the outer-axis kernels are chosen by timing every
+  // candidate on scratch data; each launch depends on its own parameter
+  // only, so one timed convolution per candidate index serves them all.
+  // Runs in the constructor unless disabled process-wide.
+  static void setAutotune(bool on);
+
 private:
   ConvInfo I;
   long batch;
@@ -87,12 +95,14 @@ private:
   int nlaunch;
   bool timing;
   bool normalize;
+  static bool autotune;
   std::vector<cudaEvent_t> events;
   int marks;
   void tick(cudaStream_t s);
   template<typename T> cudaError_t runT(const void *const *in,
                                         void *const *out, cudaStream_t s);
   void allocate();
+  void tune();
 };
 
 // Twiddle table W_n^t = exp(2 pi i t/n), t < n, on the current device,

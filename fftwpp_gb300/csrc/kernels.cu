@@ -389,8 +389,7 @@ hermRowKernel(const HermRowPlan<T> P)
   extern __shared__ __align__(16) unsigned char smemRaw[];
   const int A=P.A, B=P.B, H=P.H, Nh=P.Nh, R=P.rpc;
   const int ld=A*R, lb=B*R;
-  cplx<T> *zin=(cplx<T> *) smemRaw;
-  cplx<T> *x=zin+ld*H;
+  cplx<T> *x=(cplx<T> *) smemRaw;
   cplx<T> *y=x+padded(Nh*ld);
   const int tid=threadIdx.x, nthr=blockDim.x;
   const typename TwT<T>::type *tw=P.twN;
@@ -402,21 +401,21 @@ hermRowKernel(const HermRowPlan<T> P)
   // Rows g*R .. g*R+R-1 are transformed together; column col = a*R + rho.
   for(long long g=blockIdx.x; g < groups; g += gridDim.x) {
     const long long row0=g*R;
-    for(int i=tid; i < ld*H; i += nthr) {
-      int col=fdiv(i,invH), k=i-col*H;
-      int a=fdiv(col,invR);
-      long long row=row0+col-a*R;
-      zin[i]=row < P.nrows ? loadIO(P.in[a]+row*P.rowStride+k,P.io64 & 1) :
-        mk((T) 0,(T) 0);
-    }
-    __syncthreads();
-    // Y[k] = (Z[k] + conj Z[Nh-k]) + i W_N^k (Z[k] - conj Z[Nh-k])
+    // Y[k] = (Z[k] + conj Z[Nh-k]) + i W_N^k (Z[k] - conj Z[Nh-k]), with
+    // Z read from the row itself (the two reads of an element are L1/L2
+    // hits; every read of the group precedes its writes, so in = out is
+    // safe).
     for(int i=tid; i < Nh*ld; i += nthr) {
       int k=fdiv(i,invLd), col=i-k*ld;
-      cplx<T> zk=k < H ? zin[col*H+k] : mk((T) 0,(T) 0);
+      int a=fdiv(col,invR);
+      long long row=row0+col-a*R;
+      const cplx<T> *zr=P.in[a]+row*P.rowStride;
+      const bool live=row < P.nrows;
+      cplx<T> zk=live && k < H ? loadIO(zr+k,P.io64 & 1) : mk((T) 0,(T) 0);
       if(k == 0) zk.y=(T) 0;
       int kk=Nh-k;
-      cplx<T> zc=kk < H ? conjg(zin[col*H+kk]) : mk((T) 0,(T) 0);
+      cplx<T> zc=live && kk < H ? conjg(loadIO(zr+kk,P.io64 & 1)) :
+        mk((T) 0,(T) 0);
       cplx<T> s=zk+zc;
       cplx<T> d=twmul<1>(zk-zc,tw[k]);
       x[sp(i)]=mk(s.x-d.y,s.y+d.x);
@@ -533,8 +532,11 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
                                              int z, unsigned char *smemRaw)
 {
   const int tile=P.tile, m=P.m, N=P.N, c=P.cshift, L=P.L;
+  // One residue: the outputs come straight from the transform, with no
+  // accumulator in shared memory.
+  const bool direct=P.q == 1;
   cplx<T> *acc=(cplx<T> *) smemRaw;
-  cplx<T> *x=acc+L*tile;
+  cplx<T> *x=direct ? acc : acc+L*tile;
   cplx<T> *y=x+padded(m*tile);
   const int tid=threadIdx.x, nthr=blockDim.x;
   const int col0=ctile*tile;
@@ -545,7 +547,8 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
   const typename TwT<T>::type *tw=P.twN;
   const float invTile=1.0f/(float) tile;
 
-  for(int i=tid; i < L*tile; i += nthr) acc[i]=mk((T) 0,(T) 0);
+  if(!direct)
+    for(int i=tid; i < L*tile; i += nthr) acc[i]=mk((T) 0,(T) 0);
   for(int r=0; r < P.q; ++r) {
     if(CG) {
       // Data written by other CTAs of this launch: L2 loads.
@@ -577,6 +580,17 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
       __syncthreads();
     }
     cplx<T> *X=fftSmem<T,-1>(x,y,P.fp,tile,tile,tid,nthr);
+    if(direct) {
+      for(int i=tid; i < L*tile; i += nthr) {
+        int s=fdiv(i,invTile), cc=i-s*tile;
+        int col=col0+cc;
+        long long off=(long long) s*P.outRow+col;
+        if(col < P.C && off < P.Ltot)
+          storeIO(dst+off,X[sp(posmod(s-c,m)*tile+cc)]*P.scale,P.io64 & 2);
+      }
+      __syncthreads();
+      return;
+    }
     for(int i=tid; i < L*tile; i += nthr) {
       int s=fdiv(i,invTile), cc=i-s*tile;
       int t=posmod(s-c,m);
@@ -861,16 +875,17 @@ template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc)
 }
 template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc)
 {
-  return sizeof(cplx<T>)*((size_t) A*rpc*H+2*(size_t) padded(Nh*A*rpc));
+  return sizeof(cplx<T>)*2*(size_t) padded(Nh*A*rpc);
 }
 template<typename T> size_t outerFwdSmem(int L, int m, int tile)
 {
   size_t pm=padded(m*tile);
   return sizeof(cplx<T>)*(pm+std::max(pm,(size_t) L*tile));
 }
-template<typename T> size_t outerBwdSmem(int L, int m, int tile)
+template<typename T> size_t outerBwdSmem(int L, int m, int tile, int q)
 {
-  return sizeof(cplx<T>)*((size_t) L*tile+2*(size_t) padded(m*tile));
+  size_t acc=q == 1 ? 0 : (size_t) L*tile;
+  return sizeof(cplx<T>)*(acc+2*(size_t) padded(m*tile));
 }
 template<typename T> size_t outerRealSmem(int L, int Nh, int tile)
 {
@@ -942,7 +957,7 @@ cudaError_t launchOuterFwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
 template<typename T>
 cudaError_t launchOuterBwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
 {
-  size_t sm=outerBwdSmem<T>(P.L,P.m,P.tile);
+  size_t sm=outerBwdSmem<T>(P.L,P.m,P.tile,P.q);
   cudaError_t e=setSmem(outerBwdKernel<T>,sm);
   if(e != cudaSuccess) return e;
   dim3 grid((P.C+P.tile-1)/P.tile,1,P.nbatch*P.count);
@@ -984,7 +999,7 @@ cudaError_t launchOuterRealBwd(const OuterPlan<T>& P, int threads,
   template size_t rowSmem<T>(int,int,int,int,int); \
   template size_t hermRowSmem<T>(int,int,int,int); \
   template size_t outerFwdSmem<T>(int,int,int); \
-  template size_t outerBwdSmem<T>(int,int,int); \
+  template size_t outerBwdSmem<T>(int,int,int,int); \
   template size_t outerRealSmem<T>(int,int,int); \
   template cudaError_t launchBatch<T>(const BatchArgs<T>&,int,int,size_t,cudaStream_t); \
   template int batchBlocksPerSM<T>(int,size_t,int,int,int);

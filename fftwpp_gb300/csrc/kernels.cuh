@@ -160,7 +160,9 @@ template<typename T> cudaError_t launchOuterRealBwd(const OuterPlan<T>& P,
 template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc=1);
 template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc=1);
 template<typename T> size_t outerFwdSmem(int L, int m, int tile);
-template<typename T> size_t outerBwdSmem(int L, int m, int tile);
+// q == 1: the backward writes its outputs without an accumulator; q = 0
+// sizes for any residue count.
+template<typename T> size_t outerBwdSmem(int L, int m, int tile, int q=0);
 template<typename T> size_t outerRealSmem(int L, int Nh, int tile);
 
 } // namespace fgb

@@ -73,6 +73,13 @@ int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out);
  * (convolve.h:123-145). */
 int fgb_info(const fgb_conv *c, long *info);
 
+/* Plan-time autotuning, process-wide (default on): fgb_create times the
+ * candidate rows-per-CTA of the innermost-axis kernel and column tiles of
+ * the outer-axis kernels on scratch data and keeps the fastest, the GPU
+ * counterpart of FFTW++'s optimiser (convolve.cc:177-470).  0 keeps the
+ * planner's cost-model choice. */
+void fgb_set_autotune(int on);
+
 /* Normalisation switch: 1 (default) scales the result by 1/prod(m q) as
  * Convolution::convolve does; 0 returns the unnormalised sum of
  * Convolution::convolveRaw (convolve.h:1151-1160). */

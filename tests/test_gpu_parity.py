@@ -189,3 +189,19 @@ def test_float_float_scales(native_lib, scales):
         assert not np.any(got[0])
     else:
         assert rel_l2(got[0], want) <= 1e-13
+
+
+@pytest.mark.parametrize("precision", ["f64", "ff", "f32"])
+def test_autotune_changes_schedule_only(native_lib, precision):
+    """Autotuned tiles and rows per CTA regroup columns and rows across
+    CTAs without changing any arithmetic: results are bit-identical to the
+    cost-model plan."""
+    kinds, L, M = [H.REAL, H.PAD, H.PAD], [12, 10, 9], [23, 19, 17]
+    fs = _inputs(kinds, L, 2, seed=17)
+    try:
+        native_lib.fgb_set_autotune(0)
+        plain, c0 = run_gpu(kinds, L, M, fs, "binary", precision)
+    finally:
+        native_lib.fgb_set_autotune(1)
+    tuned, c1 = run_gpu(kinds, L, M, fs, "binary", precision)
+    assert np.array_equal(plain[0], tuned[0])
