@@ -175,26 +175,26 @@ static const size_t SMEM_MAX=227*1024;
 
 // 16-byte complex elements (FP64 and float-float) or 8-byte ones (FP32).
 static bool wide(int prec) {return prec != PREC_F32;}
+
+// A kernel-side size function evaluated for the arithmetic type of prec.
+#define FGB_BY_PREC(prec,F,...) ((prec) == PREC_F64 ? F<double>(__VA_ARGS__) : \
+  (prec) == PREC_FF ? F<ff>(__VA_ARGS__) : F<float>(__VA_ARGS__))
 static size_t elem(int prec) {return wide(prec) ? 16 : 8;}
 
 static size_t rowNeed(int prec, long L, long m, int A, int B, int rpc=1)
 {
-  return wide(prec) ? rowSmem<double>(L,m,A,B,rpc) :
-    rowSmem<float>(L,m,A,B,rpc);
+  return FGB_BY_PREC(prec,rowSmem,L,m,A,B,rpc);
 }
 
 static size_t hermNeed(int prec, long H, long Nh, int A, int rpc=1)
 {
-  return wide(prec) ? hermRowSmem<double>(H,Nh,A,rpc) :
-    hermRowSmem<float>(H,Nh,A,rpc);
+  return FGB_BY_PREC(prec,hermRowSmem,H,Nh,A,rpc);
 }
 
 static size_t outerNeed(int prec, long L, long m, int tile)
 {
-  size_t f=wide(prec) ? outerFwdSmem<double>(L,m,tile) :
-    outerFwdSmem<float>(L,m,tile);
-  size_t b=wide(prec) ? outerBwdSmem<double>(L,m,tile) :
-    outerBwdSmem<float>(L,m,tile);
+  size_t f=FGB_BY_PREC(prec,outerFwdSmem,L,m,tile);
+  size_t b=FGB_BY_PREC(prec,outerBwdSmem,L,m,tile);
   return std::max(f,b);
 }
 
@@ -321,8 +321,7 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
     a.rows=a.N/2+1;
     long Nh=a.N/2;
     auto sm=[&](int t) {
-      return wide(prec) ? outerRealSmem<double>(a.L,Nh,t) :
-        outerRealSmem<float>(a.L,Nh,t);
+      return FGB_BY_PREC(prec,outerRealSmem,a.L,Nh,t);
     };
     a.tile=pickTile(maxTile,C,nbatch*A,sm,minTile);
     a.tileB=pickTile(maxTile,C,nbatch*B,sm,minTile);
@@ -359,12 +358,10 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
   a.cshift=centered ? (int) (a.L/2) : 0;
   a.rows=a.N;
   auto smf=[&](int t) {
-    return wide(prec) ? outerFwdSmem<double>(a.L,a.m,t) :
-      outerFwdSmem<float>(a.L,a.m,t);
+    return FGB_BY_PREC(prec,outerFwdSmem,a.L,a.m,t);
   };
   auto smb=[&](int t) {
-    return wide(prec) ? outerBwdSmem<double>(a.L,a.m,t,(int) a.q) :
-      outerBwdSmem<float>(a.L,a.m,t,(int) a.q);
+    return FGB_BY_PREC(prec,outerBwdSmem,a.L,a.m,t,(int) a.q);
   };
   a.tile=pickTile(maxTile,C,nbatch*a.q*A,smf,minTile);
   a.tileB=pickTile(maxTile,C,nbatch*B,smb,minTile);
@@ -519,13 +516,10 @@ void Conv::tune()
       for(int t=1; t <= (wide(prec) ? 8 : 16) && t <= C; t *= 2) {
         size_t sf, sb;
         if(a.kind == KIND_REAL) {
-          sf=sb=wide(prec) ? outerRealSmem<double>(a.L,a.N/2,t) :
-            outerRealSmem<float>(a.L,a.N/2,t);
+          sf=sb=FGB_BY_PREC(prec,outerRealSmem,a.L,a.N/2,t);
         } else {
-          sf=wide(prec) ? outerFwdSmem<double>(a.L,a.m,t) :
-            outerFwdSmem<float>(a.L,a.m,t);
-          sb=wide(prec) ? outerBwdSmem<double>(a.L,a.m,t,(int) a.q) :
-            outerBwdSmem<float>(a.L,a.m,t,(int) a.q);
+          sf=FGB_BY_PREC(prec,outerFwdSmem,a.L,a.m,t);
+          sb=FGB_BY_PREC(prec,outerBwdSmem,a.L,a.m,t,(int) a.q);
         }
         if(sf <= SMEM_MAX) f.cands.push_back(t);
         if(sb <= SMEM_MAX) b.cands.push_back(t);

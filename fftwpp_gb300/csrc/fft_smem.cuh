@@ -227,4 +227,98 @@ __device__ cplx<T> *fftSmem(cplx<T> *x, cplx<T> *y, const FFTPlanDev& p,
   return x;
 }
 
+// ---------------------------------------------------------------------------
+// In-place transforms for convolutions.  A decimation-in-frequency pass
+// (fftDIF) takes natural order and leaves the spectrum in mixed-radix
+// digit-reversed order; a decimation-in-time pass (fftDIT) over the same
+// radices takes that order back to natural.  A pointwise product between
+// them does not care about the order, so a convolution needs no
+// permutation, and since every butterfly reads and writes the same R
+// elements one buffer suffices (half the shared memory of the ping-pong
+// Stockham form).  Stage with span Ls (m = Ls/R): butterfly (b, j) takes
+// elements b Ls + j + r m; DIF multiplies output r by W_Ls^{S r j} after
+// the R-point DFT, DIT multiplies input r by it before.
+template<typename T, int R, int S, bool DIF>
+__device__ __forceinline__ void ipStage(cplx<T> *__restrict__ x, int n, int Ls,
+                                        int ncol, int ld,
+                                        const typename TwT<T>::type *__restrict__ tw,
+                                        int tid, int nthr)
+{
+  const int m=Ls/R;
+  const int tstride=n/Ls;
+  const int total=(n/R)*ncol;
+  const float invNcol=1.0f/(float) ncol;
+  const float invM=1.0f/(float) m;
+  for(int idx=tid; idx < total; idx += nthr) {
+    int q=fdiv(idx,invNcol);
+    int c=idx-q*ncol;
+    int b=fdiv(q,invM);
+    int j=q-b*m;
+    int base=b*Ls+j;
+    cplx<T> a[R];
+#pragma unroll
+    for(int r=0; r < R; ++r) a[r]=x[sp((base+r*m)*ld+c)];
+    if(!DIF && m > 1) {
+#pragma unroll
+      for(int r=1; r < R; ++r) a[r]=twmul<S>(a[r],tw[r*j*tstride]);
+    }
+    Codelet<R,S,T>::run(a);
+    if(DIF && m > 1) {
+#pragma unroll
+      for(int r=1; r < R; ++r) a[r]=twmul<S>(a[r],tw[r*j*tstride]);
+    }
+#pragma unroll
+    for(int r=0; r < R; ++r) x[sp((base+r*m)*ld+c)]=a[r];
+  }
+}
+
+template<typename T, int S, bool DIF>
+__device__ __forceinline__ void ipDispatch(int R, cplx<T> *x, int n, int Ls,
+                                           int ncol, int ld,
+                                           const typename TwT<T>::type *tw,
+                                           int tid, int nthr)
+{
+  switch(R) {
+    case 8: ipStage<T,8,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;
+    case 4: ipStage<T,4,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;
+    case 2: ipStage<T,2,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;
+    case 3: ipStage<T,3,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;
+    case 5: ipStage<T,5,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;
+    case 7: ipStage<T,7,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;
+    default: break;
+  }
+}
+
+// Natural order in, digit-reversed spectrum out (in place).  Every thread
+// of the block calls it after the block has synchronised; it returns
+// synchronised.
+template<typename T, int S>
+__device__ void fftDIF(cplx<T> *x, const FFTPlanDev& p, int ncol, int ld,
+                       int tid, int nthr)
+{
+  const typename TwT<T>::type *tw=(const typename TwT<T>::type *) p.tw;
+  int Ls=p.n;
+  for(int s=0; s < p.nst; ++s) {
+    int R=p.radix[s];
+    ipDispatch<T,S,true>(R,x,p.n,Ls,ncol,ld,tw,tid,nthr);
+    __syncthreads();
+    Ls /= R;
+  }
+}
+
+// Digit-reversed spectrum (as fftDIF leaves it) in, natural order out.
+template<typename T, int S>
+__device__ void fftDIT(cplx<T> *x, const FFTPlanDev& p, int ncol, int ld,
+                       int tid, int nthr)
+{
+  const typename TwT<T>::type *tw=(const typename TwT<T>::type *) p.tw;
+  int Ls=1;
+  for(int s=p.nst-1; s >= 0; --s) {
+    int R=p.radix[s];
+    Ls *= R;
+    ipDispatch<T,S,false>(R,x,p.n,Ls,ncol,ld,tw,tid,nthr);
+    __syncthreads();
+  }
+}
+
 } // namespace fgb

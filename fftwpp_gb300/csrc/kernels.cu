@@ -201,6 +201,14 @@ __device__ __forceinline__ void convertStaged(cplx<T> *y, int i)
   }
 }
 
+// The row kernels transform in place (fftDIF/fftDIT, one buffer) on the
+// FP32 pipe; the FP64 form keeps the ping-pong Stockham transform, which
+// measured faster on GB300's FP64 pipe.
+template<typename T> __host__ __device__ constexpr bool inplaceFFT()
+{
+  return !std::is_same<T,double>::value;
+}
+
 // Exponent ((s-c) mod N)*r mod N of a residue twiddle.
 __device__ __forceinline__ int twExp(int s, int c, int r, int N)
 {
@@ -299,7 +307,7 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
   cplx<T> *fin=(cplx<T> *) smemRaw;
   cplx<T> *acc=fin+ld*L;
   cplx<T> *x=acc+lb*L;
-  cplx<T> *y=x+padded(m*ld);
+  cplx<T> *y=x+padded(m*ld);         // ping-pong buffer of the FP64 form
   const int tid=threadIdx.x, nthr=blockDim.x;
   const typename TwT<T>::type *tw=P.twN;
   const float invL=1.0f/(float) L, invLd=1.0f/(float) ld;
@@ -336,14 +344,26 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
       x[sp(i)]=sum;
     }
     __syncthreads();
-    cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
-    cplx<T> *Y=X == x ? y : x;
-    for(int i=tid; i < m*R; i += nthr) {
-      int j=fdiv(i,invR), rho=i-j*R;
-      multiplySlot<K>(X,j*ld+rho,R,A,B,P.mult);
+    const cplx<T> *Z;
+    if constexpr(inplaceFFT<T>()) {
+      fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
+      for(int i=tid; i < m*R; i += nthr) {
+        int j=fdiv(i,invR), rho=i-j*R;
+        multiplySlot<K>(x,j*ld+rho,R,A,B,P.mult);
+      }
+      __syncthreads();
+      fftDIT<T,-1>(x,P.fp,lb,ld,tid,nthr);
+      Z=x;
+    } else {
+      cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
+      cplx<T> *Y=X == x ? y : x;
+      for(int i=tid; i < m*R; i += nthr) {
+        int j=fdiv(i,invR), rho=i-j*R;
+        multiplySlot<K>(X,j*ld+rho,R,A,B,P.mult);
+      }
+      __syncthreads();
+      Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
     }
-    __syncthreads();
-    cplx<T> *Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
     for(int i=tid; i < lb*L; i += nthr) {
       int col=fdiv(i,invL), s=i-col*L;
       int t=posmod(s-c,m);
@@ -390,7 +410,7 @@ hermRowKernel(const HermRowPlan<T> P)
   const int A=P.A, B=P.B, H=P.H, Nh=P.Nh, R=P.rpc;
   const int ld=A*R, lb=B*R;
   cplx<T> *x=(cplx<T> *) smemRaw;
-  cplx<T> *y=x+padded(Nh*ld);
+  cplx<T> *y=x+padded(Nh*ld);        // ping-pong buffer of the FP64 form
   const int tid=threadIdx.x, nthr=blockDim.x;
   const typename TwT<T>::type *tw=P.twN;
   const T half=(T) 0.5;
@@ -421,14 +441,26 @@ hermRowKernel(const HermRowPlan<T> P)
       x[sp(i)]=mk(s.x-d.y,s.y+d.x);
     }
     __syncthreads();
-    cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
-    cplx<T> *Y=X == x ? y : x;
-    for(int i=tid; i < Nh*R; i += nthr) {
-      int t=fdiv(i,invR), rho=i-t*R;
-      multiplySlot<K>(X,t*ld+rho,R,A,B,P.mult);
+    const cplx<T> *Z;
+    if constexpr(inplaceFFT<T>()) {
+      fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
+      for(int i=tid; i < Nh*R; i += nthr) {
+        int t=fdiv(i,invR), rho=i-t*R;
+        multiplySlot<K>(x,t*ld+rho,R,A,B,P.mult);
+      }
+      __syncthreads();
+      fftDIT<T,-1>(x,P.fp,lb,ld,tid,nthr);
+      Z=x;
+    } else {
+      cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
+      cplx<T> *Y=X == x ? y : x;
+      for(int i=tid; i < Nh*R; i += nthr) {
+        int t=fdiv(i,invR), rho=i-t*R;
+        multiplySlot<K>(X,t*ld+rho,R,A,B,P.mult);
+      }
+      __syncthreads();
+      Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
     }
-    __syncthreads();
-    cplx<T> *Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
     // V[k] = E[k] + W_N^{-k} O[k],  E=(Zk+conj Zm)/2, O=(Zk-conj Zm)/(2i)
     for(int i=tid; i < lb*H; i += nthr) {
       int col=fdiv(i,invH), k=i-col*H;
@@ -871,11 +903,13 @@ int batchBlocksPerSM(int threads, size_t smem, int mult, int A, int B)
 // outer kernel also stages its L x tile input block in the second buffer.
 template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc)
 {
-  return sizeof(cplx<T>)*((size_t) (A+B)*rpc*L+2*(size_t) padded(m*A*rpc));
+  size_t nbuf=inplaceFFT<T>() ? 1 : 2;
+  return sizeof(cplx<T>)*((size_t) (A+B)*rpc*L+nbuf*(size_t) padded(m*A*rpc));
 }
 template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc)
 {
-  return sizeof(cplx<T>)*2*(size_t) padded(Nh*A*rpc);
+  size_t nbuf=inplaceFFT<T>() ? 1 : 2;
+  return sizeof(cplx<T>)*nbuf*(size_t) padded(Nh*A*rpc);
 }
 template<typename T> size_t outerFwdSmem(int L, int m, int tile)
 {
