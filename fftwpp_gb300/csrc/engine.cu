@@ -357,11 +357,12 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
   a.p=ceilquotient(a.L,a.m);
   a.cshift=centered ? (int) (a.L/2) : 0;
   a.rows=a.N;
+  const int ip=a.p == 1;     // in-place outer transforms (FP32-pipe modes)
   auto smf=[&](int t) {
-    return FGB_BY_PREC(prec,outerFwdSmem,a.L,a.m,t);
+    return FGB_BY_PREC(prec,outerFwdSmem,a.L,a.m,t,ip);
   };
   auto smb=[&](int t) {
-    return FGB_BY_PREC(prec,outerBwdSmem,a.L,a.m,t,(int) a.q);
+    return FGB_BY_PREC(prec,outerBwdSmem,a.L,a.m,t,(int) a.q,ip);
   };
   a.tile=pickTile(maxTile,C,nbatch*a.q*A,smf,minTile);
   a.tileB=pickTile(maxTile,C,nbatch*B,smb,minTile);
@@ -518,8 +519,9 @@ void Conv::tune()
         if(a.kind == KIND_REAL) {
           sf=sb=FGB_BY_PREC(prec,outerRealSmem,a.L,a.N/2,t);
         } else {
-          sf=FGB_BY_PREC(prec,outerFwdSmem,a.L,a.m,t);
-          sb=FGB_BY_PREC(prec,outerBwdSmem,a.L,a.m,t,(int) a.q);
+          sf=FGB_BY_PREC(prec,outerFwdSmem,a.L,a.m,t,(int) (a.p == 1));
+          sb=FGB_BY_PREC(prec,outerBwdSmem,a.L,a.m,t,(int) a.q,
+                         (int) (a.p == 1));
         }
         if(sf <= SMEM_MAX) f.cands.push_back(t);
         if(sb <= SMEM_MAX) b.cands.push_back(t);
@@ -698,6 +700,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
     P.twX=NULL; P.NX=1;
     P.io64=0;
+    P.inplace=inplaceFFT<T>() && a.kind != KIND_REAL && a.p == 1;
   };
   // Float-float mode: the first launch reads the caller's FP64 arrays and
   // the last one writes them.
@@ -737,6 +740,8 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.twN=(const typename TwT<T>::type *) twiddles(q,I.prec);
     O.twX=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
     O.NX=a.N;
+    O.io64=0;
+    O.inplace=0;
     O.count=A; O.nbatch=1; O.inBatch=O.outBatch=0;
     O.inRow=m; O.outRow=m; O.C=(int) m; O.Ltot=a.L;
     O.scale=(T) 1;
@@ -948,6 +953,7 @@ cudaError_t PadTransform::runT(const void *in, void *out, bool fwd,
   P.fp=fftPlan(a.kind == KIND_REAL ? a.N/2 : a.m,prec);
   P.twN=(const typename TwT<T>::type *) twiddles(a.N,prec);
   P.twX=NULL; P.NX=1;
+  P.io64=0; P.inplace=0;     // the public layout is natural order
   P.count=1; P.nbatch=1; P.inBatch=P.outBatch=0;
   P.inRow=C; P.outRow=C; P.C=(int) C; P.Ltot=(long long) a.L*C;
   P.scale=(T) 1;

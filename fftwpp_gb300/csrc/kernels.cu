@@ -201,14 +201,6 @@ __device__ __forceinline__ void convertStaged(cplx<T> *y, int i)
   }
 }
 
-// The row kernels transform in place (fftDIF/fftDIT, one buffer) on the
-// FP32 pipe; the FP64 form keeps the ping-pong Stockham transform, which
-// measured faster on GB300's FP64 pipe.
-template<typename T> __host__ __device__ constexpr bool inplaceFFT()
-{
-  return !std::is_same<T,double>::value;
-}
-
 // Exponent ((s-c) mod N)*r mod N of a residue twiddle.
 __device__ __forceinline__ int twExp(int s, int c, int r, int N)
 {
@@ -500,6 +492,46 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
   const typename TwT<T>::type *tw=P.twN;
   const float invTile=1.0f/(float) tile;
 
+  if constexpr(inplaceFFT<T>()) {
+    if(P.inplace) {
+      // One term per output (L <= m): fold straight from memory into the
+      // transform buffer, transform in place (digit-reversed j; the row
+      // kernels do not depend on row order and the backward undoes it).
+      // Asynchronous copies straight to each value's slot, then the
+      // conversion and residue twiddle in place by the same thread.
+      for(int i=tid; i < m*tile; i += nthr) {
+        int t=fdiv(i,invTile), cc=i-t*tile;
+        int col=col0+cc;
+        int s=posmod(t+c,m);
+        long long off=(long long) s*P.inRow+col;
+        if(s < L && col < P.C && off < P.Ltot) cpAsync(x+sp(i),src+off);
+        else x[sp(i)]=mk((T) 0,(T) 0);
+      }
+      cpAsyncWait();
+      if(r != 0 || (P.io64 & 1)) {
+        for(int i=tid; i < m*tile; i += nthr) {
+          int t=fdiv(i,invTile), cc=i-t*tile;
+          int col=col0+cc;
+          int s=posmod(t+c,m);
+          long long off=(long long) s*P.inRow+col;
+          if(s < L && col < P.C && off < P.Ltot) {
+            if(P.io64 & 1) convertStaged(x,sp(i));
+            if(r != 0) x[sp(i)]=twmul<1>(x[sp(i)],tw[twExp(s,c,r,N)]);
+          }
+        }
+      }
+      __syncthreads();
+      fftDIF<T,1>(x,P.fp,tile,tile,tid,nthr);
+      for(int i=tid; i < m*tile; i += nthr) {
+        int j=fdiv(i,invTile), cc=i-j*tile;
+        int col=col0+cc;
+        if(col < P.C) dst[((long long) r*m+j)*P.outRow+col]=x[sp(i)];
+      }
+      __syncthreads();
+      return;
+    }
+  }
+
   // Stage the L x tile input block in y with asynchronous copies (many
   // loads in flight per thread instead of one dependent load per output).
   for(int i=tid; i < L*tile; i += nthr) {
@@ -611,7 +643,13 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
       }
       __syncthreads();
     }
-    cplx<T> *X=fftSmem<T,-1>(x,y,P.fp,tile,tile,tid,nthr);
+    cplx<T> *X;
+    if(inplaceFFT<T>() && P.inplace) {
+      fftDIT<T,-1>(x,P.fp,tile,tile,tid,nthr);
+      X=x;
+    } else {
+      X=fftSmem<T,-1>(x,y,P.fp,tile,tile,tid,nthr);
+    }
     if(direct) {
       for(int i=tid; i < L*tile; i += nthr) {
         int s=fdiv(i,invTile), cc=i-s*tile;
@@ -911,15 +949,18 @@ template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc)
   size_t nbuf=inplaceFFT<T>() ? 1 : 2;
   return sizeof(cplx<T>)*nbuf*(size_t) padded(Nh*A*rpc);
 }
-template<typename T> size_t outerFwdSmem(int L, int m, int tile)
+template<typename T> size_t outerFwdSmem(int L, int m, int tile, int inplace)
 {
   size_t pm=padded(m*tile);
+  if(inplaceFFT<T>() && inplace) return sizeof(cplx<T>)*pm;
   return sizeof(cplx<T>)*(pm+std::max(pm,(size_t) L*tile));
 }
-template<typename T> size_t outerBwdSmem(int L, int m, int tile, int q)
+template<typename T> size_t outerBwdSmem(int L, int m, int tile, int q,
+                                         int inplace)
 {
   size_t acc=q == 1 ? 0 : (size_t) L*tile;
-  return sizeof(cplx<T>)*(acc+2*(size_t) padded(m*tile));
+  size_t nbuf=inplaceFFT<T>() && inplace ? 1 : 2;
+  return sizeof(cplx<T>)*(acc+nbuf*(size_t) padded(m*tile));
 }
 template<typename T> size_t outerRealSmem(int L, int Nh, int tile)
 {
@@ -980,7 +1021,7 @@ cudaError_t launchHermRow(const HermRowPlan<T>& P, int threads,
 template<typename T>
 cudaError_t launchOuterFwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
 {
-  size_t sm=outerFwdSmem<T>(P.L,P.m,P.tile);
+  size_t sm=outerFwdSmem<T>(P.L,P.m,P.tile,P.inplace);
   cudaError_t e=setSmem(outerFwdKernel<T>,sm);
   if(e != cudaSuccess) return e;
   dim3 grid((P.C+P.tile-1)/P.tile,P.q,P.nbatch*P.count);
@@ -991,7 +1032,7 @@ cudaError_t launchOuterFwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
 template<typename T>
 cudaError_t launchOuterBwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
 {
-  size_t sm=outerBwdSmem<T>(P.L,P.m,P.tile,P.q);
+  size_t sm=outerBwdSmem<T>(P.L,P.m,P.tile,P.q,P.inplace);
   cudaError_t e=setSmem(outerBwdKernel<T>,sm);
   if(e != cudaSuccess) return e;
   dim3 grid((P.C+P.tile-1)/P.tile,1,P.nbatch*P.count);
@@ -1032,8 +1073,8 @@ cudaError_t launchOuterRealBwd(const OuterPlan<T>& P, int threads,
   template cudaError_t launchOuterRealBwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
   template size_t rowSmem<T>(int,int,int,int,int); \
   template size_t hermRowSmem<T>(int,int,int,int); \
-  template size_t outerFwdSmem<T>(int,int,int); \
-  template size_t outerBwdSmem<T>(int,int,int,int); \
+  template size_t outerFwdSmem<T>(int,int,int,int); \
+  template size_t outerBwdSmem<T>(int,int,int,int,int); \
   template size_t outerRealSmem<T>(int,int,int); \
   template cudaError_t launchBatch<T>(const BatchArgs<T>&,int,int,size_t,cudaStream_t); \
   template int batchBlocksPerSM<T>(int,size_t,int,int,int);

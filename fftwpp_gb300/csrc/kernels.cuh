@@ -25,7 +25,17 @@
 
 #include "fft_smem.cuh"
 
+#include <type_traits>
+
 namespace fgb {
+
+// The row and outer kernels transform in place (fftDIF/fftDIT, one buffer)
+// on the FP32 pipe; the FP64 form keeps the ping-pong Stockham transform,
+// which measured faster on GB300's FP64 pipe.
+template<typename T> __host__ __device__ constexpr bool inplaceFFT()
+{
+  return !std::is_same<T,double>::value;
+}
 
 #define FGB_MAXA 8
 
@@ -84,6 +94,9 @@ struct OuterPlan {
   int L, m, q, N, cshift;
   int tile;
   int io64;                // as RowPlan::io64
+  int inplace;             // FP32-pipe modes with L <= m and no twX: fold
+                           // from memory and transform in place, rows of
+                           // a residue block in digit-reversed order
   T scale;
   FFTPlanDev fp;           // length-m (complex) or length-N/2 (real) FFT
   const typename TwT<T>::type *twN;
@@ -159,10 +172,12 @@ template<typename T> cudaError_t launchOuterRealBwd(const OuterPlan<T>& P,
 // Shared-memory bytes each kernel needs (for plan-time sizing).
 template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc=1);
 template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc=1);
-template<typename T> size_t outerFwdSmem(int L, int m, int tile);
+template<typename T> size_t outerFwdSmem(int L, int m, int tile,
+                                         int inplace=0);
 // q == 1: the backward writes its outputs without an accumulator; q = 0
 // sizes for any residue count.
-template<typename T> size_t outerBwdSmem(int L, int m, int tile, int q=0);
+template<typename T> size_t outerBwdSmem(int L, int m, int tile, int q=0,
+                                         int inplace=0);
 template<typename T> size_t outerRealSmem(int L, int Nh, int tile);
 
 } // namespace fgb
