@@ -27,8 +27,12 @@ using ::fma;
 // The operations are the error-free transformations of Knuth (TwoSum),
 // Dekker (FastTwoSum) and the FMA-based TwoProduct; the addition is the
 // "sloppy" double-word sum, whose error is bounded by 2^-46 (|a| + |b|),
-// which is the normwise bound an FFT needs.  The _rn intrinsics keep the
-// compiler from fusing the error terms into multiply-adds.
+// which is the normwise bound an FFT needs.  Renormalisation is lazy: the
+// arithmetic operators return hi + lo unrenormalised (|lo| may exceed
+// ulp(hi)/2 by a small factor) and the transforms renormalise every value
+// they load (nrm), so a chain of at most one radix stage runs between
+// renormalisations.  The _rn intrinsics keep the compiler from fusing the
+// error terms into multiply-adds.
 struct ff {
   float hi, lo;
   ff() = default;
@@ -52,10 +56,12 @@ __device__ __forceinline__ ff ffFast(float s, float e)
   return ff(t,__fsub_rn(e,__fsub_rn(t,s)));
 }
 
+__device__ __forceinline__ ff nrm(ff a) {return ffFast(a.hi,a.lo);}
+
 __device__ __forceinline__ ff operator+(ff a, ff b)
 {
   ff s=ffTwoSum(a.hi,b.hi);
-  return ffFast(s.hi,__fadd_rn(s.lo,__fadd_rn(a.lo,b.lo)));
+  return ff(s.hi,__fadd_rn(s.lo,__fadd_rn(a.lo,b.lo)));
 }
 __device__ __forceinline__ ff operator-(ff a) {return ff(-a.hi,-a.lo);}
 __device__ __forceinline__ ff operator-(ff a, ff b) {return a+(-b);}
@@ -66,7 +72,7 @@ __device__ __forceinline__ ff operator*(ff a, ff b)
   float e=fmaf(a.hi,b.hi,-p);
   e=fmaf(a.hi,b.lo,e);
   e=fmaf(a.lo,b.hi,e);
-  return ffFast(p,e);
+  return ff(p,e);
 }
 
 // a*b + c.
@@ -78,7 +84,7 @@ __device__ __forceinline__ ff fma(ff a, ff b, ff c)
   float l=__fadd_rn(__fadd_rn(s.lo,e),c.lo);
   l=fmaf(a.hi,b.lo,l);
   l=fmaf(a.lo,b.hi,l);
-  return ffFast(s.hi,l);
+  return ff(s.hi,l);
 }
 
 // a*b + c*d with one renormalisation (complex multiplies).
@@ -94,7 +100,7 @@ __device__ __forceinline__ ff ffDot2(ff a, ff b, ff c, ff d)
   l=fmaf(a.lo,b.hi,l);
   l=fmaf(c.hi,d.lo,l);
   l=fmaf(c.lo,d.hi,l);
-  return ffFast(s.hi,l);
+  return ff(s.hi,l);
 }
 
 template<typename T> struct cplx { T x, y; };
@@ -140,6 +146,14 @@ __device__ __forceinline__ cplx<ff> cmulconj(cplx<ff> a, cplx<ff> b)
 
 template<typename T>
 __device__ __forceinline__ cplx<T> conjg(cplx<T> a) { return mk(a.x,-a.y); }
+
+// Renormalise a loaded value (float-float only).
+template<typename T>
+__device__ __forceinline__ cplx<T> nrm(cplx<T> a) { return a; }
+__device__ __forceinline__ cplx<ff> nrm(cplx<ff> a)
+{
+  return mk(nrm(a.x),nrm(a.y));
+}
 
 // s*i*a for s = +1 or -1 (compile time).
 template<int S, typename T>

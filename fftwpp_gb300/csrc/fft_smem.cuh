@@ -185,7 +185,7 @@ __device__ __forceinline__ void fftStage(const cplx<T> *__restrict__ x,
     int k=j-fdiv(j,invNs)*Ns;
     cplx<T> a[R];
 #pragma unroll
-    for(int r=0; r < R; ++r) a[r]=x[sp((j+r*nR)*ld+c)];
+    for(int r=0; r < R; ++r) a[r]=nrm(x[sp((j+r*nR)*ld+c)]);
     // Uniform per stage: the first stage has no twiddles; later stages apply
     // them to every element (W^0 = 1 exactly, so k = 0 needs no branch).
     if(Ns > 1) {
@@ -257,7 +257,7 @@ __device__ __forceinline__ void ipStage(cplx<T> *__restrict__ x, int n, int Ls,
     int base=b*Ls+j;
     cplx<T> a[R];
 #pragma unroll
-    for(int r=0; r < R; ++r) a[r]=x[sp((base+r*m)*ld+c)];
+    for(int r=0; r < R; ++r) a[r]=nrm(x[sp((base+r*m)*ld+c)]);
     if(!DIF && m > 1) {
 #pragma unroll
       for(int r=1; r < R; ++r) a[r]=twmul<S>(a[r],tw[r*j*tstride]);

@@ -88,13 +88,13 @@ __device__ __forceinline__ void multiplySlot(cplx<T> *X, int base, int stride,
     constexpr int KA=MultArity<K>::A, KB=MultArity<K>::B;
     cplx<T> v[KA];
 #pragma unroll
-    for(int a=0; a < KA; ++a) v[a]=X[sp(base+a*stride)];
+    for(int a=0; a < KA; ++a) v[a]=nrm(X[sp(base+a*stride)]);
     applyMult(K,v,KA);
 #pragma unroll
     for(int b=0; b < KB; ++b) X[sp(base+b*stride)]=v[b];
   } else {
     cplx<T> v[FGB_MAXA];
-    for(int a=0; a < A; ++a) v[a]=X[sp(base+a*stride)];
+    for(int a=0; a < A; ++a) v[a]=nrm(X[sp(base+a*stride)]);
     applyMult(kind,v,A);
     for(int b=0; b < B; ++b) X[sp(base+b*stride)]=v[b];
   }
