@@ -135,15 +135,35 @@ __device__ __forceinline__ ff toFF(double x)
   unsigned sign=(unsigned) (b >> 32) & 0x80000000u;
   float hi=__uint_as_float(sign | ((unsigned) (e+127) << 23) |
                            (unsigned) ((b >> 29) & 0x7fffffu));
-  float lo=__uint2float_rn((unsigned) (b & 0x1fffffffull));    // < 2^29
+  // The remaining 29 significand bits R as a float without an integer
+  // conversion: R = 64 Ra + Rb, each part exact through the 2^23 bias,
+  // rounded once by the multiply-add.
+  unsigned R=(unsigned) (b & 0x1fffffffull);
+  float ra=__fsub_rn(__uint_as_float(0x4b000000u | (R >> 6)),8388608.0f);
+  float rb=__fsub_rn(__uint_as_float(0x4b000000u | (R & 63u)),8388608.0f);
+  float lo=fmaf(ra,64.0f,rb);
   lo=__fmul_rn(lo,__uint_as_float((unsigned) (e-52+127) << 23)); // * 2^(e-52)
   lo=__uint_as_float(__float_as_uint(lo) | sign);
   return ffFast(hi,lo);
 }
 
+// A float widened to double exactly by moving its fields (the FP64 pipe
+// only for subnormals, infinities and NaNs).
+__device__ __forceinline__ double widen(float f)
+{
+  unsigned u=__float_as_uint(f);
+  unsigned ef=(u >> 23) & 0xffu;
+  unsigned long long sign=(unsigned long long) (u & 0x80000000u) << 32;
+  if((u & 0x7fffffffu) == 0) return __longlong_as_double((long long) sign);
+  if(ef == 0 || ef == 255) return (double) f;
+  return __longlong_as_double((long long) (sign |
+    ((unsigned long long) (ef+896) << 52) |
+    ((unsigned long long) (u & 0x7fffffu) << 29)));
+}
+
 __device__ __forceinline__ double fromFF(ff v)
 {
-  return (double) v.hi+(double) v.lo;
+  return widen(v.hi)+widen(v.lo);
 }
 
 template<typename T>
