@@ -498,26 +498,30 @@ def run_ours(args, w):
     # Compute roofline of the FP64 kernels: FP64 instructions per launch
     # (ncu, committed under profiles/) over the live launch time, against
     # the DFMA issue rate measured on this GPU.
+    # The FP64 kernels against the DFMA issue rate (FP64 instructions per
+    # launch, DPINST); the float-float and FP32 kernels against the FFMA
+    # issue rate (FP32 instructions per launch, SPINST).  Both counts come
+    # from the committed ncu summaries, the rates from fgb_measure_fma_rate.
     compute = None
     dfma, ffma = measured_fma_rates()
-    if prec == "f64" and dfma:
-        dp = [profile_figure("DPINST", args.workload, n, prec) for n in names]
-        if dp[dom]:
-            total_dp = sum(x for x in dp if x) if all(dp) else None
-            compute = {
-                "bound": "fp64_issue", "kernel": names[dom],
-                "achieved": dp[dom] / (per_launch[dom] * 1e-3),
-                "peak": dfma, "unit": "FP64 inst/s",
-                "frac": dp[dom] / (per_launch[dom] * 1e-3) / dfma,
-                "whole_step_frac": (total_dp / (total_ms / args.steps * 1e-3)
-                                    / dfma) if total_dp else None,
-                "fp64_tflops_peak_measured": 2 * dfma / 1e12,
-                "fp32_tflops_peak_measured": 2 * ffma / 1e12,
-                "source": "DP instructions per launch from ncu "
-                          "(profiles/), peak from fgb_measure_fma_rate"}
-    elif dfma:
+    tag, rate, bound = (("DPINST", dfma, "fp64_issue") if prec == "f64" else
+                        ("SPINST", ffma, "fp32_issue"))
+    if rate:
+        cnt = [profile_figure(tag, args.workload, n, prec) for n in names]
         compute = {"fp64_tflops_peak_measured": 2 * dfma / 1e12,
                    "fp32_tflops_peak_measured": 2 * ffma / 1e12}
+        if cnt[dom]:
+            total = sum(cnt) if all(cnt) else None
+            compute.update({
+                "bound": bound, "kernel": names[dom],
+                "achieved": cnt[dom] / (per_launch[dom] * 1e-3),
+                "peak": rate,
+                "unit": ("FP64" if tag == "DPINST" else "FP32") + " inst/s",
+                "frac": cnt[dom] / (per_launch[dom] * 1e-3) / rate,
+                "whole_step_frac": (total / (total_ms / args.steps * 1e-3)
+                                    / rate) if total else None,
+                "source": f"{tag} lines (instructions per launch, ncu) "
+                          "under profiles/, peak from fgb_measure_fma_rate"})
 
     # Accuracy at full size against the CPU oracle (FP64 restatement), or,
     # for the 256^3 workload, against FP64 direct sums at sampled outputs.
