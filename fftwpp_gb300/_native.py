@@ -92,6 +92,8 @@ def load():
     lib.fgb_pad_destroy.argtypes = [vp]
     lib.fgb_set_autotune.restype = None
     lib.fgb_set_autotune.argtypes = [ctypes.c_int]
+    lib.fgb_set_zero_copy.restype = None
+    lib.fgb_set_zero_copy.argtypes = [ctypes.c_int]
     lib.fgb_destroy.restype = None
     lib.fgb_destroy.argtypes = [vp]
     lib.fgb_last_error.restype = ctypes.c_char_p

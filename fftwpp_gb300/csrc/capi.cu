@@ -653,6 +653,7 @@ int fgb_info(const fgb_conv *c, long *info)
 }
 
 void fgb_set_autotune(int on) {Conv::setAutotune(on != 0);}
+void fgb_set_zero_copy(int on) {Conv::setZeroCopy(on != 0);}
 
 int fgb_set_normalize(fgb_conv *c, int normalize)
 {

@@ -893,11 +893,75 @@ cudaError_t Conv::run(const void *const *in, void *const *out, cudaStream_t s)
   return runT<ff>(in,out,s);        // float-float, FP64 at the interface
 }
 
+bool Conv::zeroCopy=true;
+void Conv::setZeroCopy(bool on) {zeroCopy=on;}
+
+// The device address of page-locked host memory, or NULL for memory the GPU
+// cannot address directly.
+static void *mappedAddress(const void *p)
+{
+  cudaPointerAttributes at;
+  if(cudaPointerGetAttributes(&at,p) != cudaSuccess) {
+    cudaGetLastError();
+    return NULL;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : NULL;
+}
+
+// Whether the first and last kernels touch the caller's arrays in runs of at
+// least 64 contiguous bytes (then they may read and write host memory
+// directly without wasting the link's lines).
+bool Conv::directSegments() const
+{
+  const AxisPlan& a=I.axis[0];
+  if(I.dim == 1 && !I.longRow) return true;        // whole rows
+  size_t e=elemBytes();
+  return (size_t) a.tile*e >= 64 && (size_t) a.tileB*e >= 64;
+}
+
 cudaError_t Conv::runHost(const void *const *in, void *const *out,
                           cudaStream_t s)
 {
   size_t bytes=elements()*elemBytes();
   int A=I.A, B=I.B;
+  if(zeroCopy) {
+    // Page-locked arrays: the first kernel reads them and the last one
+    // writes them in place over the host link (NVLink-C2C on Grace), so
+    // the transfers overlap the transforms instead of preceding them.
+    std::vector<const void *> min(A);
+    std::vector<void *> mout(B);
+    bool ok=true;
+    for(int a=0; a < A && ok; ++a) ok=(min[a]=mappedAddress(in[a])) != NULL;
+    for(int b=0; b < B && ok; ++b) ok=(mout[b]=mappedAddress(out[b])) != NULL;
+    if(ok && directSegments()) {
+      cudaError_t e=run(min.data(),mout.data(),s);
+      if(e != cudaSuccess) return e;
+      return cudaStreamSynchronize(s);
+    }
+    if(ok && bytes % 16 == 0) {
+      // Narrow column segments would waste the link's lines: move the
+      // arrays whole with the SMs and convolve in device memory.
+      if(!hostIn &&
+         cudaMalloc(&hostIn,bytes*A) != cudaSuccess) return cudaErrorMemoryAllocation;
+      std::vector<void *> din(A);
+      CopyArgs C;
+      C.count=A; C.bytes=bytes;
+      for(int a=0; a < A; ++a) {
+        din[a]=(char *) hostIn+a*bytes;
+        C.src[a]=min[a];
+        C.dst[a]=din[a];
+      }
+      cudaError_t e=launchBulkCopy(C,s);
+      if(e != cudaSuccess) return e;
+      e=run(din.data(),din.data(),s);
+      if(e != cudaSuccess) return e;
+      C.count=B;
+      for(int b=0; b < B; ++b) {C.src[b]=din[b]; C.dst[b]=mout[b];}
+      e=launchBulkCopy(C,s);
+      if(e != cudaSuccess) return e;
+      return cudaStreamSynchronize(s);
+    }
+  }
   if(!hostIn) {
     if(cudaMalloc(&hostIn,bytes*A) != cudaSuccess) return cudaErrorMemoryAllocation;
   }

@@ -59,9 +59,12 @@ public:
   // problems back to back in every array.
   cudaError_t run(const void *const *in, void *const *out, cudaStream_t s);
 
-  // Host pointers: copy in, run, copy out (synchronous on s).
+  // Host pointers (synchronous on s).  Page-locked arrays are read and
+  // written by the kernels in place (zero copy) unless disabled
+  // process-wide; other host memory is copied in and out.
   cudaError_t runHost(const void *const *in, void *const *out,
                       cudaStream_t s);
+  static void setZeroCopy(bool on);
 
   const ConvInfo& info() const {return I;}
   size_t elemBytes() const;        // bytes per stored element
@@ -96,6 +99,7 @@ private:
   bool timing;
   bool normalize;
   static bool autotune;
+  static bool zeroCopy;
   std::vector<cudaEvent_t> events;
   int marks;
   void tick(cudaStream_t s);
@@ -103,6 +107,7 @@ private:
                                         void *const *out, cudaStream_t s);
   void allocate();
   void tune();
+  bool directSegments() const;
 };
 
 // Twiddle table W_n^t = exp(2 pi i t/n), t < n, on the current device,

@@ -1099,6 +1099,39 @@ cudaError_t launchOuterRealBwd(const OuterPlan<T>& P, int threads,
   template cudaError_t launchBatch<T>(const BatchArgs<T>&,int,int,size_t,cudaStream_t); \
   template int batchBlocksPerSM<T>(int,size_t,int,int,int);
 
+#if !defined(FGB_ONLY_FLOAT) && !defined(FGB_ONLY_FF)
+// Bulk copy by the SMs (16-byte vectors, four in flight per thread): between
+// page-locked host memory and the device it reads and writes whole lines
+// over the host link.
+__global__ void __launch_bounds__(256) bulkCopyKernel(CopyArgs P)
+{
+  const size_t n=P.bytes/16;
+  const size_t stride=(size_t) gridDim.x*blockDim.x;
+  for(int a=0; a < P.count; ++a) {
+    const uint4 *src=(const uint4 *) P.src[a];
+    uint4 *dst=(uint4 *) P.dst[a];
+    size_t i=blockIdx.x*(size_t) blockDim.x+threadIdx.x;
+    for(; i+3*stride < n; i += 4*stride) {
+      uint4 v0=src[i], v1=src[i+stride], v2=src[i+2*stride],
+        v3=src[i+3*stride];
+      dst[i]=v0; dst[i+stride]=v1; dst[i+2*stride]=v2; dst[i+3*stride]=v3;
+    }
+    for(; i < n; i += stride) dst[i]=src[i];
+  }
+}
+
+cudaError_t launchBulkCopy(const CopyArgs& P, cudaStream_t s)
+{
+  if(P.bytes % 16) return cudaErrorInvalidValue;
+  for(int a=0; a < P.count; ++a)
+    if(((size_t) P.src[a] | (size_t) P.dst[a]) % 16)
+      return cudaErrorInvalidValue;
+  if(P.bytes == 0 || P.count == 0) return cudaSuccess;
+  bulkCopyKernel<<<152*8,256,0,s>>>(P);
+  return cudaGetLastError();
+}
+#endif
+
 // Each precision may be compiled as its own translation unit (build.py
 // compiles this file once per precision, in parallel): FGB_ONLY_<P> keeps
 // one of DOUBLE, FLOAT and FF.

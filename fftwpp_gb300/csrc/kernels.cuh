@@ -169,6 +169,16 @@ template<typename T> cudaError_t launchOuterRealBwd(const OuterPlan<T>& P,
                                                     int threads,
                                                     cudaStream_t s);
 
+// Copy `count` arrays of `bytes` bytes each (16-byte aligned, a multiple of
+// 16) with the SMs.
+struct CopyArgs {
+  const void *src[FGB_MAXA];
+  void *dst[FGB_MAXA];
+  int count;
+  size_t bytes;
+};
+cudaError_t launchBulkCopy(const CopyArgs& P, cudaStream_t s);
+
 // Shared-memory bytes each kernel needs (for plan-time sizing).
 template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc=1);
 template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc=1);

@@ -62,8 +62,16 @@ fgb_conv *fgb_create(int dim, const int *kinds, const size_t *L,
 int fgb_convolve_device(fgb_conv *c, void *const *in, void *const *out,
                         void *stream);
 
-/* Same on host arrays: copies in, runs, copies out, synchronises. */
+/* Same on host arrays, synchronous.  Page-locked arrays (create_*Align,
+ * cudaHostAlloc) are read by the first kernel and written by the last one
+ * directly over the host link (zero copy: on Grace the NVLink-C2C
+ * transfers overlap the transforms); other host memory is copied in and
+ * out.  This is also the path of the FFTW++-compatible convolve calls. */
 int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out);
+
+/* Process-wide switch of the zero-copy host path (default on); 0 always
+ * copies page-locked arrays in and out as well. */
+void fgb_set_zero_copy(int on);
 
 /* Plan parameters: for each axis d, info[8d..8d+7] = m, p, q, N, stored
  * length, centred offset, outer tile, rows produced.  info[24] = kernels per

@@ -205,3 +205,35 @@ def test_autotune_changes_schedule_only(native_lib, precision):
         native_lib.fgb_set_autotune(1)
     tuned, c1 = run_gpu(kinds, L, M, fs, "binary", precision)
     assert np.array_equal(plain[0], tuned[0])
+
+
+@pytest.mark.parametrize("precision", ["f64", "ff", "f32"])
+@pytest.mark.parametrize("case", [
+    ([H.CENTERED, H.HERMITIAN], [31, 31], [46, 46], "realbinary"),
+    ([H.PAD], [300], [599], "binary"),
+    ([H.REAL, H.PAD, H.PAD], [12, 10, 9], [23, 19, 17], "binary")])
+def test_zero_copy_host_path(native_lib, precision, case):
+    """Page-locked host arrays are read and written by the kernels in place
+    over the host link; the result equals the copying path bit for bit."""
+    import torch
+    from fftwpp_gb300.gpu import HybridConvolution
+    kinds, L, M, mult = case
+    fs = _inputs(kinds, L, 2, seed=23)
+    want = H.convolve(fs, kinds, L, M, mult=mult)[0]
+    conv = HybridConvolution(kinds, L, M, mult=mult, precision=precision)
+    tdt = conv.dtype
+
+    def pinned():
+        return [torch.from_numpy(np.ascontiguousarray(f)).to(tdt).pin_memory()
+                .numpy() for f in fs]
+    zc = pinned()
+    conv.convolve_host(*zc)
+    assert rel_l2(zc[0], want) <= TOL[precision]
+    try:
+        native_lib.fgb_set_zero_copy(0)
+        cp = pinned()
+        conv.convolve_host(*cp)
+    finally:
+        native_lib.fgb_set_zero_copy(1)
+    assert np.array_equal(zc[0], cp[0])
+    assert np.array_equal(zc[1], cp[1])      # the second input is untouched
