@@ -90,6 +90,13 @@ def load():
     lib.fgb_pad_index.argtypes = [vp, sz, sz]
     lib.fgb_pad_destroy.restype = None
     lib.fgb_pad_destroy.argtypes = [vp]
+    lib.fgb_fft_create.restype = vp
+    lib.fgb_fft_create.argtypes = [ctypes.c_int, sz, ctypes.c_int, sz, sz, sz,
+                                   sz, sz, sz, ctypes.c_int]
+    lib.fgb_fft_execute_device.restype = ctypes.c_int
+    lib.fgb_fft_execute_device.argtypes = [vp, vp, vp, vp]
+    lib.fgb_fft_destroy.restype = None
+    lib.fgb_fft_destroy.argtypes = [vp]
     lib.fgb_set_autotune.restype = None
     lib.fgb_set_autotune.argtypes = [ctypes.c_int]
     lib.fgb_set_zero_copy.restype = None

@@ -64,7 +64,9 @@ class _Jacobian(torch.autograd.Function):
 
 class AdvectionJacobian:
     """J(psi, omega) on Lx x ceil(Ly/2) centred-Hermitian modes with the
-    2/3-rule padding M = 3 ceil(L/2) - 2 (L mod 2) on both axes."""
+    2/3-rule padding M = 3 ceil(L/2) - 2 (L mod 2) on both axes.
+    precision: "f64", "ff" (FP64 tensors, float-float arithmetic) or
+    "f32"."""
 
     def __init__(self, Lx: int, Ly: int, precision: str = "f64"):
         self.Lx, self.Ly = Lx, Ly
@@ -81,9 +83,11 @@ class AdvectionJacobian:
     def scale_columns(self, t, s0, s1):
         rows, cols = t.shape
         s = torch.cuda.current_stream()
+        # The float-float mode keeps FP64 data: scale it as FP64.
+        data = _native.F32 if self.fwd.prec == _native.F32 else _native.F64
         rc = self.lib.fgb_scale_columns_device(
             rows, cols, s0, s1, ctypes.c_void_p(t.data_ptr()),
-            self.fwd.prec, ctypes.c_void_p(s.cuda_stream))
+            data, ctypes.c_void_p(s.cuda_stream))
         if rc != 0:
             raise RuntimeError(_native.last_error())
 

@@ -20,6 +20,11 @@ struct fgb_pad {
   std::unique_ptr<PadTransform> t;
 };
 
+struct fgb_fft {
+  std::unique_ptr<PlainFFT> t;
+  bool inplaceOK;
+};
+
 struct fgb_conv {
   std::unique_ptr<Conv> conv;
   cudaStream_t stream;
@@ -799,6 +804,46 @@ size_t fgb_pad_index(const fgb_pad *h, size_t r, size_t j)
 }
 
 void fgb_pad_destroy(fgb_pad *h) {delete h;}
+
+// Plain FFTs (engine.h, class PlainFFT).
+fgb_fft *fgb_fft_create(int kind, size_t n, int sign, size_t C, size_t B,
+                        size_t istride, size_t ibatch, size_t ostride,
+                        size_t obatch, int precision)
+{
+  try {
+    fgb_fft *h=new fgb_fft;
+    h->t.reset(new PlainFFT(kind,(long) n,sign,(long) C,(long) B,
+                            (long) istride,(long) ibatch,(long) ostride,
+                            (long) obatch,precision));
+    // Interleaved real transforms read and write columns of different
+    // widths, so other CTAs' columns would overlap in place.
+    h->inplaceOK=kind == FFT_C2C || C == 1;
+    return h;
+  } catch(std::exception& e) {
+    report("fgb_fft_create",e.what());
+    return NULL;
+  }
+}
+
+int fgb_fft_execute_device(fgb_fft *h, const void *in, void *out,
+                           void *stream)
+{
+  if(!h || !in || !out) {report("fgb_fft_execute_device","null argument");
+    return -1;}
+  if(in == out && !h->inplaceOK) {
+    report("fgb_fft_execute_device","interleaved real transforms must be "
+           "out of place");
+    return -1;
+  }
+  cudaError_t e=h->t->execute(in,out,(cudaStream_t) stream);
+  if(e != cudaSuccess) {
+    report("fgb_fft_execute_device",cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
+void fgb_fft_destroy(fgb_fft *h) {delete h;}
 
 const char *fgb_last_error(void)
 {

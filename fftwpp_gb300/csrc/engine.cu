@@ -701,6 +701,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.twX=NULL; P.NX=1;
     P.io64=0;
     P.inplace=inplaceFFT<T>() && a.kind != KIND_REAL && a.p == 1;
+    P.conj=0;
   };
   // Float-float mode: the first launch reads the caller's FP64 arrays and
   // the last one writes them.
@@ -742,6 +743,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.NX=a.N;
     O.io64=0;
     O.inplace=0;
+    O.conj=0;
     O.count=A; O.nbatch=1; O.inBatch=O.outBatch=0;
     O.inRow=m; O.outRow=m; O.C=(int) m; O.Ltot=a.L;
     O.scale=(T) 1;
@@ -1018,6 +1020,7 @@ cudaError_t PadTransform::runT(const void *in, void *out, bool fwd,
   P.twN=(const typename TwT<T>::type *) twiddles(a.N,prec);
   P.twX=NULL; P.NX=1;
   P.io64=0; P.inplace=0;     // the public layout is natural order
+  P.conj=0;
   P.count=1; P.nbatch=1; P.inBatch=P.outBatch=0;
   P.inRow=C; P.outRow=C; P.C=(int) C; P.Ltot=(long long) a.L*C;
   P.scale=(T) 1;
@@ -1040,6 +1043,80 @@ cudaError_t PadTransform::backward(const void *F, void *f, cudaStream_t s)
 {
   return prec == PREC_F64 ? runT<double>(F,f,false,s) :
     runT<float>(F,f,false,s);
+}
+
+// ---------------------------------------------------------------------------
+// Plain FFTs (engine.h).
+
+PlainFFT::PlainFFT(int kind, long n, int sign, long C, long B, long istride,
+                   long ibatch, long ostride, long obatch, int prec)
+  : kind(kind), sign(sign), prec(prec), n(n), C(C), B(B), istride(istride),
+    ibatch(ibatch), ostride(ostride), obatch(obatch), tile(1)
+{
+  if(kind != FFT_C2C && kind != FFT_R2C && kind != FFT_C2R)
+    throw std::runtime_error("unknown transform kind");
+  if(prec != PREC_F64 && prec != PREC_F32)
+    throw std::runtime_error("plain FFTs run in FP64 or FP32");
+  if(sign != 1 && sign != -1) throw std::runtime_error("sign must be +1 or -1");
+  if(n < 1 || C < 1 || B < 1 || istride < 1 || ostride < 1 ||
+     (B > 1 && (ibatch < 1 || obatch < 1)))
+    throw std::runtime_error("sizes and strides must be positive");
+  if(C > 1 && (istride < C || ostride < C))
+    throw std::runtime_error("interleaved sequences need stride >= C");
+  if(C > INT_MAX || B > INT_MAX)
+    throw std::runtime_error("too many sequences");
+  if(!smooth(n))
+    throw std::runtime_error("length "+std::to_string(n)+
+                             " is not a product of 2, 3, 5 and 7");
+  if(kind != FFT_C2C && n % 2)
+    throw std::runtime_error("real transforms need an even length");
+  int maxTile=wide(prec) ? 8 : 16;
+  auto sm=[&](int t) -> size_t {
+    if(kind == FFT_C2C)
+      return std::max(FGB_BY_PREC(prec,outerFwdSmem,n,n,t,0),
+                      FGB_BY_PREC(prec,outerBwdSmem,n,n,t,1,0));
+    return FGB_BY_PREC(prec,outerRealSmem,n,n/2,t);
+  };
+  if(sm(1) > SMEM_MAX)
+    throw std::runtime_error("length "+std::to_string(n)+
+                             " is too long for one CTA's shared memory");
+  tile=C > 1 ? pickTile(maxTile,C,B,sm) : 1;
+}
+
+template<typename T>
+cudaError_t PlainFFT::runT(const void *in, void *out, cudaStream_t s)
+{
+  typedef cplx<T> Cx;
+  OuterPlan<T> P;
+  const bool real=kind != FFT_C2C;
+  P.L=(int) n; P.m=(int) n; P.q=1; P.N=(int) n; P.cshift=0;
+  P.tile=tile;
+  P.fp=fftPlan(real ? n/2 : n,prec);
+  P.twN=(const typename TwT<T>::type *) twiddles(n,prec);
+  P.twX=NULL; P.NX=1;
+  P.io64=0; P.inplace=0;
+  // The real kernels compute the sign +1 r2c and sign -1 c2r; FFTW's r2c
+  // (-1) and c2r (+1) are their conjugates on the complex side.
+  P.conj=real ? 1 : 0;
+  P.count=1;
+  P.C=(int) C;
+  P.nbatch=(int) B;
+  P.inRow=istride; P.outRow=ostride;
+  P.inBatch=ibatch; P.outBatch=obatch;
+  P.Ltot=LLONG_MAX;
+  P.scale=(T) 1;
+  P.in[0]=(const Cx *) in;
+  P.out[0]=(Cx *) out;
+  const int threads=256;
+  if(kind == FFT_R2C) return launchOuterRealFwd<T>(P,threads,s);
+  if(kind == FFT_C2R) return launchOuterRealBwd<T>(P,threads,s);
+  return sign > 0 ? launchOuterFwd<T>(P,threads,s) :
+    launchOuterBwd<T>(P,threads,s);
+}
+
+cudaError_t PlainFFT::execute(const void *in, void *out, cudaStream_t s)
+{
+  return prec == PREC_F64 ? runT<double>(in,out,s) : runT<float>(in,out,s);
 }
 
 } // namespace fgb

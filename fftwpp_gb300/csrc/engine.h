@@ -144,6 +144,31 @@ private:
                                         cudaStream_t s);
 };
 
+// Plain unnormalised FFTs of length n, the fft1d / mfft1d / rcfft1d /
+// mrcfft1d / crfft1d / mcrfft1d classes of fftw++.h (fftw++.h:556-1197; the
+// 2D and 3D classes compose passes of these), on the shared-memory radix
+// kernels of the convolutions.  C interleaved sequences in each of B
+// batches: element s of sequence c in batch b is at b*batch + s*stride + c,
+// counted in the element type of each side (real values on the real side
+// of r2c/c2r).  Signs follow FFTW: c2c either, r2c -1, c2r +1.  n is a
+// product of 2, 3, 5 and 7 (even for real transforms) that fits one CTA's
+// shared memory.
+enum FFTKind {FFT_C2C=0, FFT_R2C=1, FFT_C2R=2};
+
+class PlainFFT {
+public:
+  PlainFFT(int kind, long n, int sign, long C, long B, long istride,
+           long ibatch, long ostride, long obatch, int prec);
+  cudaError_t execute(const void *in, void *out, cudaStream_t s);
+  int columnsPerCTA() const {return tile;}
+private:
+  int kind, sign, prec;
+  long n, C, B, istride, ibatch, ostride, obatch;
+  int tile;
+  template<typename T> cudaError_t runT(const void *in, void *out,
+                                        cudaStream_t s);
+};
+
 const void *twiddles(long n, int prec);
 
 std::string lastError();

@@ -756,7 +756,7 @@ outerRealFwdKernel(const OuterPlan<T> P)
     cplx<T> v;
     if(k == Nh) v=e-o;
     else v=e+twmul<1>(o,tw[k]);
-    dst[(long long) k*P.outRow+col]=v;
+    dst[(long long) k*P.outRow+col]=P.conj ? conjg(v) : v;
   }
 }
 
@@ -786,8 +786,12 @@ outerRealBwdKernel(const OuterPlan<T> P)
     cplx<T> v=mk((T) 0,(T) 0);
     if(col < P.C) {
       cplx<T> gk=src[(long long) k*P.inRow+col];
-      if(k == 0) gk.y=(T) 0;
       cplx<T> gm=src[(long long) (Nh-k)*P.inRow+col];
+      if(P.conj) {
+        gk=conjg(gk);
+        gm=conjg(gm);
+      }
+      if(k == 0) gk.y=(T) 0;
       if(k == 0) gm.y=(T) 0;
       gm=conjg(gm);
       cplx<T> s=gk+gm;

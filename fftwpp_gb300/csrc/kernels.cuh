@@ -97,6 +97,8 @@ struct OuterPlan {
   int inplace;             // FP32-pipe modes with L <= m and no twX: fold
                            // from memory and transform in place, rows of
                            // a residue block in digit-reversed order
+  int conj;                // real kernels: conjugate the complex side
+                           // (the sign -1 r2c / sign +1 c2r of plain FFTs)
   T scale;
   FFTPlanDev fp;           // length-m (complex) or length-N/2 (real) FFT
   const typename TwT<T>::type *twN;

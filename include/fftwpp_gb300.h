@@ -158,6 +158,28 @@ int fgb_pad_info(const fgb_pad *t, long *info);
 size_t fgb_pad_index(const fgb_pad *t, size_t r, size_t j);
 void fgb_pad_destroy(fgb_pad *t);
 
+/* Plain unnormalised FFTs on the same shared-memory radix kernels: the
+ * fft1d / mfft1d (FGB_FFT_C2C, sign +1 or -1), rcfft1d / mrcfft1d
+ * (FGB_FFT_R2C, n reals -> n/2+1 complex, sign -1) and crfft1d / mcrfft1d
+ * (FGB_FFT_C2R, sign +1) classes of fftw++.h:556-1197; the 2D and 3D
+ * classes (fftw++.h:1199-1585) are passes of these (fftwpp_gb300/fft.py).
+ * C interleaved sequences in each of B batches: element s of sequence c in
+ * batch b at b*batch + s*stride + c, counted in the element type of each
+ * side (stride >= C when C > 1).  n: a product of 2, 3, 5, 7 (even for
+ * real transforms) within one CTA's shared memory.  Complex transforms may
+ * run in place, real ones only with C == 1.  Device pointers, asynchronous
+ * on stream.  No normalisation (fftNormalized divides by n). */
+#define FGB_FFT_C2C 0
+#define FGB_FFT_R2C 1
+#define FGB_FFT_C2R 2
+typedef struct fgb_fft fgb_fft;
+fgb_fft *fgb_fft_create(int kind, size_t n, int sign, size_t C, size_t B,
+                        size_t istride, size_t ibatch, size_t ostride,
+                        size_t obatch, int precision);
+int fgb_fft_execute_device(fgb_fft *t, const void *in, void *out,
+                           void *stream);
+void fgb_fft_destroy(fgb_fft *t);
+
 /* Text of the last error on this thread. */
 const char *fgb_last_error(void);
 

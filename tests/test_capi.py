@@ -145,3 +145,26 @@ def test_padded_transform_plans(native_lib):
     assert "fftPadReal" in _native.last_error()
     assert not lib.fgb_pad_create(0, 16, 8, 1, 0, 0)
     assert "greater than M" in _native.last_error()
+
+
+def test_plain_fft_plans(native_lib):
+    """Plain FFT plans are validated on the host (no GPU needed)."""
+    from fftwpp_gb300 import _native
+    lib = native_lib
+    ok = lib.fgb_fft_create(0, 768, -1, 4, 3, 4, 3072, 4, 3072, 0)
+    assert ok
+    lib.fgb_fft_destroy(ok)
+    for args, msg in [((0, 11, -1, 1, 1, 1, 11, 1, 11, 0), "product of 2"),
+                      ((1, 30, -1, 1, 1, 1, 30, 1, 16, 0), None),
+                      ((1, 15, -1, 1, 1, 1, 15, 1, 8, 0), "even length"),
+                      ((0, 16, 2, 1, 1, 1, 16, 1, 16, 0), "sign"),
+                      ((0, 16, 1, 8, 1, 4, 0, 8, 0, 0), "stride >= C"),
+                      ((0, 16, 1, 1, 1, 1, 16, 1, 16, 2), "FP64 or FP32"),
+                      ((0, 1 << 16, 1, 1, 1, 1, 1, 1, 1, 0), "too long")]:
+        h = lib.fgb_fft_create(*args)
+        if msg is None:
+            assert h
+            lib.fgb_fft_destroy(h)
+        else:
+            assert not h
+            assert msg in _native.last_error(), _native.last_error()

@@ -136,3 +136,23 @@ def test_fp32_gradient_close_to_fp64(native_lib):
                        for g in torch.autograd.grad(loss, (psi, omega))]
     for g32, g64 in zip(grads["f32"], grads["f64"]):
         assert rel_l2(g32, g64) <= 1e-5
+
+
+def test_float_float_gradient_matches_fp64(native_lib):
+    """The float-float mode (FP64 tensors, hi+lo float arithmetic) gives the
+    FP64 gradient to FP64-grade accuracy."""
+    import torch
+    from fftwpp_gb300.autograd import AdvectionJacobian
+    Lx = Ly = 63
+    grads = {}
+    for prec in ("f64", "ff"):
+        op = AdvectionJacobian(Lx, Ly, prec)
+        assert op.dtype == torch.complex128
+        psi, omega = spectra(Lx, Ly, 6, torch.complex128)
+        psi.requires_grad_(True)
+        omega.requires_grad_(True)
+        loss = _loss(op, psi, omega)
+        grads[prec] = [g.detach().cpu().numpy()
+                       for g in torch.autograd.grad(loss, (psi, omega))]
+    for gff, g64 in zip(grads["ff"], grads["f64"]):
+        assert rel_l2(gff, g64) <= 1e-12
