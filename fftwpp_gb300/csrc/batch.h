@@ -34,6 +34,9 @@ public:
   long totalLength() const {return total;}
   int shortProblems() const {return nsmall;}
   int longProblems() const {return nlong;}
+  int precision() const {return prec;}
+  int inputs() const {return A;}
+  int outputs() const {return B;}
 
   static std::vector<long> candidates(long L, long M, int A, int B, int prec,
                                       size_t budget);

@@ -81,6 +81,16 @@ void report(const char *where, const std::string& what)
   fprintf(stderr,"fftwpp_gb300: %s: %s\n",where,what.c_str());
 }
 
+// Every kernel moves whole elements with vector accesses (16-byte for
+// complex FP64): a misaligned array would fault the GPU, so it is refused.
+bool aligned(const void *p, size_t a) {return (size_t) p % a == 0;}
+
+bool alignedAll(const void *const *p, int n, size_t a)
+{
+  for(int i=0; i < n; ++i) if(!aligned(p[i],a)) return false;
+  return true;
+}
+
 fgb_conv *make(int dim, const int *kinds, const long *L, const long *M,
                const long *m, int A, int B, int mult, int prec, long batch,
                const char *where)
@@ -619,6 +629,13 @@ int fgb_convolve_device(fgb_conv *c, void *const *in, void *const *out,
                         void *stream)
 {
   if(!c || !in || !out) {report("fgb_convolve_device","bad arguments"); return -1;}
+  const ConvInfo& I=c->conv->info();
+  if(!alignedAll(in,I.A,c->conv->elemBytes()) ||
+     !alignedAll(out,I.B,c->conv->elemBytes())) {
+    report("fgb_convolve_device","arrays must be aligned to their element "
+           "size ("+std::to_string(c->conv->elemBytes())+" bytes)");
+    return -1;
+  }
   cudaError_t e=c->conv->run(in,out,(cudaStream_t) stream);
   if(e != cudaSuccess) {
     report("fgb_convolve_device",cudaGetErrorString(e));
@@ -714,6 +731,12 @@ int fgb_batch_convolve_device(fgb_batch *h, void *const *in, void *const *out,
                               void *stream, int use_graph)
 {
   if(!h || !in || !out) {report("fgb_batch_convolve_device","bad arguments"); return -1;}
+  size_t eb=h->b->precision() == PREC_F64 ? 16 : 8;
+  if(!alignedAll(in,h->b->inputs(),eb) || !alignedAll(out,h->b->outputs(),eb)) {
+    report("fgb_batch_convolve_device","packed arrays must be aligned to "
+           "their element size ("+std::to_string(eb)+" bytes)");
+    return -1;
+  }
   cudaError_t e=use_graph ? h->b->runGraph(in,out,(cudaStream_t) stream) :
     h->b->run(in,out,(cudaStream_t) stream);
   if(e != cudaSuccess) {
@@ -766,6 +789,11 @@ int fgb_pad_forward_device(fgb_pad *h, const void *f, void *F, void *stream)
 {
   if(!h || !f || !F) {report("fgb_pad_forward_device","null argument");
     return -1;}
+  if(!h->t->aligned(f,F)) {
+    report("fgb_pad_forward_device","arrays must be aligned to their "
+           "element size");
+    return -1;
+  }
   cudaError_t e=h->t->forward(f,F,(cudaStream_t) stream);
   if(e != cudaSuccess) {
     report("fgb_pad_forward_device",cudaGetErrorString(e));
@@ -778,6 +806,11 @@ int fgb_pad_backward_device(fgb_pad *h, const void *F, void *f, void *stream)
 {
   if(!h || !f || !F) {report("fgb_pad_backward_device","null argument");
     return -1;}
+  if(!h->t->aligned(f,F)) {
+    report("fgb_pad_backward_device","arrays must be aligned to their "
+           "element size");
+    return -1;
+  }
   cudaError_t e=h->t->backward(F,f,(cudaStream_t) stream);
   if(e != cudaSuccess) {
     report("fgb_pad_backward_device",cudaGetErrorString(e));
@@ -830,6 +863,11 @@ int fgb_fft_execute_device(fgb_fft *h, const void *in, void *out,
 {
   if(!h || !in || !out) {report("fgb_fft_execute_device","null argument");
     return -1;}
+  if(!h->t->aligned(in,out)) {
+    report("fgb_fft_execute_device","arrays must be aligned to their "
+           "element size");
+    return -1;
+  }
   if(in == out && !h->inplaceOK) {
     report("fgb_fft_execute_device","interleaved real transforms must be "
            "out of place");

@@ -935,12 +935,20 @@ cudaError_t Conv::runHost(const void *const *in, void *const *out,
     bool ok=true;
     for(int a=0; a < A && ok; ++a) ok=(min[a]=mappedAddress(in[a])) != NULL;
     for(int b=0; b < B && ok; ++b) ok=(mout[b]=mappedAddress(out[b])) != NULL;
-    if(ok && directSegments()) {
+    bool elemAligned=true;
+    for(int a=0; a < A && ok; ++a)
+      elemAligned=elemAligned && (size_t) min[a] % elemBytes() == 0;
+    for(int b=0; b < B && ok; ++b)
+      elemAligned=elemAligned && (size_t) mout[b] % elemBytes() == 0;
+    if(ok && elemAligned && directSegments()) {
       cudaError_t e=run(min.data(),mout.data(),s);
       if(e != cudaSuccess) return e;
       return cudaStreamSynchronize(s);
     }
-    if(ok && bytes % 16 == 0) {
+    bool aligned=bytes % 16 == 0;
+    for(int a=0; a < A; ++a) aligned=aligned && (size_t) min[a] % 16 == 0;
+    for(int b=0; b < B; ++b) aligned=aligned && (size_t) mout[b] % 16 == 0;
+    if(ok && aligned) {
       // Narrow column segments would waste the link's lines: move the
       // arrays whole with the SMs and convolve in device memory.
       if(!hostIn &&
@@ -1007,6 +1015,12 @@ PadTransform::PadTransform(int kind, long L, long M, long C, long mForce,
 }
 
 size_t PadTransform::outElements() const {return (size_t) a.rows*C;}
+
+bool PadTransform::aligned(const void *f, const void *F) const
+{
+  size_t cplx=elem(prec), data=a.kind == KIND_REAL ? cplx/2 : cplx;
+  return (size_t) f % data == 0 && (size_t) F % cplx == 0;
+}
 
 template<typename T>
 cudaError_t PadTransform::runT(const void *in, void *out, bool fwd,
@@ -1112,6 +1126,13 @@ cudaError_t PlainFFT::runT(const void *in, void *out, cudaStream_t s)
   if(kind == FFT_C2R) return launchOuterRealBwd<T>(P,threads,s);
   return sign > 0 ? launchOuterFwd<T>(P,threads,s) :
     launchOuterBwd<T>(P,threads,s);
+}
+
+bool PlainFFT::aligned(const void *in, const void *out) const
+{
+  size_t cplx=elem(prec), real=cplx/2;
+  size_t ai=kind == FFT_R2C ? real : cplx, ao=kind == FFT_C2R ? real : cplx;
+  return (size_t) in % ai == 0 && (size_t) out % ao == 0;
 }
 
 cudaError_t PlainFFT::execute(const void *in, void *out, cudaStream_t s)

@@ -136,6 +136,9 @@ public:
   int precision() const {return prec;}
   size_t inElements() const {return (size_t) a.L*C;}
   size_t outElements() const;
+  // Whether f (data side) and F (transform side) meet the element
+  // alignment the kernels' vector accesses need.
+  bool aligned(const void *f, const void *F) const;
 private:
   AxisPlan a;
   long C;
@@ -161,6 +164,7 @@ public:
            long ibatch, long ostride, long obatch, int prec);
   cudaError_t execute(const void *in, void *out, cudaStream_t s);
   int columnsPerCTA() const {return tile;}
+  bool aligned(const void *in, const void *out) const;
 private:
   int kind, sign, prec;
   long n, C, B, istride, ibatch, ostride, obatch;

@@ -113,6 +113,8 @@ extern "C" int fgb_hconv2d_convolve_noalloc(const void *f, const void *g,
   using namespace fgb;
   typedef cplx<double> Cx;
   if(!f || !g || !h || Lx < 1 || Ly < 1) return fail("bad arguments");
+  if(((size_t) f | (size_t) g | (size_t) h) % 16)
+    return fail("arrays must be 16-byte aligned (complex128 elements)");
   const long Hy=(long) ceilquotient(Ly,2);
   // Default padding of the reference's hconv2d (HybridConvolution.h:94-95).
   const long Mx=3*(long) ceilquotient(Lx,2)-2*(long) (Lx % 2);

@@ -168,3 +168,28 @@ def test_plain_fft_plans(native_lib):
         else:
             assert not h
             assert msg in _native.last_error(), _native.last_error()
+
+
+def test_misaligned_arrays_refused(native_lib):
+    """Transform entry points refuse arrays that are not aligned to their
+    element size before anything reaches the GPU (the kernels' vector
+    accesses would fault on them)."""
+    from fftwpp_gb300 import _native
+    lib = native_lib
+    t = lib.fgb_pad_create(0, 64, 127, 1, 0, 0)
+    try:
+        assert lib.fgb_pad_forward_device(t, 4096 + 8, 8192, None) == -1
+        assert "aligned" in _native.last_error()
+        assert lib.fgb_pad_backward_device(t, 4096, 8192 + 8, None) == -1
+    finally:
+        lib.fgb_pad_destroy(t)
+    f = lib.fgb_fft_create(1, 64, -1, 1, 1, 1, 64, 1, 33, 0)     # r2c FP64
+    try:
+        assert lib.fgb_fft_execute_device(f, 4096 + 4, 8192, None) == -1
+        assert "aligned" in _native.last_error()
+        assert lib.fgb_fft_execute_device(f, 4096 + 8, 8192 + 8, None) == -1
+    finally:
+        lib.fgb_fft_destroy(f)
+    assert lib.fgb_hconv2d_convolve_noalloc(4096 + 8, 8192, 12288, 63, 63,
+                                            None) != 0
+    assert "aligned" in _native.last_error()

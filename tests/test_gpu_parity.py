@@ -237,3 +237,23 @@ def test_zero_copy_host_path(native_lib, precision, case):
         native_lib.fgb_set_zero_copy(1)
     assert np.array_equal(zc[0], cp[0])
     assert np.array_equal(zc[1], cp[1])      # the second input is untouched
+
+
+def test_host_path_misaligned_pinned(native_lib):
+    """Page-locked arrays that start off a 16-byte boundary take the copying
+    path instead of failing."""
+    import torch
+    from fftwpp_gb300.gpu import HybridConvolution
+    kinds, L, M = [H.CENTERED, H.HERMITIAN], [31, 31], [46, 46]
+    fs = _inputs(kinds, L, 2, seed=29)
+    want = H.convolve(fs, kinds, L, M, mult="realbinary")[0]
+    conv = HybridConvolution(kinds, L, M, mult="realbinary")
+    hs = []
+    for f in fs:
+        raw = torch.empty(f.size * 2 + 1, dtype=torch.float64).pin_memory()
+        a = raw.numpy()[1:].view(np.complex128).reshape(f.shape)
+        a[...] = f
+        assert a.ctypes.data % 16 == 8
+        hs.append(a)
+    conv.convolve_host(*hs)
+    assert rel_l2(hs[0], want) <= 1e-13
