@@ -179,10 +179,14 @@ __device__ __forceinline__ void fftStage(const cplx<T> *__restrict__ x,
   const int total=nR*ncol;
   const float invNcol=1.0f/(float) ncol;
   const float invNs=1.0f/(float) Ns;
+  // Power-of-two column counts and spans (the common case) divide by
+  // shifts and masks; the others through the float reciprocal.
+  const bool p2c=(ncol & (ncol-1)) == 0, p2s=(Ns & (Ns-1)) == 0;
+  const int lc=__ffs(ncol)-1;
   for(int idx=tid; idx < total; idx += nthr) {
-    int j=fdiv(idx,invNcol);
+    int j=p2c ? idx >> lc : fdiv(idx,invNcol);
     int c=idx-j*ncol;
-    int k=j-fdiv(j,invNs)*Ns;
+    int k=p2s ? j & (Ns-1) : j-fdiv(j,invNs)*Ns;
     cplx<T> a[R];
 #pragma unroll
     for(int r=0; r < R; ++r) a[r]=nrm(x[sp((j+r*nR)*ld+c)]);
@@ -249,10 +253,12 @@ __device__ __forceinline__ void ipStage(cplx<T> *__restrict__ x, int n, int Ls,
   const int total=(n/R)*ncol;
   const float invNcol=1.0f/(float) ncol;
   const float invM=1.0f/(float) m;
+  const bool p2c=(ncol & (ncol-1)) == 0, p2m=(m & (m-1)) == 0;
+  const int lc=__ffs(ncol)-1, lm=__ffs(m)-1;
   for(int idx=tid; idx < total; idx += nthr) {
-    int q=fdiv(idx,invNcol);
+    int q=p2c ? idx >> lc : fdiv(idx,invNcol);
     int c=idx-q*ncol;
-    int b=fdiv(q,invM);
+    int b=p2m ? q >> lm : fdiv(q,invM);
     int j=q-b*m;
     int base=b*Ls+j;
     cplx<T> a[R];
