@@ -26,9 +26,10 @@ static const int THREADS=256;
 
 static size_t elemBytes(int prec) {return prec == PREC_F64 ? 16 : 8;}
 
-static size_t rowNeedB(int prec, long L, long m, int A, int B)
+static size_t rowNeedB(int prec, long L, long m, int A, int B, int rpc=1)
 {
-  return prec == PREC_F64 ? rowSmem<double>(L,m,A,B) : rowSmem<float>(L,m,A,B);
+  return prec == PREC_F64 ? rowSmem<double>(L,m,A,B,rpc) :
+    rowSmem<float>(L,m,A,B,rpc);
 }
 
 static size_t outerNeedB(int prec, long L, long m, int tile)
@@ -93,6 +94,8 @@ BatchConv::BatchConv(int nprob, const long *L, const long *M,
     throw std::runtime_error("batched problems are fftPad or fftPadCentered");
   if(prec != PREC_F64 && prec != PREC_F32)
     throw std::runtime_error("batched problems run in FP64 or FP32");
+  // Per-task shared memory: three CTAs per SM (a larger FP64 budget with
+  // two CTAs per SM measured slower).
   budget=72*1024;
   Ls.assign(L,L+nprob);
   Ms.assign(M,M+nprob);
@@ -210,8 +213,12 @@ void BatchConv::build()
       long N=nextfftsize(M);
       if(N % m) throw std::runtime_error("row length must divide N");
       long qc=N/m, pc=ceilquotient(L,m);
-      int tile=prec == PREC_F64 ? 8 : 16;
-      while(tile > 1 && outerNeedB(prec,pc,qc,tile) > budget) tile /= 2;
+      // Column tasks take as many columns as the shared-memory budget
+      // allows (each column is only a qc-point transform, so narrow tiles
+      // would be dominated by per-task overhead).
+      int tile=128;
+      while(tile > 1 && (tile > m || outerNeedB(prec,pc,qc,tile) > budget))
+        tile /= 2;
       stagingOff[i]=(long) stagingBytes;
       stagingBytes += e*(size_t) N*A;
       OuterPlan<T>& F=P.fwd;
@@ -227,16 +234,20 @@ void BatchConv::build()
       G.count=B;
       G.scale=(T) (1.0/(double) N);
       for(int b=0; b < B; ++b) G.out[b]=(cplx<T> *) (offsets[i]*e);
+      // Several rows per row task where they fit the budget.
+      int rpc=1;
+      while(rpc < 8 && rpc < qc &&
+            rowNeedB(prec,m,m,A,B,rpc+1) <= budget) ++rpc;
       RowPlan<T>& R=P.row;
       R.L=(int) m; R.m=(int) m; R.q=1; R.N=(int) m; R.cshift=0;
-      R.A=A; R.B=B; R.mult=mult; R.realIO=0; R.rpc=1; R.scale=(T) 1;
+      R.A=A; R.B=B; R.mult=mult; R.realIO=0; R.rpc=rpc; R.scale=(T) 1;
       R.fp=fftPlanPublic(m,prec);
       R.twN=(const Tw *) twiddles(m,prec);
       R.rowStride=m; R.nrows=qc;
       P.rel=4|8;
       P.nfwd=(int) (ceilquotient(m,tile)*A);
-      P.nrows=(int) qc;
-      smem=std::max(smem,rowNeedB(prec,m,m,A,B));
+      P.nrows=(int) ceilquotient(qc,rpc);   // row tasks the backward waits for
+      smem=std::max(smem,rowNeedB(prec,m,m,A,B,rpc));
       smem=std::max(smem,outerNeedB(prec,pc,qc,tile));
       lng.push_back({(double) N*std::log2((double) N),i});
       ++nlong;
