@@ -78,6 +78,10 @@ def load():
     lib.fgb_batch_error.argtypes = [vp]
     lib.fgb_batch_destroy.restype = None
     lib.fgb_batch_destroy.argtypes = [vp]
+    lib.fgb_batch_set_spin_limit.restype = ctypes.c_int
+    lib.fgb_batch_set_spin_limit.argtypes = [vp, ctypes.c_longlong]
+    lib.fgb_batch_block_problem.restype = ctypes.c_int
+    lib.fgb_batch_block_problem.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.fgb_pad_create.restype = vp
     lib.fgb_pad_create.argtypes = [ctypes.c_int, sz, sz, sz, sz, ctypes.c_int]
     lib.fgb_pad_forward_device.restype = ctypes.c_int

@@ -9,6 +9,9 @@
 // copies inside the persistent kernel and keeps the fastest; results are
 // cached for the life of the process.
 #include "batch.h"
+
+#include <climits>
+#include <cstddef>
 #include "kernels.cuh"
 
 #include <algorithm>
@@ -292,6 +295,10 @@ void BatchConv::build()
       for(int b=0; b < B; ++b) tasks.push_back({TASK_COLBWD,o.i,t,b});
   }
   ntasks=(int) tasks.size();
+  nfwd0.resize(n);
+  for(int i=0; i < n; ++i) nfwd0[i]=probs[i].nfwd;
+  probBytes=sizeof(BatchProblem<T>);
+  nfwdOffset=offsetof(BatchProblem<T>,nfwd);
   size_t pb=sizeof(BatchProblem<T>)*n, tb=sizeof(BatchTask)*tasks.size();
   if(cudaMalloc(&dProbs,pb) != cudaSuccess ||
      cudaMalloc(&dTasks,tb) != cudaSuccess ||
@@ -326,7 +333,7 @@ cudaError_t BatchConv::launch(const void *const *in, void *const *out,
   P.queue=(int *) dCounters;
   P.err=(int *) dCounters+1;
   P.done=(int *) dCounters+2;
-  P.spinLimit=20000000LL;
+  P.spinLimit=spinLimit;
   P.mult=mult;
   P.A=A;
   P.B=B;
@@ -385,5 +392,19 @@ int BatchConv::error()
 }
 
 long BatchConv::choice(int i) const {return choices[i];}
+
+void BatchConv::setSpinLimit(long long polls)
+{
+  spinLimit=polls;
+  graphKey.clear();                // the limit is a launch argument
+}
+
+cudaError_t BatchConv::blockProblem(int i, bool blocked)
+{
+  if(i < 0 || i >= n || choices[i] > 0) return cudaErrorInvalidValue;
+  int v=blocked ? INT_MAX : nfwd0[i];
+  return cudaMemcpy((char *) dProbs+(size_t) i*probBytes+nfwdOffset,&v,
+                    sizeof(int),cudaMemcpyHostToDevice);
+}
 
 } // namespace fgb

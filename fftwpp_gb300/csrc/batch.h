@@ -27,6 +27,12 @@ public:
   // Nonzero if a bounded wait inside the kernel gave up (reading clears it).
   int error();
 
+  // Failure detection: polls before a dependency wait gives up (default
+  // 2e7, seconds), and a test hook that makes the waits of long problem i
+  // unreachable so that they time out (blocked) or restores them.
+  void setSpinLimit(long long polls);
+  cudaError_t blockProblem(int i, bool blocked);
+
   long choice(int i) const;
   int tasks() const {return ntasks;}
   int gridSize() const {return grid;}
@@ -43,6 +49,9 @@ public:
 
 private:
   int n, A, B, mult, prec, kind;
+  long long spinLimit=20000000LL;
+  std::vector<int> nfwd0;          // per problem: forward tasks a row waits for
+  size_t probBytes=0, nfwdOffset=0;
   std::vector<long> Ls, Ms, offsets, choices;
   long total;
   void *dProbs, *dTasks, *dCounters, *staging;

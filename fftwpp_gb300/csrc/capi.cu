@@ -770,6 +770,26 @@ int fgb_batch_error(fgb_batch *h)
 
 void fgb_batch_destroy(fgb_batch *h) {delete h;}
 
+int fgb_batch_set_spin_limit(fgb_batch *h, long long polls)
+{
+  if(!h || polls < 0) {report("fgb_batch_set_spin_limit","bad arguments");
+    return -1;}
+  h->b->setSpinLimit(polls);
+  return 0;
+}
+
+int fgb_batch_block_problem(fgb_batch *h, int i, int blocked)
+{
+  if(!h) {report("fgb_batch_block_problem","null handle"); return -1;}
+  cudaError_t e=h->b->blockProblem(i,blocked != 0);
+  if(e != cudaSuccess) {
+    report("fgb_batch_block_problem","problem "+std::to_string(i)+
+           " is not a long problem of this batch");
+    return -1;
+  }
+  return 0;
+}
+
 // Standalone padded transforms (engine.h, class PadTransform).
 fgb_pad *fgb_pad_create(int kind, size_t L, size_t M, size_t C, size_t m,
                         int precision)

@@ -131,6 +131,15 @@ long fgb_batch_choice(const fgb_batch *b, int i);
 int fgb_batch_error(fgb_batch *b);
 void fgb_batch_destroy(fgb_batch *b);
 
+/* Failure detection.  Every dependency wait of the persistent kernel polls
+ * at most `polls` times (default 2e7, seconds) and then gives up: its task
+ * is skipped, fgb_batch_error() reports it, the launch still finishes and
+ * the CUDA context stays usable.  fgb_batch_block_problem makes the waits
+ * of long problem i (fgb_batch_choice(i) < 0) unreachable (blocked != 0)
+ * or restores them, so tests can make a wait run out on purpose. */
+int fgb_batch_set_spin_limit(fgb_batch *b, long long polls);
+int fgb_batch_block_problem(fgb_batch *b, int i, int blocked);
+
 /* Standalone padded transforms: the forward and backward transforms of
  * fftPad / fftPadCentered / fftPadReal (convolve.h:515-536, 623-646,
  * 855-877; driven stand-alone by the reference's tests/hybrid.cc and

@@ -56,3 +56,48 @@ def test_batched_matches_single_plans(native_lib):
         s = single.convolve(torch.from_numpy(f[o:o + L].copy()).cuda(),
                             torch.from_numpy(g[o:o + L].copy()).cuda())[0]
         assert rel_l2(out[o:o + L], s.cpu().numpy()) <= 1e-13
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_bounded_wait_runs_out(native_lib, graph):
+    """Failure detection without a GPU fault: one long problem's dependency
+    counter is made unreachable, so its row and column tasks poll a count
+    that never completes until the (short) poll limit runs out; they give
+    up, the error flag is raised, the launch finishes, every other problem
+    is still exact, and the context stays usable."""
+    import torch
+    from fftwpp_gb300.gpu import BatchedConvolution
+    lib = native_lib
+    Ls = [40, 700, 20000, 3000, 25000, 90]
+    conv = BatchedConvolution(Ls, precision="f64")
+    long_ids = [i for i in range(len(Ls)) if conv.choice(i) < 0]
+    short_ids = [i for i in range(len(Ls)) if conv.choice(i) > 0]
+    assert long_ids and short_ids
+    assert lib.fgb_batch_block_problem(conv.handle, short_ids[0], 1) == -1
+    bad = long_ids[0]
+    rng = np.random.default_rng(3)
+    f = rng.uniform(-1, 1, conv.total) + 1j * rng.uniform(-1, 1, conv.total)
+    g = rng.uniform(-1, 1, conv.total) + 1j * rng.uniform(-1, 1, conv.total)
+    tf, tg = torch.from_numpy(f).cuda(), torch.from_numpy(g).cuda()
+    want = [H.convolve([f[o:o + L], g[o:o + L]], [H.PAD], [L], [2 * L - 1])[0]
+            for o, L in zip(conv.offsets, Ls)]
+
+    assert lib.fgb_batch_set_spin_limit(conv.handle, 2000) == 0
+    assert lib.fgb_batch_block_problem(conv.handle, bad, 1) == 0
+    out = conv.convolve(tf, tg, graph=graph)[0]
+    torch.cuda.synchronize()
+    assert conv.error() == 1
+    assert conv.error() == 0                      # reading clears the flag
+    h = out.cpu().numpy()
+    for i, (o, L) in enumerate(zip(conv.offsets, Ls)):
+        if i != bad:
+            assert rel_l2(h[o:o + L], want[i]) <= 1e-13
+
+    assert lib.fgb_batch_block_problem(conv.handle, bad, 0) == 0
+    assert lib.fgb_batch_set_spin_limit(conv.handle, 20000000) == 0
+    out = conv.convolve(tf, tg, graph=graph)[0]
+    torch.cuda.synchronize()
+    assert conv.error() == 0
+    h = out.cpu().numpy()
+    for i, (o, L) in enumerate(zip(conv.offsets, Ls)):
+        assert rel_l2(h[o:o + L], want[i]) <= 1e-13
