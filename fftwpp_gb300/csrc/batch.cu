@@ -119,7 +119,16 @@ BatchConv::BatchConv(int nprob, const long *L, const long *M,
       throw std::runtime_error("no batched plan for L="+std::to_string(Ls[i]));
     choices[i]=tune ? tuned(Ls[i],Ms[i],cand) : cand[0];
   }
-  if(prec == PREC_F64) build<double>(); else build<float>();
+  try {
+    if(prec == PREC_F64) build<double>(); else build<float>();
+  } catch(...) {
+    // A throwing constructor runs no destructor: release what was taken.
+    if(dProbs) cudaFree(dProbs);
+    if(dTasks) cudaFree(dTasks);
+    if(dCounters) cudaFree(dCounters);
+    if(staging) cudaFree(staging);
+    throw;
+  }
 }
 
 // Timing autotuner: per (L, M, A, B, prec, mult, kind) the fastest

@@ -472,8 +472,15 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
     in.rpc=pickRpc(in.m,A,nrows,[&](int r) {
       return rowNeed(prec,in.stored,in.m,A,B,r);});
   }
-  allocate();
-  if(autotune) tune();
+  try {
+    allocate();
+    if(autotune) tune();
+  } catch(...) {
+    // A throwing constructor runs no destructor: release what was taken.
+    for(void *p : bufs) cudaFree(p);
+    bufs.clear();
+    throw;
+  }
 }
 
 bool Conv::autotune=true;
