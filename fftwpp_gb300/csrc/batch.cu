@@ -120,15 +120,82 @@ BatchConv::BatchConv(int nprob, const long *L, const long *M,
     choices[i]=tune ? tuned(Ls[i],Ms[i],cand) : cand[0];
   }
   try {
+    if(tune && nlongCount() > 0) {
+      // Tile shapes: time the whole batch under each cap on the column
+      // tiles of its long problems and keep the fastest.
+      double best=1e300;
+      int bestCap=tileCap;
+      for(int cap : {16,32,64,128}) {
+        tileCap=cap;
+        if(prec == PREC_F64) build<double>(); else build<float>();
+        double t=timeLaunch(3);
+        if(t < best) {best=t; bestCap=cap;}
+        release();
+      }
+      tileCap=bestCap;
+    }
     if(prec == PREC_F64) build<double>(); else build<float>();
   } catch(...) {
     // A throwing constructor runs no destructor: release what was taken.
-    if(dProbs) cudaFree(dProbs);
-    if(dTasks) cudaFree(dTasks);
-    if(dCounters) cudaFree(dCounters);
-    if(staging) cudaFree(staging);
+    release();
     throw;
   }
+}
+
+int BatchConv::nlongCount() const
+{
+  int k=0;
+  for(long c : choices) k += c < 0;
+  return k;
+}
+
+void BatchConv::release()
+{
+  if(exec) {cudaGraphExecDestroy(exec); exec=NULL;}
+  if(graph) {cudaGraphDestroy(graph); graph=NULL;}
+  graphKey.clear();
+  if(dProbs) cudaFree(dProbs);
+  if(dTasks) cudaFree(dTasks);
+  if(dCounters) cudaFree(dCounters);
+  if(staging) cudaFree(staging);
+  dProbs=dTasks=dCounters=staging=NULL;
+  stagingSize=0;
+  nsmall=nlong=0;
+}
+
+// Milliseconds of one launch of the current build on zero-filled scratch
+// arrays (median of reps after a warm-up), or a huge value on failure.
+double BatchConv::timeLaunch(int reps)
+{
+  size_t bytes=elemBytes(prec)*(size_t) total;
+  std::vector<void *> bufs(std::max(A,B),NULL);
+  cudaStream_t s=NULL;
+  cudaEvent_t e0=NULL, e1=NULL;
+  bool ok=cudaStreamCreateWithFlags(&s,cudaStreamNonBlocking) == cudaSuccess &&
+    cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+  for(auto& p : bufs)
+    ok=ok && cudaMalloc(&p,bytes) == cudaSuccess &&
+      cudaMemsetAsync(p,0,bytes,s) == cudaSuccess;
+  std::vector<float> t;
+  if(ok) ok=run(bufs.data(),bufs.data(),s) == cudaSuccess;
+  for(int r=0; r < reps && ok; ++r) {
+    ok=cudaEventRecord(e0,s) == cudaSuccess &&
+      run(bufs.data(),bufs.data(),s) == cudaSuccess &&
+      cudaEventRecord(e1,s) == cudaSuccess &&
+      cudaEventSynchronize(e1) == cudaSuccess;
+    float ms=0;
+    if(ok && cudaEventElapsedTime(&ms,e0,e1) == cudaSuccess) t.push_back(ms);
+  }
+  if(s) cudaStreamSynchronize(s);
+  ok=ok && error() == 0;
+  for(void *p : bufs) if(p) cudaFree(p);
+  if(e0) cudaEventDestroy(e0);
+  if(e1) cudaEventDestroy(e1);
+  if(s) cudaStreamDestroy(s);
+  cudaGetLastError();
+  if(!ok || t.empty()) return 1e300;
+  std::sort(t.begin(),t.end());
+  return t[t.size()/2];
 }
 
 // Timing autotuner: per (L, M, A, B, prec, mult, kind) the fastest
@@ -228,7 +295,7 @@ void BatchConv::build()
       // Column tasks take as many columns as the shared-memory budget
       // allows (each column is only a qc-point transform, so narrow tiles
       // would be dominated by per-task overhead).
-      int tile=128;
+      int tile=tileCap;
       while(tile > 1 && (tile > m || outerNeedB(prec,pc,qc,tile) > budget))
         tile /= 2;
       stagingOff[i]=(long) stagingBytes;
@@ -322,13 +389,8 @@ void BatchConv::build()
 
 BatchConv::~BatchConv()
 {
-  if(exec) cudaGraphExecDestroy(exec);
-  if(graph) cudaGraphDestroy(graph);
+  release();
   if(captureStream) cudaStreamDestroy(captureStream);
-  if(dProbs) cudaFree(dProbs);
-  if(dTasks) cudaFree(dTasks);
-  if(dCounters) cudaFree(dCounters);
-  if(staging) cudaFree(staging);
 }
 
 template<typename T>

@@ -50,6 +50,10 @@ public:
 private:
   int n, A, B, mult, prec, kind;
   long long spinLimit=20000000LL;
+  int tileCap=128;                 // widest column tile of a long problem
+  void release();
+  double timeLaunch(int reps);
+  int nlongCount() const;
   std::vector<int> nfwd0;          // per problem: forward tasks a row waits for
   size_t probBytes=0, nfwdOffset=0;
   std::vector<long> Ls, Ms, offsets, choices;
