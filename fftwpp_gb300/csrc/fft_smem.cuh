@@ -40,6 +40,25 @@ __device__ __forceinline__ int fdiv(int a, float invb)
   return __float2int_rz(((float) a+0.5f)*invb);
 }
 
+// Division by a block-uniform divisor d >= 1: a shift when d is a power of
+// two (the common case), else fdiv's float reciprocal.
+struct UDiv {
+  float inv;
+  int sh;
+  bool p2;
+  __device__ __forceinline__ explicit UDiv(int d)
+    : inv(1.0f/(float) d), sh(0), p2((d & (d-1)) == 0)
+  {
+#ifdef __CUDA_ARCH__
+    sh=__ffs(d)-1;
+#endif
+  }
+  __device__ __forceinline__ int operator()(int a) const
+  {
+    return p2 ? a >> sh : fdiv(a,inv);
+  }
+};
+
 struct FFTPlanDev {
   int n;
   int nst;

@@ -322,13 +322,13 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
   cplx<T> *y=x+padded(m*ld);         // ping-pong buffer of the FP64 form
   const int tid=threadIdx.x, nthr=blockDim.x;
   const typename TwT<T>::type *tw=P.twN;
-  const float invL=1.0f/(float) L, invLd=1.0f/(float) ld;
-  const float invR=1.0f/(float) R;
+  const UDiv dL(L), dLd(ld);
+  const UDiv dR(R);
   const long long row0=group*R;
 
   for(int i=tid; i < ld*L; i += nthr) {
-    int col=fdiv(i,invL), s=i-col*L;
-    int a=fdiv(col,invR);
+    int col=dL(i), s=i-col*L;
+    int a=dR(col);
     long long row=row0+col-a*R;
     cplx<T> v=mk((T) 0,(T) 0);
     if(row < P.nrows) {
@@ -345,7 +345,7 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
   for(int r=0; r < P.q; ++r) {
     // Fold the data into one length-m block with the residue twiddles.
     for(int i=tid; i < m*ld; i += nthr) {
-      int t=fdiv(i,invLd), col=i-t*ld;
+      int t=dLd(i), col=i-t*ld;
       int s0=posmod(t+c,m);
       cplx<T> sum=mk((T) 0,(T) 0);
       for(int s=s0; s < L; s += m) {
@@ -360,7 +360,7 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
     if constexpr(inplaceFFT<T>()) {
       fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
       for(int i=tid; i < m*R; i += nthr) {
-        int j=fdiv(i,invR), rho=i-j*R;
+        int j=dR(i), rho=i-j*R;
         multiplySlot<K>(x,j*ld+rho,R,A,B,P.mult);
       }
       __syncthreads();
@@ -370,14 +370,14 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
       cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
       cplx<T> *Y=X == x ? y : x;
       for(int i=tid; i < m*R; i += nthr) {
-        int j=fdiv(i,invR), rho=i-j*R;
+        int j=dR(i), rho=i-j*R;
         multiplySlot<K>(X,j*ld+rho,R,A,B,P.mult);
       }
       __syncthreads();
       Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
     }
     for(int i=tid; i < lb*L; i += nthr) {
-      int col=fdiv(i,invL), s=i-col*L;
+      int col=dL(i), s=i-col*L;
       int t=posmod(s-c,m);
       cplx<T> v=Z[sp(t*ld+col)];
       if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
@@ -386,8 +386,8 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
     __syncthreads();
   }
   for(int i=tid; i < lb*L; i += nthr) {
-    int col=fdiv(i,invL), s=i-col*L;
-    int b=fdiv(col,invR);
+    int col=dL(i), s=i-col*L;
+    int b=dR(col);
     long long row=row0+col-b*R;
     if(row >= P.nrows) continue;
     long long off=row*P.rowStride+s;
@@ -426,8 +426,8 @@ hermRowKernel(const HermRowPlan<T> P)
   const int tid=threadIdx.x, nthr=blockDim.x;
   const typename TwT<T>::type *tw=P.twN;
   const T half=(T) 0.5;
-  const float invH=1.0f/(float) H, invLd=1.0f/(float) ld;
-  const float invR=1.0f/(float) R;
+  const UDiv dH(H), dLd(ld);
+  const UDiv dR(R);
   const long long groups=(P.nrows+R-1)/R;
 
   // Rows g*R .. g*R+R-1 are transformed together; column col = a*R + rho.
@@ -438,8 +438,8 @@ hermRowKernel(const HermRowPlan<T> P)
     // hits; every read of the group precedes its writes, so in = out is
     // safe).
     for(int i=tid; i < Nh*ld; i += nthr) {
-      int k=fdiv(i,invLd), col=i-k*ld;
-      int a=fdiv(col,invR);
+      int k=dLd(i), col=i-k*ld;
+      int a=dR(col);
       long long row=row0+col-a*R;
       const cplx<T> *zr=P.in[a]+row*P.rowStride;
       const bool live=row < P.nrows;
@@ -457,7 +457,7 @@ hermRowKernel(const HermRowPlan<T> P)
     if constexpr(inplaceFFT<T>()) {
       fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
       for(int i=tid; i < Nh*R; i += nthr) {
-        int t=fdiv(i,invR), rho=i-t*R;
+        int t=dR(i), rho=i-t*R;
         multiplySlot<K>(x,t*ld+rho,R,A,B,P.mult);
       }
       __syncthreads();
@@ -467,7 +467,7 @@ hermRowKernel(const HermRowPlan<T> P)
       cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
       cplx<T> *Y=X == x ? y : x;
       for(int i=tid; i < Nh*R; i += nthr) {
-        int t=fdiv(i,invR), rho=i-t*R;
+        int t=dR(i), rho=i-t*R;
         multiplySlot<K>(X,t*ld+rho,R,A,B,P.mult);
       }
       __syncthreads();
@@ -475,8 +475,8 @@ hermRowKernel(const HermRowPlan<T> P)
     }
     // V[k] = E[k] + W_N^{-k} O[k],  E=(Zk+conj Zm)/2, O=(Zk-conj Zm)/(2i)
     for(int i=tid; i < lb*H; i += nthr) {
-      int col=fdiv(i,invH), k=i-col*H;
-      int b=fdiv(col,invR);
+      int col=dH(i), k=i-col*H;
+      int b=dR(col);
       long long row=row0+col-b*R;
       if(row >= P.nrows) continue;
       cplx<T> zk=Z[sp(k*ld+col)];
@@ -510,7 +510,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
   const cplx<T> *src=P.in[a]+batch*P.inBatch;
   cplx<T> *dst=P.out[a]+batch*P.outBatch;
   const typename TwT<T>::type *tw=P.twN;
-  const float invTile=1.0f/(float) tile;
+  const UDiv dTile(tile);
 
   if constexpr(inplaceFFT<T>()) {
     if(P.inplace) {
@@ -520,7 +520,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
       // Asynchronous copies straight to each value's slot, then the
       // conversion and residue twiddle in place by the same thread.
       for(int i=tid; i < m*tile; i += nthr) {
-        int t=fdiv(i,invTile), cc=i-t*tile;
+        int t=dTile(i), cc=i-t*tile;
         int col=col0+cc;
         int s=posmod(t+c,m);
         long long off=(long long) s*P.inRow+col;
@@ -530,7 +530,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
       cpAsyncWait();
       if(r != 0 || (P.io64 & 1)) {
         for(int i=tid; i < m*tile; i += nthr) {
-          int t=fdiv(i,invTile), cc=i-t*tile;
+          int t=dTile(i), cc=i-t*tile;
           int col=col0+cc;
           int s=posmod(t+c,m);
           long long off=(long long) s*P.inRow+col;
@@ -543,7 +543,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
       __syncthreads();
       fftDIF<T,1>(x,P.fp,tile,tile,tid,nthr);
       for(int i=tid; i < m*tile; i += nthr) {
-        int j=fdiv(i,invTile), cc=i-j*tile;
+        int j=dTile(i), cc=i-j*tile;
         int col=col0+cc;
         if(col < P.C) dst[((long long) r*m+j)*P.outRow+col]=x[sp(i)];
       }
@@ -555,7 +555,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
   // Stage the L x tile input block in y with asynchronous copies (many
   // loads in flight per thread instead of one dependent load per output).
   for(int i=tid; i < L*tile; i += nthr) {
-    int s=fdiv(i,invTile), cc=i-s*tile;
+    int s=dTile(i), cc=i-s*tile;
     int col=col0+cc;
     long long off=(long long) s*P.inRow+col;
     if(col < P.C && off < P.Ltot) cpAsync(y+i,src+off);
@@ -565,7 +565,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
   if(std::is_same<T,ff>::value && (P.io64 & 1)) {
     // The caller's FP64 values were staged as they are: convert them.
     for(int i=tid; i < L*tile; i += nthr) {
-      int s=fdiv(i,invTile), cc=i-s*tile;
+      int s=dTile(i), cc=i-s*tile;
       int col=col0+cc;
       long long off=(long long) s*P.inRow+col;
       if(col < P.C && off < P.Ltot) convertStaged(y,i);
@@ -573,7 +573,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
   }
   __syncthreads();
   for(int i=tid; i < m*tile; i += nthr) {
-    int t=fdiv(i,invTile), cc=i-t*tile;
+    int t=dTile(i), cc=i-t*tile;
     cplx<T> sum=mk((T) 0,(T) 0);
     int s0=posmod(t+c,m);
     for(int s=s0; s < L; s += m) {
@@ -586,7 +586,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
   __syncthreads();
   cplx<T> *X=fftSmem<T,1>(x,y,P.fp,tile,tile,tid,nthr);
   for(int i=tid; i < m*tile; i += nthr) {
-    int j=fdiv(i,invTile), cc=i-j*tile;
+    int j=dTile(i), cc=i-j*tile;
     int col=col0+cc;
     if(col < P.C) {
       cplx<T> v=X[sp(i)];
@@ -629,7 +629,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
   const cplx<T> *src=P.in[b]+batch*P.inBatch;
   cplx<T> *dst=P.out[b]+batch*P.outBatch;
   const typename TwT<T>::type *tw=P.twN;
-  const float invTile=1.0f/(float) tile;
+  const UDiv dTile(tile);
 
   if(!direct)
     for(int i=tid; i < L*tile; i += nthr) acc[i]=mk((T) 0,(T) 0);
@@ -637,7 +637,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
     if(CG) {
       // Data written by other CTAs of this launch: L2 loads.
       for(int i=tid; i < m*tile; i += nthr) {
-        int j=fdiv(i,invTile), cc=i-j*tile;
+        int j=dTile(i), cc=i-j*tile;
         int col=col0+cc;
         cplx<T> v=mk((T) 0,(T) 0);
         if(col < P.C) v=ldx<CG>(src+((long long) r*m+j)*P.inRow+col);
@@ -645,7 +645,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
       }
     } else {
       for(int i=tid; i < m*tile; i += nthr) {
-        int j=fdiv(i,invTile), cc=i-j*tile;
+        int j=dTile(i), cc=i-j*tile;
         int col=col0+cc;
         if(col < P.C) cpAsync(x+sp(i),src+((long long) r*m+j)*P.inRow+col);
         else x[sp(i)]=mk((T) 0,(T) 0);
@@ -655,7 +655,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
     __syncthreads();
     if(P.twX) {
       for(int i=tid; i < m*tile; i += nthr) {
-        int j=fdiv(i,invTile), cc=i-j*tile;
+        int j=dTile(i), cc=i-j*tile;
         unsigned long long e=((unsigned long long) (col0+cc)*
                               (unsigned long long) ((long long) r*m+j)) %
           (unsigned long long) P.NX;
@@ -672,7 +672,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
     }
     if(direct) {
       for(int i=tid; i < L*tile; i += nthr) {
-        int s=fdiv(i,invTile), cc=i-s*tile;
+        int s=dTile(i), cc=i-s*tile;
         int col=col0+cc;
         long long off=(long long) s*P.outRow+col;
         if(col < P.C && off < P.Ltot)
@@ -682,7 +682,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
       return;
     }
     for(int i=tid; i < L*tile; i += nthr) {
-      int s=fdiv(i,invTile), cc=i-s*tile;
+      int s=dTile(i), cc=i-s*tile;
       int t=posmod(s-c,m);
       cplx<T> v=X[sp(t*tile+cc)];
       if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
@@ -691,7 +691,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
     __syncthreads();
   }
   for(int i=tid; i < L*tile; i += nthr) {
-    int s=fdiv(i,invTile), cc=i-s*tile;
+    int s=dTile(i), cc=i-s*tile;
     int col=col0+cc;
     long long off=(long long) s*P.outRow+col;
     if(col < P.C && off < P.Ltot) storeIO(dst+off,acc[i]*P.scale,P.io64 & 2);
@@ -727,10 +727,10 @@ outerRealFwdKernel(const OuterPlan<T> P)
   cplx<T> *dst=P.out[a]+batch*P.outBatch;
   const typename TwT<T>::type *tw=P.twN;
   const T half=(T) 0.5;
-  const float invTile=1.0f/(float) tile;
+  const UDiv dTile(tile);
 
   for(int i=tid; i < Nh*tile; i += nthr) {
-    int t=fdiv(i,invTile), cc=i-t*tile;
+    int t=dTile(i), cc=i-t*tile;
     int col=col0+cc;
     T re=(T) 0, im=(T) 0;
     if(col < P.C) {
@@ -743,7 +743,7 @@ outerRealFwdKernel(const OuterPlan<T> P)
   __syncthreads();
   cplx<T> *X=fftSmem<T,1>(x,y,P.fp,tile,tile,tid,nthr);
   for(int i=tid; i < (Nh+1)*tile; i += nthr) {
-    int k=fdiv(i,invTile), cc=i-k*tile;
+    int k=dTile(i), cc=i-k*tile;
     int col=col0+cc;
     if(col >= P.C) continue;
     int k0=k == Nh ? 0 : k;
@@ -778,10 +778,10 @@ outerRealBwdKernel(const OuterPlan<T> P)
   const cplx<T> *src=P.in[b]+batch*P.inBatch;
   T *dst=(T *) P.out[b]+batch*P.outBatch;
   const typename TwT<T>::type *tw=P.twN;
-  const float invTile=1.0f/(float) tile;
+  const UDiv dTile(tile);
 
   for(int i=tid; i < Nh*tile; i += nthr) {
-    int k=fdiv(i,invTile), cc=i-k*tile;
+    int k=dTile(i), cc=i-k*tile;
     int col=col0+cc;
     cplx<T> v=mk((T) 0,(T) 0);
     if(col < P.C) {
@@ -803,7 +803,7 @@ outerRealBwdKernel(const OuterPlan<T> P)
   __syncthreads();
   cplx<T> *X=fftSmem<T,-1>(x,y,P.fp,tile,tile,tid,nthr);
   for(int i=tid; i < Nh*tile; i += nthr) {
-    int t=fdiv(i,invTile), cc=i-t*tile;
+    int t=dTile(i), cc=i-t*tile;
     int col=col0+cc;
     if(col >= P.C) continue;
     cplx<T> v=X[sp(i)]*P.scale;
