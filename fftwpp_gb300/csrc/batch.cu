@@ -46,7 +46,7 @@ static size_t outerNeedB(int prec, long L, long m, int tile)
 
 static double fftCostB(long m) {return m*std::log2((double) std::max(m,2L));}
 
-FFTPlanDev fftPlanPublic(long n, int prec);   // engine.cu
+FFTPlanDev fftPlanPublic(long n, int prec, bool oddFirst);   // engine.cu
 
 // Candidate plans of one problem, cheapest (by the cost model) first.
 // choice > 0: short problem with residue block m = choice;
@@ -276,7 +276,7 @@ void BatchConv::build()
       R.cshift=kind == KIND_CENTERED ? (int) (L/2) : 0;
       R.A=A; R.B=B; R.mult=mult; R.realIO=0; R.rpc=1;
       R.scale=(T) (1.0/(double) (m*q));
-      R.fp=fftPlanPublic(m,prec);
+      R.fp=fftPlanPublic(m,prec,prec != PREC_F64);   // in-place rows in FP32
       R.twN=(const Tw *) twiddles(m*q,prec);
       R.rowStride=L; R.nrows=1;
       for(int a=0; a < A; ++a) R.in[a]=(const cplx<T> *) (offsets[i]*e);
@@ -302,7 +302,7 @@ void BatchConv::build()
       stagingBytes += e*(size_t) N*A;
       OuterPlan<T>& F=P.fwd;
       F.L=(int) pc; F.m=(int) qc; F.q=1; F.N=(int) qc; F.cshift=0;
-      F.tile=tile; F.fp=fftPlanPublic(qc,prec);
+      F.tile=tile; F.fp=fftPlanPublic(qc,prec,false);
       F.twN=(const Tw *) twiddles(qc,prec);
       F.twX=(const Tw *) twiddles(N,prec); F.NX=N;
       F.count=A; F.nbatch=1; F.inBatch=F.outBatch=0;
@@ -320,7 +320,7 @@ void BatchConv::build()
       RowPlan<T>& R=P.row;
       R.L=(int) m; R.m=(int) m; R.q=1; R.N=(int) m; R.cshift=0;
       R.A=A; R.B=B; R.mult=mult; R.realIO=0; R.rpc=rpc; R.scale=(T) 1;
-      R.fp=fftPlanPublic(m,prec);
+      R.fp=fftPlanPublic(m,prec,prec != PREC_F64);   // in-place rows in FP32
       R.twN=(const Tw *) twiddles(m,prec);
       R.rowStride=m; R.nrows=qc;
       P.rel=4|8;

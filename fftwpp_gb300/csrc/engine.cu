@@ -143,7 +143,11 @@ const void *twiddles(long n, int prec)
   return d;
 }
 
-static FFTPlanDev fftPlan(long n, int prec)
+// Radices of an n-point transform.  The Stockham form wants the products of
+// earlier radices to be powers of two (odd radices last); the in-place
+// decimation forms want the spans n/(R0...Rs) to be powers of two (odd
+// radices first).  Either way the stage divisions become shifts.
+static FFTPlanDev fftPlan(long n, int prec, bool oddFirst=false)
 {
   if(!smooth(n))
     throw std::runtime_error("transform length "+std::to_string(n)+
@@ -161,12 +165,23 @@ static FFTPlanDev fftPlan(long n, int prec)
   while(r % 3 == 0) {p.radix[p.nst++]=3; r /= 3;}
   if(p.nst > FGB_MAXSTAGES)
     throw std::runtime_error("too many FFT stages");
+  if(oddFirst) {
+    int k=0, tmp[FGB_MAXSTAGES];
+    for(int s=0; s < p.nst; ++s)          // odd radices, then even, in order
+      if(p.radix[s] % 2) tmp[k++]=p.radix[s];
+    for(int s=0; s < p.nst; ++s)
+      if(p.radix[s] % 2 == 0) tmp[k++]=p.radix[s];
+    for(int s=0; s < p.nst; ++s) p.radix[s]=tmp[s];
+  }
   p.tw=twiddles(n,prec);
   if(!p.tw) throw std::runtime_error("twiddle table allocation failed");
   return p;
 }
 
-FFTPlanDev fftPlanPublic(long n, int prec) {return fftPlan(n,prec);}
+FFTPlanDev fftPlanPublic(long n, int prec, bool oddFirst)
+{
+  return fftPlan(n,prec,oddFirst);
+}
 
 // ---------------------------------------------------------------------------
 // Planning.
@@ -689,7 +704,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.realIO=a.kind == KIND_REAL && I.dim == 1;
     P.rpc=I.axis[I.dim-1].rpc;
     P.io64=0;
-    P.fp=fftPlan(a.m,I.prec);
+    P.fp=fftPlan(a.m,I.prec,inplaceFFT<T>());
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };
   auto hermPlan=[&](HermRowPlan<T>& P, const AxisPlan& a) {
@@ -697,18 +712,18 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.A=A; P.B=B; P.mult=I.mult;
     P.rpc=a.rpc;
     P.io64=0;
-    P.fp=fftPlan(a.N/2,I.prec);
+    P.fp=fftPlan(a.N/2,I.prec,inplaceFFT<T>());
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };
   auto outerPlan=[&](OuterPlan<T>& P, const AxisPlan& a) {
     P.L=(int) a.L; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
     P.cshift=a.cshift; P.tile=a.tile;
-    P.fp=fftPlan(a.kind == KIND_REAL ? a.N/2 : a.m,I.prec);
-    P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
-    P.twX=NULL; P.NX=1;
     P.io64=0;
     P.inplace=inplaceFFT<T>() && a.kind != KIND_REAL && a.p == 1;
     P.conj=0;
+    P.fp=fftPlan(a.kind == KIND_REAL ? a.N/2 : a.m,I.prec,P.inplace != 0);
+    P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
+    P.twX=NULL; P.NX=1;
   };
   // Float-float mode: the first launch reads the caller's FP64 arrays and
   // the last one writes them.
