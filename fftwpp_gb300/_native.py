@@ -103,6 +103,10 @@ def load():
     lib.fgb_fft_destroy.argtypes = [vp]
     lib.fgb_set_autotune.restype = None
     lib.fgb_set_autotune.argtypes = [ctypes.c_int]
+    lib.fgb_set_drop_in_precision.restype = ctypes.c_int
+    lib.fgb_set_drop_in_precision.argtypes = [ctypes.c_int]
+    lib.fgb_get_drop_in_precision.restype = ctypes.c_int
+    lib.fgb_get_drop_in_precision.argtypes = []
     lib.fgb_set_zero_copy.restype = None
     lib.fgb_set_zero_copy.argtypes = [ctypes.c_int]
     lib.fgb_destroy.restype = None

@@ -40,6 +40,10 @@ namespace {
 
 size_t maxthreads=1;
 
+// Arithmetic of the FFTW++-compatible creators (their arrays are FP64):
+// FP64 or float-float (fgb_set_drop_in_precision).
+int dropInPrec=PREC_F64;
+
 // Host allocations handed out by create_*Align: page-locked when a GPU is
 // present, else posix_memalign; remembered so delete_* frees correctly.
 std::mutex allocMutex;
@@ -154,7 +158,7 @@ fgb_conv *makeDot(int dim, const int *kinds, const long *L, size_t pairs,
   for(int d=0; d < dim; ++d) Ms[d]=defaultM(kinds[d],L[d]);
   int K=(int) std::min<size_t>(pairs,FGB_MAXA/2);
   fgb_conv *c=make(dim,kinds,L,Ms,NULL,2*K,1,
-                   hermitian ? MULT_REALDOT : MULT_DOT,PREC_F64,1,where);
+                   hermitian ? MULT_REALDOT : MULT_DOT,dropInPrec,1,where);
   if(c) c->pairs=pairs;
   return c;
 }
@@ -370,7 +374,7 @@ void *fftwpp_create_conv1d(size_t L)
 {
   int k[]={KIND_PAD};
   long Ls[]={(long) L}, Ms[]={defaultM(KIND_PAD,L)};
-  return make(1,k,Ls,Ms,NULL,2,1,MULT_BINARY,PREC_F64,1,"fftwpp_create_conv1d");
+  return make(1,k,Ls,Ms,NULL,2,1,MULT_BINARY,dropInPrec,1,"fftwpp_create_conv1d");
 }
 void fftwpp_conv1d_delete(void *c) {destroy((fgb_conv *) c);}
 void fftwpp_conv1d_convolve(void *c, void *a, void *b)
@@ -382,7 +386,7 @@ void *fftwpp_create_hconv1d(size_t L)
 {
   int k[]={KIND_HERMITIAN};
   long Ls[]={(long) L}, Ms[]={defaultM(KIND_HERMITIAN,L)};
-  return make(1,k,Ls,Ms,NULL,2,1,MULT_REALBINARY,PREC_F64,1,
+  return make(1,k,Ls,Ms,NULL,2,1,MULT_REALBINARY,dropInPrec,1,
               "fftwpp_create_hconv1d");
 }
 void fftwpp_hconv1d_delete(void *c) {destroy((fgb_conv *) c);}
@@ -397,7 +401,7 @@ void *fftwpp_create_conv2d(size_t Lx, size_t Ly)
   int k[]={KIND_PAD,KIND_PAD};
   long Ls[]={(long) Lx,(long) Ly};
   long Ms[]={defaultM(KIND_PAD,Lx),defaultM(KIND_PAD,Ly)};
-  return make(2,k,Ls,Ms,NULL,2,1,MULT_BINARY,PREC_F64,1,"fftwpp_create_conv2d");
+  return make(2,k,Ls,Ms,NULL,2,1,MULT_BINARY,dropInPrec,1,"fftwpp_create_conv2d");
 }
 void fftwpp_conv2d_delete(void *c) {destroy((fgb_conv *) c);}
 void fftwpp_HermitianSymmetrizeX(size_t Hx, size_t Hy, size_t x0, double *f)
@@ -414,7 +418,7 @@ void *fftwpp_create_hconv2d(size_t Lx, size_t Ly)
   int k[]={KIND_CENTERED,KIND_HERMITIAN};
   long Ls[]={(long) Lx,(long) Ly};
   long Ms[]={defaultM(KIND_CENTERED,Lx),defaultM(KIND_HERMITIAN,Ly)};
-  return make(2,k,Ls,Ms,NULL,2,1,MULT_REALBINARY,PREC_F64,1,
+  return make(2,k,Ls,Ms,NULL,2,1,MULT_REALBINARY,dropInPrec,1,
               "fftwpp_create_hconv2d");
 }
 void fftwpp_hconv2d_delete(void *c) {destroy((fgb_conv *) c);}
@@ -428,7 +432,7 @@ void *fftwpp_create_conv3d(size_t Lx, size_t Ly, size_t Lz)
   int k[]={KIND_PAD,KIND_PAD,KIND_PAD};
   long Ls[]={(long) Lx,(long) Ly,(long) Lz};
   long Ms[]={defaultM(KIND_PAD,Lx),defaultM(KIND_PAD,Ly),defaultM(KIND_PAD,Lz)};
-  return make(3,k,Ls,Ms,NULL,2,1,MULT_BINARY,PREC_F64,1,"fftwpp_create_conv3d");
+  return make(3,k,Ls,Ms,NULL,2,1,MULT_BINARY,dropInPrec,1,"fftwpp_create_conv3d");
 }
 void fftwpp_conv3d_delete(void *c) {destroy((fgb_conv *) c);}
 void fftwpp_HermitianSymmetrizeXY(size_t Hx, size_t Hy, size_t Hz, size_t x0,
@@ -447,7 +451,7 @@ void *fftwpp_create_hconv3d(size_t Lx, size_t Ly, size_t Lz)
   long Ls[]={(long) Lx,(long) Ly,(long) Lz};
   long Ms[]={defaultM(KIND_CENTERED,Lx),defaultM(KIND_CENTERED,Ly),
              defaultM(KIND_HERMITIAN,Lz)};
-  return make(3,k,Ls,Ms,NULL,2,1,MULT_REALBINARY,PREC_F64,1,
+  return make(3,k,Ls,Ms,NULL,2,1,MULT_REALBINARY,dropInPrec,1,
               "fftwpp_create_hconv3d");
 }
 void fftwpp_hconv3d_delete(void *c) {destroy((fgb_conv *) c);}
@@ -675,6 +679,19 @@ int fgb_info(const fgb_conv *c, long *info)
 }
 
 void fgb_set_autotune(int on) {Conv::setAutotune(on != 0);}
+
+int fgb_set_drop_in_precision(int precision)
+{
+  if(precision != PREC_F64 && precision != PREC_FF) {
+    report("fgb_set_drop_in_precision","the FFTW++-compatible entry points "
+           "take FP64 arrays: FGB_F64 or FGB_FF");
+    return -1;
+  }
+  dropInPrec=precision;
+  return 0;
+}
+
+int fgb_get_drop_in_precision(void) {return dropInPrec;}
 void fgb_set_zero_copy(int on) {Conv::setZeroCopy(on != 0);}
 
 int fgb_set_normalize(fgb_conv *c, int normalize)

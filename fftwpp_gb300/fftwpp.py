@@ -20,7 +20,8 @@ import numpy as np
 from . import _native
 
 __all__ = ["Convolution", "HConvolution", "complex_align",
-           "fftwpp_set_maxthreads", "fftwpp_get_maxthreads"]
+           "fftwpp_set_maxthreads", "fftwpp_get_maxthreads",
+           "set_drop_in_precision"]
 
 
 def complex_align(shape):
@@ -39,6 +40,15 @@ def fftwpp_set_maxthreads(nthreads):
 
 def fftwpp_get_maxthreads():
     return _native.load().get_fftwpp_maxthreads()
+
+
+def set_drop_in_precision(precision: str = "f64"):
+    """Arithmetic of convolutions created afterwards (their arrays stay
+    complex128): "f64" (default) or "ff" (float-float, FP64-grade accuracy,
+    about 3x faster on GB300).  Not in the reference module."""
+    code = {"f64": _native.F64, "ff": _native.FF}.get(precision)
+    if code is None or _native.load().fgb_set_drop_in_precision(code) != 0:
+        raise ValueError("precision must be 'f64' or 'ff'")
 
 
 def _check(a, shape):

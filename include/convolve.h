@@ -282,7 +282,7 @@ protected:
       inner *= (size_t) axes[d]->inputLength();
     }
     plan=fgb_create(dim,kinds,L,M,m,(int) A,(int) B,
-                    multiplierCode(app.mult),FGB_F64,1);
+                    multiplierCode(app.mult),fgb_get_drop_in_precision(),1);
     if(!plan) throw std::runtime_error(fgb_last_error());
     long info[32];
     fgb_info(plan,info);

@@ -193,3 +193,13 @@ def test_misaligned_arrays_refused(native_lib):
     assert lib.fgb_hconv2d_convolve_noalloc(4096 + 8, 8192, 12288, 63, 63,
                                             None) != 0
     assert "aligned" in _native.last_error()
+
+
+def test_drop_in_precision_switch(native_lib):
+    lib = native_lib
+    assert lib.fgb_get_drop_in_precision() == 0
+    assert lib.fgb_set_drop_in_precision(1) == -1        # FP32 arrays differ
+    assert lib.fgb_set_drop_in_precision(2) == 0
+    assert lib.fgb_get_drop_in_precision() == 2
+    assert lib.fgb_set_drop_in_precision(0) == 0
+    assert lib.fgb_get_drop_in_precision() == 0

@@ -184,3 +184,23 @@ def test_golden_reference_outputs(native_lib):
             assert err <= tol, (c["key"], prec, err)
         seen += 1
     assert seen >= 500
+
+
+def test_drop_in_float_float(native_lib):
+    """The FFTW++-compatible entry points in float-float mode: same arrays,
+    FP64-grade results."""
+    from fftwpp_gb300 import fftwpp
+    Lx = Ly = 63
+    kinds = [H.CENTERED, H.HERMITIAN]
+    fs = _inputs(kinds, [Lx, Ly], 2, seed=31)
+    want = H.convolve(fs, kinds, [Lx, Ly], [94, 94], mult="realbinary")[0]
+    try:
+        fftwpp.set_drop_in_precision("ff")
+        c = fftwpp.HConvolution(fs[0].shape)
+        f, g = fs[0].copy(), fs[1].copy()
+        c.convolve(f, g)
+    finally:
+        fftwpp.set_drop_in_precision("f64")
+    assert rel_l2(f, want) <= 1e-13
+    with pytest.raises(ValueError):
+        fftwpp.set_drop_in_precision("f32")
