@@ -101,6 +101,8 @@ def load():
     lib.fgb_fft_execute_device.argtypes = [vp, vp, vp, vp]
     lib.fgb_fft_destroy.restype = None
     lib.fgb_fft_destroy.argtypes = [vp]
+    lib.fgb_debug_fail_allocation_after.restype = None
+    lib.fgb_debug_fail_allocation_after.argtypes = [ctypes.c_long]
     lib.fgb_set_autotune.restype = None
     lib.fgb_set_autotune.argtypes = [ctypes.c_int]
     lib.fgb_set_drop_in_precision.restype = ctypes.c_int

@@ -174,7 +174,7 @@ double BatchConv::timeLaunch(int reps)
   bool ok=cudaStreamCreateWithFlags(&s,cudaStreamNonBlocking) == cudaSuccess &&
     cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
   for(auto& p : bufs)
-    ok=ok && cudaMalloc(&p,bytes) == cudaSuccess &&
+    ok=ok && devAlloc((void **) &p,bytes) == cudaSuccess &&
       cudaMemsetAsync(p,0,bytes,s) == cudaSuccess;
   std::vector<float> t;
   if(ok) ok=run(bufs.data(),bufs.data(),s) == cudaSuccess;
@@ -218,7 +218,7 @@ long BatchConv::tuned(long L, long M, const std::vector<long>& cand)
     std::vector<void *> bufs(A,NULL);
     bool ok=true;
     for(int a=0; a < A && ok; ++a)
-      ok=cudaMalloc(&bufs[a],bytes) == cudaSuccess &&
+      ok=devAlloc((void **) &bufs[a],bytes) == cudaSuccess &&
         cudaMemset(bufs[a],0,bytes) == cudaSuccess;
     cudaStream_t s;
     cudaEvent_t e0, e1;
@@ -333,7 +333,7 @@ void BatchConv::build()
     }
   }
   if(stagingBytes) {
-    if(cudaMalloc(&staging,stagingBytes) != cudaSuccess)
+    if(devAlloc((void **) &staging,stagingBytes) != cudaSuccess)
       throw std::runtime_error("batched staging allocation failed");
     stagingSize=stagingBytes;
   }
@@ -376,9 +376,9 @@ void BatchConv::build()
   probBytes=sizeof(BatchProblem<T>);
   nfwdOffset=offsetof(BatchProblem<T>,nfwd);
   size_t pb=sizeof(BatchProblem<T>)*n, tb=sizeof(BatchTask)*tasks.size();
-  if(cudaMalloc(&dProbs,pb) != cudaSuccess ||
-     cudaMalloc(&dTasks,tb) != cudaSuccess ||
-     cudaMalloc(&dCounters,sizeof(int)*(2+2*(size_t) n)) != cudaSuccess)
+  if(devAlloc((void **) &dProbs,pb) != cudaSuccess ||
+     devAlloc((void **) &dTasks,tb) != cudaSuccess ||
+     devAlloc((void **) &dCounters,sizeof(int)*(2+2*(size_t) n)) != cudaSuccess)
     throw std::runtime_error("batched plan allocation failed");
   cudaMemcpy(dProbs,probs.data(),pb,cudaMemcpyHostToDevice);
   cudaMemcpy(dTasks,tasks.data(),tb,cudaMemcpyHostToDevice);

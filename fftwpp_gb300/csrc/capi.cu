@@ -178,7 +178,7 @@ int convolveDot(fgb_conv *c, void *const *a, void *const *b,
   if(c->dotBuf.empty()) {
     c->dotBuf.assign(2*K+2,NULL);
     for(void *&p : c->dotBuf)
-      if(e == cudaSuccess) e=cudaMalloc(&p,bytes);
+      if(e == cudaSuccess) e=devAlloc((void **) &p,bytes);
     if(e != cudaSuccess) {
       for(void *&p : c->dotBuf) {if(p) cudaFree(p); p=NULL;}
       c->dotBuf.clear();
@@ -679,6 +679,8 @@ int fgb_info(const fgb_conv *c, long *info)
 }
 
 void fgb_set_autotune(int on) {Conv::setAutotune(on != 0);}
+
+void fgb_debug_fail_allocation_after(long n) {failAllocationAfter(n);}
 
 int fgb_set_drop_in_precision(int precision)
 {

@@ -2,6 +2,7 @@
 #include "engine.h"
 #include "kernels.cuh"
 
+#include <atomic>
 #include <climits>
 #include <cmath>
 #include <map>
@@ -84,6 +85,24 @@ std::string lastError() {return errorText;}
 void setLastError(const std::string& s) {errorText=s;}
 
 // ---------------------------------------------------------------------------
+// Device allocation with host-side failure injection.
+
+static std::atomic<long> allocCountdown(-1);
+
+void failAllocationAfter(long n) {allocCountdown=n;}
+
+cudaError_t devAlloc(void **p, size_t bytes)
+{
+  long c=allocCountdown.load();
+  while(c >= 0 && !allocCountdown.compare_exchange_weak(c,c-1)) {}
+  if(c == 0) {
+    *p=NULL;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p,bytes);
+}
+
+// ---------------------------------------------------------------------------
 // Twiddle tables.
 
 const void *twiddles(long n, int prec)
@@ -127,7 +146,7 @@ const void *twiddles(long n, int prec)
   if(prec == PREC_F64) {
     std::vector<double2> h(n);
     for(long t=0; t < n; ++t) h[t]=make_double2(c[t],s[t]);
-    if(cudaMalloc(&d,n*sizeof(double2)) != cudaSuccess) return NULL;
+    if(devAlloc((void **) &d,n*sizeof(double2)) != cudaSuccess) return NULL;
     cudaMemcpy(d,h.data(),n*sizeof(double2),cudaMemcpyHostToDevice);
   } else {
     std::vector<float4> h(n);
@@ -136,7 +155,7 @@ const void *twiddles(long n, int prec)
       h[t]=make_float4(hx,hy,(float) (c[t]-(double) hx),
                        (float) (s[t]-(double) hy));
     }
-    if(cudaMalloc(&d,n*sizeof(float4)) != cudaSuccess) return NULL;
+    if(devAlloc((void **) &d,n*sizeof(float4)) != cudaSuccess) return NULL;
     cudaMemcpy(d,h.data(),n*sizeof(float4),cudaMemcpyHostToDevice);
   }
   cache[key]=d;
@@ -560,9 +579,9 @@ void Conv::tune()
   cudaStream_t s=NULL;
   bool ok=cudaStreamCreateWithFlags(&s,cudaStreamNonBlocking) == cudaSuccess;
   for(auto& p : tin)
-    ok=ok && cudaMalloc(&p,bytes) == cudaSuccess &&
+    ok=ok && devAlloc((void **) &p,bytes) == cudaSuccess &&
       cudaMemsetAsync(p,0,bytes,s) == cudaSuccess;
-  for(auto& p : tout) ok=ok && cudaMalloc(&p,bytes) == cudaSuccess;
+  for(auto& p : tout) ok=ok && devAlloc((void **) &p,bytes) == cudaSuccess;
   const bool wasTiming=timing;
   ok=ok && enableTiming(true) == cudaSuccess;
   std::vector<int> keep;
@@ -631,7 +650,7 @@ void Conv::allocate()
   int A=I.A;
   auto get=[&](size_t bytes) {
     void *p=NULL;
-    if(cudaMalloc(&p,bytes) != cudaSuccess)
+    if(devAlloc((void **) &p,bytes) != cudaSuccess)
       throw std::runtime_error("device allocation of "+std::to_string(bytes)+
                                " bytes failed");
     bufs.push_back(p);
@@ -974,7 +993,7 @@ cudaError_t Conv::runHost(const void *const *in, void *const *out,
       // Narrow column segments would waste the link's lines: move the
       // arrays whole with the SMs and convolve in device memory.
       if(!hostIn &&
-         cudaMalloc(&hostIn,bytes*A) != cudaSuccess) return cudaErrorMemoryAllocation;
+         devAlloc((void **) &hostIn,bytes*A) != cudaSuccess) return cudaErrorMemoryAllocation;
       std::vector<void *> din(A);
       CopyArgs C;
       C.count=A; C.bytes=bytes;
@@ -995,7 +1014,7 @@ cudaError_t Conv::runHost(const void *const *in, void *const *out,
     }
   }
   if(!hostIn) {
-    if(cudaMalloc(&hostIn,bytes*A) != cudaSuccess) return cudaErrorMemoryAllocation;
+    if(devAlloc((void **) &hostIn,bytes*A) != cudaSuccess) return cudaErrorMemoryAllocation;
   }
   std::vector<void *> din(A), dout(B);
   for(int a=0; a < A; ++a) {

@@ -175,6 +175,13 @@ private:
 
 const void *twiddles(long n, int prec);
 
+// Every device allocation of the library goes through devAlloc.  Failure
+// injection for tests (host side): failAllocationAfter(n) makes the n-th
+// following allocation (0: the next one) fail as cudaMalloc would; -1
+// turns it off.
+cudaError_t devAlloc(void **p, size_t bytes);
+void failAllocationAfter(long n);
+
 std::string lastError();
 void setLastError(const std::string& s);
 

@@ -77,6 +77,12 @@ int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out);
 int fgb_set_drop_in_precision(int precision);
 int fgb_get_drop_in_precision(void);
 
+/* Failure injection for tests, on the host: the n-th following device
+ * allocation of the library (0: the next one) fails as cudaMalloc would, so
+ * error paths (NULL plans, released partial allocations) can be exercised;
+ * -1 turns it off. */
+void fgb_debug_fail_allocation_after(long n);
+
 /* Process-wide switch of the zero-copy host path (default on); 0 always
  * copies page-locked arrays in and out as well. */
 void fgb_set_zero_copy(int on);

@@ -204,3 +204,41 @@ def test_drop_in_float_float(native_lib):
     assert rel_l2(f, want) <= 1e-13
     with pytest.raises(ValueError):
         fftwpp.set_drop_in_precision("f32")
+
+
+def test_allocation_failures_are_reported(native_lib):
+    """Host-side failure injection: every device allocation of plan
+    creation fails in turn; creation reports it (or, for the autotuner's
+    scratch, falls back to the cost-model plan) and the library keeps
+    working afterwards."""
+    import torch
+    from fftwpp_gb300.gpu import BatchedConvolution, HybridConvolution
+    kinds, L, M = [H.CENTERED, H.HERMITIAN], [31, 31], [46, 46]
+    fs = _inputs(kinds, L, 2, seed=37)
+    want = H.convolve(fs, kinds, L, M, mult="realbinary")[0]
+    failures = 0
+    for k in range(12):
+        native_lib.fgb_debug_fail_allocation_after(k)
+        try:
+            conv = HybridConvolution(kinds, L, M, mult="realbinary")
+        except ValueError as e:
+            failures += 1
+            assert "allocation" in str(e) or "memory" in str(e), str(e)
+            continue
+        finally:
+            native_lib.fgb_debug_fail_allocation_after(-1)
+        ts = [torch.from_numpy(f).cuda() for f in fs]
+        got = conv.convolve(*ts)[0].cpu().numpy()
+        assert rel_l2(got, want) <= 1e-13
+    assert failures >= 1
+    for k in range(6):
+        native_lib.fgb_debug_fail_allocation_after(k)
+        try:
+            BatchedConvolution([100, 5000, 30])
+        except ValueError as e:
+            assert "allocation" in str(e) or "memory" in str(e), str(e)
+        finally:
+            native_lib.fgb_debug_fail_allocation_after(-1)
+    conv = HybridConvolution(kinds, L, M, mult="realbinary")
+    got = conv.convolve(*[torch.from_numpy(f).cuda() for f in fs])[0]
+    assert rel_l2(got.cpu().numpy(), want) <= 1e-13
