@@ -238,7 +238,7 @@ def cpu_oracle_rate(w, budget_s, max_convs, workers):
         fs = [f[0] for f in fs]
     n, t0 = 0, time.perf_counter()
     while n < max_convs:
-        H.convolve(fs, w["kinds"], w["L"], w["M"], mult=w["mult"],
+        H.convolve(fs, w["kinds"], w["L"], w["M"], ms=w.get("m"), mult=w["mult"],
                    workers=workers)
         n += 1
         if time.perf_counter() - t0 > budget_s:
@@ -349,17 +349,17 @@ def run_reference(args, w):
         fs = [f[0] for f in fs]
     # Bound the run: about 20 s of warm-up and 120 s of timed work at most.
     t0 = time.perf_counter()
-    H.convolve(fs, w["kinds"], w["L"], w["M"], mult=w["mult"],
+    H.convolve(fs, w["kinds"], w["L"], w["M"], ms=w.get("m"), mult=w["mult"],
                workers=workers)
     est = time.perf_counter() - t0
     nwarm = min(args.warmup, max(1, int(20.0 / est))) - 1
     ntimed = min(args.steps, max(1, int(120.0 / est)))
     for _ in range(nwarm):
-        H.convolve(fs, w["kinds"], w["L"], w["M"], mult=w["mult"],
+        H.convolve(fs, w["kinds"], w["L"], w["M"], ms=w.get("m"), mult=w["mult"],
                    workers=workers)
     t0 = time.perf_counter()
     for _ in range(ntimed):
-        H.convolve(fs, w["kinds"], w["L"], w["M"], mult=w["mult"],
+        H.convolve(fs, w["kinds"], w["L"], w["M"], ms=w.get("m"), mult=w["mult"],
                    workers=workers)
     dt = time.perf_counter() - t0
     value = ntimed / dt
@@ -445,7 +445,7 @@ def run_ours(args, w):
 
     prec = args.precision
     fs = synth_inputs(w, seed=1)
-    conv = HybridConvolution(w["kinds"], w["L"], w["M"], A=w["A"], B=w["B"],
+    conv = HybridConvolution(w["kinds"], w["L"], w["M"], m=w.get("m"), A=w["A"], B=w["B"],
                              mult=w["mult"], precision=prec,
                              batch=w.get("batch", 1))
     ts = [torch.from_numpy(f).to(conv.dtype).cuda() for f in fs]
@@ -487,7 +487,8 @@ def run_ours(args, w):
     if per_launch[dom] <= 0:
         raise RuntimeError("per-kernel timing recorded nothing")
     achieved = abytes / (per_launch[dom] * 1e-3) / 1e9
-    traffic = traffic_from_profiles(args.workload, names[dom], prec)
+    traffic = (None if w.get("custom") else
+               traffic_from_profiles(args.workload, names[dom], prec))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "kernel": names[dom], "peak_source": peak_src,
@@ -507,7 +508,8 @@ def run_ours(args, w):
     tag, rate, bound = (("DPINST", dfma, "fp64_issue") if prec == "f64" else
                         ("SPINST", ffma, "fp32_issue"))
     if rate:
-        cnt = [profile_figure(tag, args.workload, n, prec) for n in names]
+        cnt = [None if w.get("custom") else
+               profile_figure(tag, args.workload, n, prec) for n in names]
         compute = {"fp64_tflops_peak_measured": 2 * dfma / 1e12,
                    "fp32_tflops_peak_measured": 2 * ffma / 1e12}
         if cnt[dom]:
@@ -530,7 +532,7 @@ def run_ours(args, w):
     big = np.prod([l for l in w["L"]]) > 5e6
     want = None
     if w.get("batch", 1) == 1 and not big:
-        want = H.convolve(fs, w["kinds"], w["L"], w["M"], mult=w["mult"],
+        want = H.convolve(fs, w["kinds"], w["L"], w["M"], ms=w.get("m"), mult=w["mult"],
                           workers=os.cpu_count() or 1)[0]
     got0 = outs[0].cpu().numpy()
     if want is not None:
@@ -544,7 +546,7 @@ def run_ours(args, w):
     if not args.quick and prec == "f64":
         # The FP32-compensated and float-float modes on the same workload.
         for other, key in (("f32", "fp32_compensated"), ("ff", "float_float")):
-            co = HybridConvolution(w["kinds"], w["L"], w["M"], A=w["A"],
+            co = HybridConvolution(w["kinds"], w["L"], w["M"], m=w.get("m"), A=w["A"],
                                    B=w["B"], mult=w["mult"], precision=other,
                                    batch=w.get("batch", 1))
             to = [torch.from_numpy(f).to(co.dtype).cuda() for f in fs]
@@ -922,6 +924,34 @@ def run_batched(args):
     return 0
 
 
+def override(w, args):
+    """The workload with -L/-M/-m applied (the reference and GPU arms take
+    the same parameters, as the reference's test programs do)."""
+    if not (args.L or args.M or args.m):
+        return w
+    w = dict(w)
+    dim = len(w["kinds"])
+
+    def ints(text):
+        v = [int(x) for x in text.split(",")]
+        if len(v) != dim:
+            raise SystemExit(f"expected {dim} comma-separated values")
+        return v
+    if args.L:
+        w["L"] = ints(args.L)
+        w["M"] = [3 * ((l + 1) // 2) - 2 * (l % 2)
+                  if k in (CENTERED, HERMITIAN) else 2 * l - 1
+                  for k, l in zip(w["kinds"], w["L"])]
+    if args.M:
+        w["M"] = ints(args.M)
+    if args.m:
+        w["m"] = ints(args.m)
+    w["custom"] = True         # the committed ncu figures do not apply
+    w["desc"] = (w["desc"] + f" [overridden: L={w['L']}, M={w['M']}"
+                 + (f", m={w['m']}" if args.m else "") + "]")
+    return w
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -932,6 +962,12 @@ def main():
                     choices=sorted(WORKLOADS) + ["batched1d"])
     ap.add_argument("--precision", default="f64", choices=["f64", "f32", "ff"])
     ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--L", help="comma-separated data lengths per axis, "
+                    "outermost first (the reference tests' -L)")
+    ap.add_argument("--M", help="comma-separated minimum padded lengths "
+                    "(-M; default: the workload's dealiasing rule)")
+    ap.add_argument("--m", help="comma-separated forced residue block "
+                    "lengths (-m; 0 = planner's choice)")
     ap.add_argument("--quick", action="store_true",
                     help="skip the FP32 comparison leg")
     args = ap.parse_args()
@@ -941,7 +977,7 @@ def main():
         if args.impl == "reference":
             return run_reference_batched(args)
         return run_batched(args)
-    w = WORKLOADS[args.workload]
+    w = override(WORKLOADS[args.workload], args)
     if args.impl == "reference":
         return run_reference(args, w)
     return run_ours(args, w)

@@ -147,12 +147,24 @@ __device__ __forceinline__ cplx<ff> cmulconj(cplx<ff> a, cplx<ff> b)
 template<typename T>
 __device__ __forceinline__ cplx<T> conjg(cplx<T> a) { return mk(a.x,-a.y); }
 
+// One step of a long running sum (folds over p blocks, accumulation over
+// q residues): float-float renormalises every step, since an unrenormalised
+// chain of hundreds of additions loses accuracy in its lo parts.
+template<typename T>
+__device__ __forceinline__ cplx<T> accum(cplx<T> a, cplx<T> b) { return a+b; }
+__device__ __forceinline__ cplx<ff> accum(cplx<ff> a, cplx<ff> b);
+
 // Renormalise a loaded value (float-float only).
 template<typename T>
 __device__ __forceinline__ cplx<T> nrm(cplx<T> a) { return a; }
 __device__ __forceinline__ cplx<ff> nrm(cplx<ff> a)
 {
   return mk(nrm(a.x),nrm(a.y));
+}
+
+__device__ __forceinline__ cplx<ff> accum(cplx<ff> a, cplx<ff> b)
+{
+  return nrm(a+b);
 }
 
 // s*i*a for s = +1 or -1 (compile time).

@@ -351,7 +351,7 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
       for(int s=s0; s < L; s += m) {
         cplx<T> v=fin[col*L+s];
         if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
-        sum=sum+v;
+        sum=accum(sum,v);
       }
       x[sp(i)]=sum;
     }
@@ -381,7 +381,7 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
       int t=posmod(s-c,m);
       cplx<T> v=Z[sp(t*ld+col)];
       if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
-      acc[i]=acc[i]+v;
+      acc[i]=accum(acc[i],v);
     }
     __syncthreads();
   }
@@ -579,7 +579,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
     for(int s=s0; s < L; s += m) {
       cplx<T> v=y[s*tile+cc];
       if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
-      sum=sum+v;
+      sum=accum(sum,v);
     }
     x[sp(i)]=sum;
   }
@@ -686,7 +686,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
       int t=posmod(s-c,m);
       cplx<T> v=X[sp(t*tile+cc)];
       if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
-      acc[i]=acc[i]+v;
+      acc[i]=accum(acc[i],v);
     }
     __syncthreads();
   }

@@ -89,6 +89,29 @@ class HybridConvolution:
         if batch > 1:
             self.shape = (batch,) + self.shape
 
+    def describe(self) -> str:
+        """The plan in words: the counterpart of the reference's verbose
+        dump (convolve.cc:451-469: m, p, q, C, S and the padding kind per
+        axis), plus the GPU launch schedule (column tiles, rows per CTA,
+        kernels, staging bytes)."""
+        names = {PAD: "fftPad", CENTERED: "fftPadCentered",
+                 HERMITIAN: "fftPadHermitian", REAL: "fftPadReal"}
+        lines = [f"{self.dim}D convolution, A={self.A} B={self.B} "
+                 f"multiplier={self.mult} precision={self.precision}"
+                 + (f" batch={self.batch}" if self.batch > 1 else "")]
+        for d, (k, ax) in enumerate(zip(self.kinds, self.axes)):
+            padding = "explicit" if ax["q"] == 1 else "hybrid"
+            inner = d == self.dim - 1 and not self.long_path
+            sched = (f"rows/CTA={self.rows_per_cta}" if inner else
+                     f"tile={ax['tile']} tileB={ax['tileB']}")
+            lines.append(f"  axis {d}: {names[k]} L={self.L[d]} M={self.M[d]} "
+                         f"m={ax['m']} p={ax['p']} q={ax['q']} N={ax['N']} "
+                         f"stored={ax['stored']} ({padding}) {sched}")
+        lines.append(f"  kernels: {', '.join(self.launch_names())}"
+                     f"{' (long 1D path)' if self.long_path else ''}")
+        lines.append(f"  staging: {self.staging_bytes} bytes")
+        return "\n".join(lines)
+
     # -- layout -------------------------------------------------------------
     @property
     def dtype(self):

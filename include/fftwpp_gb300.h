@@ -48,7 +48,10 @@ typedef struct fgb_conv fgb_conv;
 
 /* Plan a convolution.  kinds, L, M: per axis, outermost first.  m: NULL or
  * per-axis forced residue block length (0 = planner's choice), the
- * Application m of the reference (convolve.h:103-111).  batch > 1 runs
+ * Application m of the reference (convolve.h:103-111); a Hermitian axis is
+ * always transformed explicitly, at the padded length m q the reference
+ * would use for that m.  Plans are then autotuned (fgb_set_autotune); the
+ * results do not depend on m, tiles or rows per CTA.  batch > 1 runs
  * independent 1D problems stored back to back.  Replaces the constructors
  * fftPad*(L,M,app,...) + Convolution{,2,3}(...) (convolve.h:515-1603).
  * Returns NULL on error. */

@@ -257,3 +257,52 @@ def test_host_path_misaligned_pinned(native_lib):
         hs.append(a)
     conv.convolve_host(*hs)
     assert rel_l2(hs[0], want) <= 1e-13
+
+
+def _smooth(n):
+    for f in (2, 3, 5, 7):
+        while n % f == 0:
+            n //= f
+    return n == 1
+
+
+@pytest.mark.parametrize("precision", ["f64", "ff", "f32"])
+def test_analytic_kat_m_sweep(native_lib, precision):
+    """The reference's analytic known answer (tests/hybridconv.cc:13-14,
+    50-69: f_j = iF e^{ij}, g_j = iG e^{ij}, h_j = iF iG (j+1) e^{ij}) for
+    L = 2^6 .. 2^12, M = 2L, every forced residue block length m the row
+    kernel holds (the sweep of tests/accuracy.py:34-50)."""
+    import torch
+    from fftwpp_gb300.gpu import HybridConvolution
+    iF, iG = np.sqrt(3) + 1j * np.sqrt(7), np.sqrt(5) + 1j * np.sqrt(11)
+    tol = TOL[precision]
+    checked = 0
+    for e in range(6, 13):
+        L = 2 ** e
+        M = 2 * L
+        j = np.arange(L)
+        f = iF * np.exp(1j * j)
+        g = iG * np.exp(1j * j)
+        want = iF * iG * (j + 1) * np.exp(1j * j)
+        for m in [2 ** k for k in range(2, e + 2)]:
+            try:
+                conv = HybridConvolution([H.PAD], [L], [M], m=[m],
+                                         precision=precision)
+            except ValueError:
+                continue                  # beyond one CTA's shared memory
+            dt = conv.dtype
+            got = conv.convolve(torch.from_numpy(f).to(dt).cuda(),
+                                torch.from_numpy(g).to(dt).cuda())[0]
+            err = rel_l2(got.cpu().numpy().astype(np.complex128), want)
+            assert err <= tol, (L, m, err)
+            checked += 1
+    assert checked >= 30
+
+
+def test_describe_plan(native_lib):
+    from fftwpp_gb300.gpu import HybridConvolution
+    conv = HybridConvolution([H.CENTERED, H.HERMITIAN], [63, 63], [94, 94],
+                             mult="realbinary")
+    text = conv.describe()
+    assert "fftPadCentered" in text and "fftPadHermitian" in text
+    assert f"m={conv.axes[0]['m']}" in text and "kernels:" in text
