@@ -167,23 +167,33 @@ def test_python_wrapper_hconvolution(native_lib):
 
 def test_golden_reference_outputs(native_lib):
     """The GPU result equals the reference's own output (tests/golden/) on
-    every fixture: FP64 <= 1e-13, FP32-compensated <= 2e-6 relative L2."""
+    every fixture: FP64 and float-float <= 1e-13, FP32-compensated <= 2e-6
+    relative L2; and again with the residue block length the reference
+    itself chose forced (its m, hence its q), where the GPU kernels take it."""
     import torch
     from fftwpp_gb300.gpu import HybridConvolution
     from test_oracle import CASES
-    seen = 0
+    seen = forced = 0
     for c in CASES:
         A = len(c["ins"])
-        for prec, tol in (("f64", 1e-13), ("f32", 2e-6)):
-            conv = HybridConvolution(c["kinds"], c["L"], c["M"], A=A, B=1,
-                                     mult=c["mult"], precision=prec)
-            ts = [torch.from_numpy(np.ascontiguousarray(f)).to(conv.dtype)
-                  .cuda() for f in c["ins"]]
-            got = conv.convolve(*ts)[0].cpu().numpy()
-            err = rel_l2(got, c["out"])
-            assert err <= tol, (c["key"], prec, err)
+        ref_m = [int(v) for v in c["info"][:, 0]]
+        for prec, tol in (("f64", 1e-13), ("ff", 1e-13), ("f32", 2e-6)):
+            for m in (None, ref_m):
+                try:
+                    conv = HybridConvolution(c["kinds"], c["L"], c["M"], m=m,
+                                             A=A, B=1, mult=c["mult"],
+                                             precision=prec)
+                except ValueError:
+                    assert m is not None     # only a forced m may not fit
+                    continue
+                ts = [torch.from_numpy(np.ascontiguousarray(f))
+                      .to(conv.dtype).cuda() for f in c["ins"]]
+                got = conv.convolve(*ts)[0].cpu().numpy()
+                err = rel_l2(got, c["out"])
+                assert err <= tol, (c["key"], prec, m, err)
+                forced += m is not None
         seen += 1
-    assert seen >= 500
+    assert seen >= 500 and forced >= 1000
 
 
 def test_drop_in_float_float(native_lib):
