@@ -637,7 +637,8 @@ def run_ours(args, w):
         "config": {"workload": w["desc"], "precision": prec,
                    "parallelism": f"replicas x{world}",
                    "l2": "flushed (256 MB write) before every timed step",
-                   "plan": conv.axes, "rows_per_cta": conv.rows_per_cta},
+                   "plan": conv.axes, "rows_per_cta": conv.rows_per_cta,
+                   "threads_per_cta": conv.threads_per_cta},
         "roofline": roofline,
         "compute_roofline": compute,
         "kernels_ms_per_step": dict(zip(names, per_launch)),

@@ -675,6 +675,7 @@ int fgb_info(const fgb_conv *c, long *info)
   info[26]=I.longRow ? 1 : 0;
   for(int d=0; d < I.dim; ++d) info[27+d]=I.axis[d].tileB;
   info[30]=I.axis[I.dim-1].rpc;
+  info[31]=I.axis[I.dim-1].thr;
   return 0;
 }
 

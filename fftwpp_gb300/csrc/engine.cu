@@ -453,6 +453,7 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
     a.stored=a.kind == KIND_HERMITIAN ? (long) ceilquotient(a.L,2) : a.L;
     a.tile=a.tileB=1;
     a.rpc=1;
+    a.thr=a.thrB=256;
     a.rows=0;
   }
   if(dim > 1 && batch != 1)
@@ -522,7 +523,14 @@ void Conv::setAutotune(bool on) {autotune=on;}
 
 void Conv::tune()
 {
-  struct Tunable {int *param; std::vector<int> cands; int launch;};
+  // A launch's tunables: one schedule parameter (rows per CTA or column
+  // tile) and its threads per CTA, tried as pairs.
+  struct Tunable {
+    int *param, *thr;
+    std::vector<std::pair<int,int>> cands;
+    int launch;
+  };
+  const int thrs[]={128,256};
   std::vector<Tunable> tn;
   const int dim=I.dim, prec=I.prec, A=I.A, B=I.B;
   AxisPlan& in=I.axis[dim-1];
@@ -533,6 +541,7 @@ void Conv::tune()
   {
     Tunable t;
     t.param=&in.rpc;
+    t.thr=&in.thr;
     t.launch=I.longRow ? 1 : dim-1;
     long avail=I.longRow ? I.rowQ : nrows;
     for(int r : {1,2,3,4,6,8}) {
@@ -540,7 +549,8 @@ void Conv::tune()
       size_t need=I.longRow ? rowNeed(prec,I.rowM,I.rowM,A,B,r) :
         in.kind == KIND_HERMITIAN ? hermNeed(prec,in.stored,in.N/2,A,r) :
         rowNeed(prec,in.stored,in.m,A,B,r);
-      if(need <= SMEM_MAX) t.cands.push_back(r);
+      if(need <= SMEM_MAX)
+        for(int th : thrs) t.cands.push_back({r,th});
     }
     if(t.cands.size() > 1) tn.push_back(t);
   }
@@ -553,6 +563,8 @@ void Conv::tune()
       Tunable f, b;
       f.param=&a.tile;
       b.param=&a.tileB;
+      f.thr=&a.thr;
+      b.thr=&a.thrB;
       f.launch=d;
       b.launch=2*(dim-1)-d;
       for(int t=1; t <= (wide(prec) ? 8 : 16) && t <= C; t *= 2) {
@@ -564,8 +576,10 @@ void Conv::tune()
           sb=FGB_BY_PREC(prec,outerBwdSmem,a.L,a.m,t,(int) a.q,
                          (int) (a.p == 1));
         }
-        if(sf <= SMEM_MAX) f.cands.push_back(t);
-        if(sb <= SMEM_MAX) b.cands.push_back(t);
+        for(int th : thrs) {
+          if(sf <= SMEM_MAX) f.cands.push_back({t,th});
+          if(sb <= SMEM_MAX) b.cands.push_back({t,th});
+        }
       }
       if(f.cands.size() > 1) tn.push_back(f);
       if(b.cands.size() > 1) tn.push_back(b);
@@ -584,8 +598,8 @@ void Conv::tune()
   for(auto& p : tout) ok=ok && devAlloc((void **) &p,bytes) == cudaSuccess;
   const bool wasTiming=timing;
   ok=ok && enableTiming(true) == cudaSuccess;
-  std::vector<int> keep;
-  for(auto& t : tn) keep.push_back(*t.param);
+  std::vector<std::pair<int,int>> keep;
+  for(auto& t : tn) keep.push_back({*t.param,*t.thr});
   if(ok) {
     size_t K=0;
     for(auto& t : tn) K=std::max(K,t.cands.size());
@@ -593,7 +607,11 @@ void Conv::tune()
                                         std::vector<double>(K,1e300));
     std::vector<double> lt(nlaunch);
     for(size_t k=0; k < K && ok; ++k) {
-      for(auto& t : tn) *t.param=t.cands[std::min(k,t.cands.size()-1)];
+      for(auto& t : tn) {
+        const auto& c=t.cands[std::min(k,t.cands.size()-1)];
+        *t.param=c.first;
+        *t.thr=c.second;
+      }
       for(int rep=0; rep < 3 && ok; ++rep) {
         ok=run(tin.data(),tout.data(),s) == cudaSuccess &&
           cudaStreamSynchronize(s) == cudaSuccess;
@@ -614,7 +632,10 @@ void Conv::tune()
       }
   }
   // The planner's choice stays wherever timing failed.
-  for(size_t i=0; i < tn.size(); ++i) *tn[i].param=keep[i];
+  for(size_t i=0; i < tn.size(); ++i) {
+    *tn[i].param=keep[i].first;
+    *tn[i].thr=keep[i].second;
+  }
   timing=wasTiming;
   cudaGetLastError();
   if(s) cudaStreamSynchronize(s);
@@ -757,7 +778,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
       P.rowStride=a.stored; P.nrows=batch; P.scale=(T) scale;
       P.io64=IN64 | OUT64;
-      e=launchHermRow<T>(P,threads,batch,s);
+      e=launchHermRow<T>(P,a.thr,batch,s);
       tick(s);
       return e;
     }
@@ -767,7 +788,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
     P.rowStride=a.stored; P.nrows=batch; P.scale=(T) scale;
     P.io64=IN64 | OUT64;
-    e=launchRow<T>(P,threads,batch,s);
+    e=launchRow<T>(P,a.thr,batch,s);
     tick(s);
     return e;
   }
@@ -800,7 +821,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
     P.rowStride=m; P.nrows=q; P.scale=(T) 1;
-    e=launchRow<T>(P,threads,q,s);
+    e=launchRow<T>(P,a.thr,q,s);
     tick(s);
     if(e != cudaSuccess) return e;
     O.count=B;
@@ -825,8 +846,8 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.scale=(T) 1;
     O.io64=IN64;
     for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) bufs[i];}
-    e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(O,threads,s) :
-      launchOuterFwd<T>(O,threads,s);
+    e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(O,ax.thr,s) :
+      launchOuterFwd<T>(O,ax.thr,s);
     tick(s);
     if(e != cudaSuccess) return e;
     if(ay.kind == KIND_HERMITIAN) {
@@ -835,14 +856,14 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
       for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
       P.rowStride=C; P.nrows=ax.rows; P.scale=(T) 1;
-      e=launchHermRow<T>(P,threads,ax.rows,s);
+      e=launchHermRow<T>(P,ay.thr,ax.rows,s);
     } else {
       RowPlan<T> P;
       rowPlan(P,ay);
       for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
       P.rowStride=C; P.nrows=ax.rows; P.scale=(T) 1;
-      e=launchRow<T>(P,threads,ax.rows,s);
+      e=launchRow<T>(P,ay.thr,ax.rows,s);
     }
     tick(s);
     if(e != cudaSuccess) return e;
@@ -851,8 +872,8 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.scale=(T) scale;
     O.io64=OUT64;
     for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) bufs[i]; O.out[i]=(Cx *) out[i];}
-    e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(O,threads,s) :
-      launchOuterBwd<T>(O,threads,s);
+    e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(O,ax.thrB,s) :
+      launchOuterBwd<T>(O,ax.thrB,s);
     tick(s);
     return e;
   }
@@ -873,8 +894,8 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   X.scale=(T) 1;
   X.io64=IN64;
   for(int i=0; i < A; ++i) {X.in[i]=(const Cx *) in[i]; X.out[i]=(Cx *) bx[i];}
-  e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(X,threads,s) :
-    launchOuterFwd<T>(X,threads,s);
+  e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(X,ax.thr,s) :
+    launchOuterFwd<T>(X,ax.thr,s);
   tick(s);
   if(e != cudaSuccess) return e;
 
@@ -885,7 +906,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   Y.inRow=nz; Y.outRow=nz; Y.C=(int) nz; Y.Ltot=(long long) ay.L*nz;
   Y.scale=(T) 1;
   for(int i=0; i < A; ++i) {Y.in[i]=(const Cx *) bx[i]; Y.out[i]=(Cx *) by[i];}
-  e=launchOuterFwd<T>(Y,threads,s);
+  e=launchOuterFwd<T>(Y,ay.thr,s);
   tick(s);
   if(e != cudaSuccess) return e;
 
@@ -896,14 +917,14 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) by[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) by[i];
     P.rowStride=nz; P.nrows=nrows; P.scale=(T) 1;
-    e=launchHermRow<T>(P,threads,nrows,s);
+    e=launchHermRow<T>(P,az.thr,nrows,s);
   } else {
     RowPlan<T> P;
     rowPlan(P,az);
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) by[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) by[i];
     P.rowStride=nz; P.nrows=nrows; P.scale=(T) 1;
-    e=launchRow<T>(P,threads,nrows,s);
+    e=launchRow<T>(P,az.thr,nrows,s);
   }
   tick(s);
   if(e != cudaSuccess) return e;
@@ -912,7 +933,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   Y.tile=ay.tileB;
   for(int i=0; i < B; ++i) {Y.in[i]=(const Cx *) by[i]; Y.out[i]=(Cx *) bx[i];}
   std::swap(Y.inBatch,Y.outBatch);
-  e=launchOuterBwd<T>(Y,threads,s);
+  e=launchOuterBwd<T>(Y,ay.thrB,s);
   tick(s);
   if(e != cudaSuccess) return e;
 
@@ -921,8 +942,8 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   X.scale=(T) scale;
   X.io64=OUT64;
   for(int i=0; i < B; ++i) {X.in[i]=(const Cx *) bx[i]; X.out[i]=(Cx *) out[i];}
-  e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(X,threads,s) :
-    launchOuterBwd<T>(X,threads,s);
+  e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(X,ax.thrB,s) :
+    launchOuterBwd<T>(X,ax.thrB,s);
   tick(s);
   return e;
 }

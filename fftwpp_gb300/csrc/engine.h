@@ -35,6 +35,8 @@ struct AxisPlan {
   int cshift;         // centred origin offset
   int tile, tileB;    // outer kernels: columns per CTA (forward, backward)
   int rpc;            // innermost axis: rows per CTA of the row kernel
+  int thr, thrB;      // threads per CTA of the forward (or row) and the
+                      // backward launch of this axis
   long rows;          // outer axis: rows produced (N, or N/2+1 if real)
 };
 

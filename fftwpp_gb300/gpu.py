@@ -85,6 +85,7 @@ class HybridConvolution:
         self.staging_bytes = info[25]
         self.long_path = bool(info[26])
         self.rows_per_cta = info[30]
+        self.threads_per_cta = info[31]
         self.shape = tuple(ax["stored"] for ax in self.axes)
         if batch > 1:
             self.shape = (batch,) + self.shape
@@ -102,7 +103,8 @@ class HybridConvolution:
         for d, (k, ax) in enumerate(zip(self.kinds, self.axes)):
             padding = "explicit" if ax["q"] == 1 else "hybrid"
             inner = d == self.dim - 1 and not self.long_path
-            sched = (f"rows/CTA={self.rows_per_cta}" if inner else
+            sched = (f"rows/CTA={self.rows_per_cta} "
+                     f"threads/CTA={self.threads_per_cta}" if inner else
                      f"tile={ax['tile']} tileB={ax['tileB']}")
             lines.append(f"  axis {d}: {names[k]} L={self.L[d]} M={self.M[d]} "
                          f"m={ax['m']} p={ax['p']} q={ax['q']} N={ax['N']} "

@@ -94,7 +94,8 @@ void fgb_set_zero_copy(int on);
  * length, centred offset, outer tile, rows produced.  info[24] = kernels per
  * convolution, info[25] = staging bytes, info[26] = 1 if the 1D long path
  * is used, info[27+d] = backward tile of axis d, info[30] = rows per CTA of
- * the innermost-axis kernel (info holds 32 longs).  Mirrors the public members m,p,q,M of fftBase
+ * the innermost-axis kernel, info[31] = its threads per CTA (info holds 32
+ * longs).  Mirrors the public members m,p,q,M of fftBase
  * (convolve.h:123-145). */
 int fgb_info(const fgb_conv *c, long *info);
 
