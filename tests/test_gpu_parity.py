@@ -306,3 +306,50 @@ def test_describe_plan(native_lib):
     text = conv.describe()
     assert "fftPadCentered" in text and "fftPadHermitian" in text
     assert f"m={conv.axes[0]['m']}" in text and "kernels:" in text
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-13), ("ff", 1e-13),
+                                           ("f32", 2e-6)])
+def test_full_size_properties_2d(native_lib, precision, tol):
+    """At the 2D benchmark size (1023 x 512 centred-Hermitian modes,
+    M = 1534): linearity in each argument and symmetry, properties that hold
+    at any size without an oracle run."""
+    import torch
+    from fftwpp_gb300.gpu import HybridConvolution
+    kinds, L, M = [H.CENTERED, H.HERMITIAN], [1023, 1023], [1534, 1534]
+    f, g1, g2 = _inputs(kinds, L, 3, seed=41)
+    conv = HybridConvolution(kinds, L, M, mult="realbinary",
+                             precision=precision)
+    dt = conv.dtype
+
+    def run(a, b):
+        ta = torch.from_numpy(np.ascontiguousarray(a)).to(dt).cuda()
+        tb = torch.from_numpy(np.ascontiguousarray(b)).to(dt).cuda()
+        return conv.convolve(ta, tb)[0].cpu().numpy().astype(np.complex128)
+    h1, h2, h12 = run(f, g1), run(f, g2), run(f, 2.0 * g1 - 0.5 * g2)
+    assert rel_l2(h12, 2.0 * h1 - 0.5 * h2) <= tol
+    assert rel_l2(run(g1, f), h1) <= tol
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-13), ("ff", 1e-13),
+                                           ("f32", 2e-6)])
+def test_full_size_properties_3d_real(native_lib, precision, tol):
+    """At the 3D benchmark size (two 256^3 real fields, M = 511):
+    linearity and symmetry."""
+    import torch
+    from fftwpp_gb300.gpu import HybridConvolution
+    kinds, L, M = [H.REAL, H.PAD, H.PAD], [256, 256, 256], [511, 511, 511]
+    rng = np.random.default_rng(43)
+    f, g1, g2 = (rng.normal(size=(256, 256, 256)) for _ in range(3))
+    conv = HybridConvolution(kinds, L, M, precision=precision)
+    dt = conv.dtype
+
+    def run(a, b):
+        ta = torch.from_numpy(a).to(dt).cuda()
+        tb = torch.from_numpy(b).to(dt).cuda()
+        return conv.convolve(ta, tb)[0].cpu().numpy().astype(np.float64)
+    h1 = run(f, g1)
+    h12 = run(f, g1 + 3.0 * g2)
+    h2 = run(f, g2)
+    assert rel_l2(h12, h1 + 3.0 * h2) <= tol
+    assert rel_l2(run(g1, f), h1) <= tol
