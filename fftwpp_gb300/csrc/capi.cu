@@ -696,6 +696,7 @@ int fgb_set_drop_in_precision(int precision)
 
 int fgb_get_drop_in_precision(void) {return dropInPrec;}
 void fgb_set_zero_copy(int on) {Conv::setZeroCopy(on != 0);}
+void fgb_set_host_path(int mode) {Conv::setHostPath(mode);}
 
 int fgb_set_normalize(fgb_conv *c, int normalize)
 {

@@ -4,6 +4,7 @@
 
 #include <atomic>
 #include <climits>
+#include <cstring>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -407,7 +408,8 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
 Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
            const long *mForce, int A, int B, int mult, int prec, long batch)
   : batch(batch), staging(0), hostIn(NULL), hostOut(NULL), nlaunch(0),
-    timing(false), normalize(true), marks(0)
+    timing(false), normalize(true), marks(0), hostTile(0), hostThr(0),
+    hostTileB(0), hostThrB(0), hostDirect(-1)
 {
   if(dim < 1 || dim > 3) throw std::runtime_error("dimension must be 1, 2 or 3");
   if(A < 1 || A > FGB_MAXA || B < 1 || B > A)
@@ -623,12 +625,24 @@ void Conv::tune()
             ms[i][k]=std::min(ms[i][k],lt[tn[i].launch]);
       }
     }
+    const size_t e=elemBytes();
+    AxisPlan& a0=I.axis[0];
     if(ok)
       for(size_t i=0; i < tn.size(); ++i) {
         size_t bk=0;
         for(size_t k=1; k < tn[i].cands.size(); ++k)
           if(ms[i][k] < ms[i][bk]) bk=k;
         keep[i]=tn[i].cands[bk];
+        // The fastest axis-0 tile whose rows are whole 64-byte host lines.
+        if(tn[i].param != &a0.tile && tn[i].param != &a0.tileB) continue;
+        long hk=-1;
+        for(size_t k=0; k < tn[i].cands.size(); ++k)
+          if((size_t) tn[i].cands[k].first*e >= 64 &&
+             (hk < 0 || ms[i][k] < ms[i][hk])) hk=k;
+        if(hk < 0) continue;
+        const bool fwd=tn[i].param == &a0.tile;
+        (fwd ? hostTile : hostTileB)=tn[i].cands[hk].first;
+        (fwd ? hostThr : hostThrB)=tn[i].cands[hk].second;
       }
   }
   // The planner's choice stays wherever timing failed.
@@ -959,6 +973,8 @@ cudaError_t Conv::run(const void *const *in, void *const *out, cudaStream_t s)
 
 bool Conv::zeroCopy=true;
 void Conv::setZeroCopy(bool on) {zeroCopy=on;}
+int Conv::hostPath=-1;
+void Conv::setHostPath(int mode) {hostPath=mode < 0 ? -1 : mode > 0;}
 
 // The device address of page-locked host memory, or NULL for memory the GPU
 // cannot address directly.
@@ -983,15 +999,97 @@ bool Conv::directSegments() const
   return (size_t) a.tile*e >= 64 && (size_t) a.tileB*e >= 64;
 }
 
+// In place over the host link: the first kernel reads the caller's arrays
+// and the last one writes them, so the transfers overlap the transforms.
+// Axis 0 takes its host-line tiles where the device-tuned ones are narrower.
+cudaError_t Conv::runDirect(const void *const *in, void *const *out,
+                            cudaStream_t s)
+{
+  AxisPlan& a=I.axis[0];
+  const int keep[4]={a.tile,a.thr,a.tileB,a.thrB};
+  if(!directSegments()) {
+    a.tile=hostTile; a.thr=hostThr;
+    a.tileB=hostTileB; a.thrB=hostThrB;
+  }
+  cudaError_t e=run(in,out,s);
+  a.tile=keep[0]; a.thr=keep[1];
+  a.tileB=keep[2]; a.thrB=keep[3];
+  return e;
+}
+
+// Whole arrays moved by the SMs (16-byte aligned mapped pointers, sizes a
+// multiple of 16 bytes), convolved in device memory.
+cudaError_t Conv::runStaged(const void *const *in, void *const *out,
+                            cudaStream_t s)
+{
+  const size_t bytes=elements()*elemBytes();
+  if(!hostIn && devAlloc((void **) &hostIn,bytes*I.A) != cudaSuccess)
+    return cudaErrorMemoryAllocation;
+  std::vector<void *> din(I.A);
+  CopyArgs C;
+  C.count=I.A; C.bytes=bytes;
+  for(int a=0; a < I.A; ++a) {
+    din[a]=(char *) hostIn+a*bytes;
+    C.src[a]=in[a];
+    C.dst[a]=din[a];
+  }
+  cudaError_t e=launchBulkCopy(C,s);
+  if(e != cudaSuccess) return e;
+  e=run(din.data(),din.data(),s);
+  if(e != cudaSuccess) return e;
+  C.count=I.B;
+  for(int b=0; b < I.B; ++b) {C.src[b]=din[b]; C.dst[b]=out[b];}
+  return launchBulkCopy(C,s);
+}
+
+// Times both host paths on page-locked scratch arrays of this plan's size
+// (the best of two runs each after one untimed); 1 if in place is faster.
+int Conv::measureHostPath(cudaStream_t s)
+{
+  const size_t bytes=elements()*elemBytes();
+  const size_t stride=(bytes+255)/256*256;
+  const int n=std::max(I.A,I.B);
+  void *h=NULL;
+  if(cudaHostAlloc(&h,stride*n,cudaHostAllocMapped) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  std::memset(h,0,stride*n);
+  void *d=mappedAddress(h);
+  std::vector<const void *> in(I.A);
+  std::vector<void *> out(I.B);
+  for(int a=0; a < I.A; ++a) in[a]=(char *) d+a*stride;
+  for(int b=0; b < I.B; ++b) out[b]=(char *) d+b*stride;
+  cudaEvent_t e0=NULL, e1=NULL;
+  bool ok=d && cudaEventCreate(&e0) == cudaSuccess &&
+    cudaEventCreate(&e1) == cudaSuccess;
+  double best[2]={1e300,1e300};
+  for(int rep=0; rep < 3 && ok; ++rep)
+    for(int mode=0; mode < 2 && ok; ++mode) {
+      ok=cudaEventRecord(e0,s) == cudaSuccess &&
+        (mode ? runDirect(in.data(),out.data(),s) :
+         runStaged(in.data(),out.data(),s)) == cudaSuccess &&
+        cudaEventRecord(e1,s) == cudaSuccess &&
+        cudaStreamSynchronize(s) == cudaSuccess;
+      float ms=0;
+      if(ok && rep > 0 && cudaEventElapsedTime(&ms,e0,e1) == cudaSuccess)
+        best[mode]=std::min(best[mode],(double) ms);
+    }
+  cudaStreamSynchronize(s);
+  if(e0) cudaEventDestroy(e0);
+  if(e1) cudaEventDestroy(e1);
+  cudaFreeHost(h);
+  cudaGetLastError();
+  return ok && best[1] < best[0] ? 1 : 0;
+}
+
 cudaError_t Conv::runHost(const void *const *in, void *const *out,
                           cudaStream_t s)
 {
   size_t bytes=elements()*elemBytes();
   int A=I.A, B=I.B;
   if(zeroCopy) {
-    // Page-locked arrays: the first kernel reads them and the last one
-    // writes them in place over the host link (NVLink-C2C on Grace), so
-    // the transfers overlap the transforms instead of preceding them.
+    // Page-locked arrays are addressed directly by the kernels.
     std::vector<const void *> min(A);
     std::vector<void *> mout(B);
     bool ok=true;
@@ -1002,37 +1100,25 @@ cudaError_t Conv::runHost(const void *const *in, void *const *out,
       elemAligned=elemAligned && (size_t) min[a] % elemBytes() == 0;
     for(int b=0; b < B && ok; ++b)
       elemAligned=elemAligned && (size_t) mout[b] % elemBytes() == 0;
-    if(ok && elemAligned && directSegments()) {
-      cudaError_t e=run(min.data(),mout.data(),s);
-      if(e != cudaSuccess) return e;
-      return cudaStreamSynchronize(s);
-    }
     bool aligned=bytes % 16 == 0;
-    for(int a=0; a < A; ++a) aligned=aligned && (size_t) min[a] % 16 == 0;
-    for(int b=0; b < B; ++b) aligned=aligned && (size_t) mout[b] % 16 == 0;
-    if(ok && aligned) {
-      // Narrow column segments would waste the link's lines: move the
-      // arrays whole with the SMs and convolve in device memory.
-      if(!hostIn &&
-         devAlloc((void **) &hostIn,bytes*A) != cudaSuccess) return cudaErrorMemoryAllocation;
-      std::vector<void *> din(A);
-      CopyArgs C;
-      C.count=A; C.bytes=bytes;
-      for(int a=0; a < A; ++a) {
-        din[a]=(char *) hostIn+a*bytes;
-        C.src[a]=min[a];
-        C.dst[a]=din[a];
+    for(int a=0; a < A && ok; ++a) aligned=aligned && (size_t) min[a] % 16 == 0;
+    for(int b=0; b < B && ok; ++b) aligned=aligned && (size_t) mout[b] % 16 == 0;
+    bool direct=ok && elemAligned && directSegments();
+    if(ok && aligned && !direct && hostTile > 0 && hostTileB > 0) {
+      // Narrow device-tuned column tiles would waste the link's lines:
+      // either widen them and stay in place, or copy the arrays whole,
+      // whichever the first call measures to be faster.
+      if(hostPath >= 0) direct=hostPath == 1;
+      else {
+        if(hostDirect < 0) hostDirect=measureHostPath(s);
+        direct=hostDirect == 1;
       }
-      cudaError_t e=launchBulkCopy(C,s);
-      if(e != cudaSuccess) return e;
-      e=run(din.data(),din.data(),s);
-      if(e != cudaSuccess) return e;
-      C.count=B;
-      for(int b=0; b < B; ++b) {C.src[b]=din[b]; C.dst[b]=mout[b];}
-      e=launchBulkCopy(C,s);
-      if(e != cudaSuccess) return e;
-      return cudaStreamSynchronize(s);
     }
+    cudaError_t e=cudaSuccess;
+    if(direct) e=runDirect(min.data(),mout.data(),s);
+    else if(ok && aligned) e=runStaged(min.data(),mout.data(),s);
+    else ok=false;
+    if(ok) return e != cudaSuccess ? e : cudaStreamSynchronize(s);
   }
   if(!hostIn) {
     if(devAlloc((void **) &hostIn,bytes*A) != cudaSuccess) return cudaErrorMemoryAllocation;

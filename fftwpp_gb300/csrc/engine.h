@@ -67,6 +67,8 @@ public:
   cudaError_t runHost(const void *const *in, void *const *out,
                       cudaStream_t s);
   static void setZeroCopy(bool on);
+  // -1: measure on the first host call, 0: staged copies, 1: in place.
+  static void setHostPath(int mode);
 
   const ConvInfo& info() const {return I;}
   size_t elemBytes() const;        // bytes per stored element
@@ -102,14 +104,27 @@ private:
   bool normalize;
   static bool autotune;
   static bool zeroCopy;
+  static int hostPath;
   std::vector<cudaEvent_t> events;
   int marks;
   void tick(cudaStream_t s);
   template<typename T> cudaError_t runT(const void *const *in,
                                         void *const *out, cudaStream_t s);
+  // Axis-0 schedule for runs over page-locked host arrays read and written
+  // in place: the fastest column tiles (and threads) whose rows span at
+  // least 64 bytes, 0 where no candidate does; and which host path the
+  // first such call measured to be faster (-1 not yet measured, 0 whole-
+  // array copies through device memory, 1 in place).
+  int hostTile, hostThr, hostTileB, hostThrB;
+  int hostDirect;
   void allocate();
   void tune();
   bool directSegments() const;
+  cudaError_t runDirect(const void *const *in, void *const *out,
+                        cudaStream_t s);
+  cudaError_t runStaged(const void *const *in, void *const *out,
+                        cudaStream_t s);
+  int measureHostPath(cudaStream_t s);
 };
 
 // Twiddle table W_n^t = exp(2 pi i t/n), t < n, on the current device,

@@ -90,6 +90,14 @@ void fgb_debug_fail_allocation_after(long n);
  * copies page-locked arrays in and out as well. */
 void fgb_set_zero_copy(int on);
 
+/* Process-wide choice of the zero-copy host path for plans whose
+ * device-tuned outer column tiles are narrower than 64 bytes: -1 (default)
+ * lets each plan's first host call time both paths on page-locked scratch
+ * arrays and keep the faster, 0 copies whole arrays through device memory,
+ * 1 reads and writes the caller's arrays in place with the fastest tiles of
+ * at least 64 bytes.  Results are identical either way. */
+void fgb_set_host_path(int mode);
+
 /* Plan parameters: for each axis d, info[8d..8d+7] = m, p, q, N, stored
  * length, centred offset, outer tile, rows produced.  info[24] = kernels per
  * convolution, info[25] = staging bytes, info[26] = 1 if the 1D long path
