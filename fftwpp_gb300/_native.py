@@ -112,7 +112,7 @@ def load():
     lib.fgb_set_zero_copy.restype = None
     lib.fgb_set_zero_copy.argtypes = [ctypes.c_int]
     lib.fgb_set_host_path.restype = None
-    lib.fgb_set_host_path.argtypes = [ctypes.c_int]
+    lib.fgb_set_host_path.argtypes = [ctypes.c_int, ctypes.c_int]
     lib.fgb_destroy.restype = None
     lib.fgb_destroy.argtypes = [vp]
     lib.fgb_last_error.restype = ctypes.c_char_p

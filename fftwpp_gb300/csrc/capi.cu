@@ -696,7 +696,10 @@ int fgb_set_drop_in_precision(int precision)
 
 int fgb_get_drop_in_precision(void) {return dropInPrec;}
 void fgb_set_zero_copy(int on) {Conv::setZeroCopy(on != 0);}
-void fgb_set_host_path(int mode) {Conv::setHostPath(mode);}
+void fgb_set_host_path(int inputs, int outputs)
+{
+  Conv::setHostPath(inputs,outputs);
+}
 
 int fgb_set_normalize(fgb_conv *c, int normalize)
 {

@@ -409,8 +409,9 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
            const long *mForce, int A, int B, int mult, int prec, long batch)
   : batch(batch), staging(0), hostIn(NULL), hostOut(NULL), nlaunch(0),
     timing(false), normalize(true), marks(0), hostTile(0), hostThr(0),
-    hostTileB(0), hostThrB(0), hostDirect(-1)
+    hostTileB(0), hostThrB(0)
 {
+  hostWay[0]=hostWay[1]=-1;
   if(dim < 1 || dim > 3) throw std::runtime_error("dimension must be 1, 2 or 3");
   if(A < 1 || A > FGB_MAXA || B < 1 || B > A)
     throw std::runtime_error("need 1 <= B <= A <= 8");
@@ -973,8 +974,13 @@ cudaError_t Conv::run(const void *const *in, void *const *out, cudaStream_t s)
 
 bool Conv::zeroCopy=true;
 void Conv::setZeroCopy(bool on) {zeroCopy=on;}
-int Conv::hostPath=-1;
-void Conv::setHostPath(int mode) {hostPath=mode < 0 ? -1 : mode > 0;}
+int Conv::hostPathIn=-1, Conv::hostPathOut=-1;
+void Conv::setHostPath(int inputs, int outputs)
+{
+  auto way=[](int w) {return w < 0 ? -1 : std::min(w,(int) HOST_INPLACE64);};
+  hostPathIn=way(inputs);
+  hostPathOut=way(outputs);
+}
 
 // The device address of page-locked host memory, or NULL for memory the GPU
 // cannot address directly.
@@ -999,60 +1005,65 @@ bool Conv::directSegments() const
   return (size_t) a.tile*e >= 64 && (size_t) a.tileB*e >= 64;
 }
 
-// In place over the host link: the first kernel reads the caller's arrays
-// and the last one writes them, so the transfers overlap the transforms.
-// Axis 0 takes its host-line tiles where the device-tuned ones are narrower.
-cudaError_t Conv::runDirect(const void *const *in, void *const *out,
-                            cudaStream_t s)
-{
-  AxisPlan& a=I.axis[0];
-  const int keep[4]={a.tile,a.thr,a.tileB,a.thrB};
-  if(!directSegments()) {
-    a.tile=hostTile; a.thr=hostThr;
-    a.tileB=hostTileB; a.thrB=hostThrB;
-  }
-  cudaError_t e=run(in,out,s);
-  a.tile=keep[0]; a.thr=keep[1];
-  a.tileB=keep[2]; a.thrB=keep[3];
-  return e;
-}
-
-// Whole arrays moved by the SMs (16-byte aligned mapped pointers, sizes a
-// multiple of 16 bytes), convolved in device memory.
-cudaError_t Conv::runStaged(const void *const *in, void *const *out,
-                            cudaStream_t s)
+// One convolution over page-locked arrays (mapped device addresses).  Each
+// side takes its own way over the host link: wayIn for the inputs, wayOut
+// for the outputs, HOST_COPY (whole arrays moved by the SMs through device
+// memory, 16-byte aligned), HOST_INPLACE (the first kernel reads, or the
+// last one writes, the caller's arrays with the device-tuned axis-0 tiles)
+// or HOST_INPLACE64 (the same with the fastest tiles whose rows span at
+// least 64 bytes, whole lines of the link).
+cudaError_t Conv::runZeroCopy(const void *const *in, void *const *out,
+                              int wayIn, int wayOut, cudaStream_t s)
 {
   const size_t bytes=elements()*elemBytes();
-  if(!hostIn && devAlloc((void **) &hostIn,bytes*I.A) != cudaSuccess)
+  const int A=I.A, B=I.B;
+  const bool copyIn=wayIn == HOST_COPY, copyOut=wayOut == HOST_COPY;
+  if((copyIn || copyOut) && !hostIn &&
+     devAlloc((void **) &hostIn,bytes*A) != cudaSuccess)
     return cudaErrorMemoryAllocation;
-  std::vector<void *> din(I.A);
+  std::vector<const void *> src(A);
+  std::vector<void *> dst(B);
+  for(int a=0; a < A; ++a)
+    src[a]=copyIn ? (const void *) ((char *) hostIn+a*bytes) : in[a];
+  for(int b=0; b < B; ++b)
+    dst[b]=copyOut ? (void *) ((char *) hostIn+b*bytes) : out[b];
   CopyArgs C;
-  C.count=I.A; C.bytes=bytes;
-  for(int a=0; a < I.A; ++a) {
-    din[a]=(char *) hostIn+a*bytes;
-    C.src[a]=in[a];
-    C.dst[a]=din[a];
+  C.bytes=bytes;
+  cudaError_t e;
+  if(copyIn) {
+    C.count=A;
+    for(int a=0; a < A; ++a) {C.src[a]=in[a]; C.dst[a]=(void *) src[a];}
+    if((e=launchBulkCopy(C,s)) != cudaSuccess) return e;
   }
-  cudaError_t e=launchBulkCopy(C,s);
-  if(e != cudaSuccess) return e;
-  e=run(din.data(),din.data(),s);
-  if(e != cudaSuccess) return e;
-  C.count=I.B;
-  for(int b=0; b < I.B; ++b) {C.src[b]=din[b]; C.dst[b]=out[b];}
+  AxisPlan& a0=I.axis[0];
+  const int keep[4]={a0.tile,a0.thr,a0.tileB,a0.thrB};
+  if(wayIn == HOST_INPLACE64 && hostTile) {a0.tile=hostTile; a0.thr=hostThr;}
+  if(wayOut == HOST_INPLACE64 && hostTileB) {
+    a0.tileB=hostTileB; a0.thrB=hostThrB;
+  }
+  e=run(src.data(),dst.data(),s);
+  a0.tile=keep[0]; a0.thr=keep[1];
+  a0.tileB=keep[2]; a0.thrB=keep[3];
+  if(e != cudaSuccess || !copyOut) return e;
+  C.count=B;
+  for(int b=0; b < B; ++b) {C.src[b]=dst[b]; C.dst[b]=out[b];}
   return launchBulkCopy(C,s);
 }
 
-// Times both host paths on page-locked scratch arrays of this plan's size
-// (the best of two runs each after one untimed); 1 if in place is faster.
-int Conv::measureHostPath(cudaStream_t s)
+// Times every combination of input and output ways on page-locked scratch
+// arrays of this plan's size (the best of two runs each, after one
+// untimed) and keeps the fastest; whole-array copies both ways if timing
+// fails.
+void Conv::measureHostPath(cudaStream_t s)
 {
+  hostWay[0]=hostWay[1]=HOST_COPY;
   const size_t bytes=elements()*elemBytes();
   const size_t stride=(bytes+255)/256*256;
   const int n=std::max(I.A,I.B);
   void *h=NULL;
   if(cudaHostAlloc(&h,stride*n,cudaHostAllocMapped) != cudaSuccess) {
     cudaGetLastError();
-    return 0;
+    return;
   }
   std::memset(h,0,stride*n);
   void *d=mappedAddress(h);
@@ -1060,27 +1071,37 @@ int Conv::measureHostPath(cudaStream_t s)
   std::vector<void *> out(I.B);
   for(int a=0; a < I.A; ++a) in[a]=(char *) d+a*stride;
   for(int b=0; b < I.B; ++b) out[b]=(char *) d+b*stride;
+  std::vector<std::pair<int,int>> ways;
+  for(int wi=HOST_COPY; wi <= HOST_INPLACE64; ++wi)
+    for(int wo=HOST_COPY; wo <= HOST_INPLACE64; ++wo)
+      if((wi != HOST_INPLACE64 || hostTile) &&
+         (wo != HOST_INPLACE64 || hostTileB)) ways.push_back({wi,wo});
   cudaEvent_t e0=NULL, e1=NULL;
   bool ok=d && cudaEventCreate(&e0) == cudaSuccess &&
     cudaEventCreate(&e1) == cudaSuccess;
-  double best[2]={1e300,1e300};
-  for(int rep=0; rep < 3 && ok; ++rep)
-    for(int mode=0; mode < 2 && ok; ++mode) {
+  ok=ok && runZeroCopy(in.data(),out.data(),HOST_COPY,HOST_COPY,s) ==
+    cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+  double best=1e300;
+  for(int rep=0; rep < 2 && ok; ++rep)
+    for(const auto& w : ways) {
       ok=cudaEventRecord(e0,s) == cudaSuccess &&
-        (mode ? runDirect(in.data(),out.data(),s) :
-         runStaged(in.data(),out.data(),s)) == cudaSuccess &&
+        runZeroCopy(in.data(),out.data(),w.first,w.second,s) == cudaSuccess &&
         cudaEventRecord(e1,s) == cudaSuccess &&
         cudaStreamSynchronize(s) == cudaSuccess;
       float ms=0;
-      if(ok && rep > 0 && cudaEventElapsedTime(&ms,e0,e1) == cudaSuccess)
-        best[mode]=std::min(best[mode],(double) ms);
+      if(!ok || cudaEventElapsedTime(&ms,e0,e1) != cudaSuccess) break;
+      if(ms < best) {
+        best=ms;
+        hostWay[0]=w.first;
+        hostWay[1]=w.second;
+      }
     }
+  if(!ok) hostWay[0]=hostWay[1]=HOST_COPY;
   cudaStreamSynchronize(s);
   if(e0) cudaEventDestroy(e0);
   if(e1) cudaEventDestroy(e1);
   cudaFreeHost(h);
   cudaGetLastError();
-  return ok && best[1] < best[0] ? 1 : 0;
 }
 
 cudaError_t Conv::runHost(const void *const *in, void *const *out,
@@ -1095,30 +1116,30 @@ cudaError_t Conv::runHost(const void *const *in, void *const *out,
     bool ok=true;
     for(int a=0; a < A && ok; ++a) ok=(min[a]=mappedAddress(in[a])) != NULL;
     for(int b=0; b < B && ok; ++b) ok=(mout[b]=mappedAddress(out[b])) != NULL;
-    bool elemAligned=true;
-    for(int a=0; a < A && ok; ++a)
-      elemAligned=elemAligned && (size_t) min[a] % elemBytes() == 0;
-    for(int b=0; b < B && ok; ++b)
-      elemAligned=elemAligned && (size_t) mout[b] % elemBytes() == 0;
-    bool aligned=bytes % 16 == 0;
-    for(int a=0; a < A && ok; ++a) aligned=aligned && (size_t) min[a] % 16 == 0;
-    for(int b=0; b < B && ok; ++b) aligned=aligned && (size_t) mout[b] % 16 == 0;
-    bool direct=ok && elemAligned && directSegments();
-    if(ok && aligned && !direct && hostTile > 0 && hostTileB > 0) {
-      // Narrow device-tuned column tiles would waste the link's lines:
-      // either widen them and stay in place, or copy the arrays whole,
-      // whichever the first call measures to be faster.
-      if(hostPath >= 0) direct=hostPath == 1;
-      else {
-        if(hostDirect < 0) hostDirect=measureHostPath(s);
-        direct=hostDirect == 1;
+    for(int a=0; a < A && ok; ++a) ok=(size_t) min[a] % elemBytes() == 0;
+    for(int b=0; b < B && ok; ++b) ok=(size_t) mout[b] % elemBytes() == 0;
+    if(ok) {
+      bool aligned=bytes % 16 == 0;
+      for(int a=0; a < A; ++a) aligned=aligned && (size_t) min[a] % 16 == 0;
+      for(int b=0; b < B; ++b) aligned=aligned && (size_t) mout[b] % 16 == 0;
+      int wi, wo;
+      if(hostPathIn >= 0 && hostPathOut >= 0) {
+        wi=hostPathIn;
+        wo=hostPathOut;
+      } else if(directSegments()) {
+        wi=wo=HOST_INPLACE;                 // whole lines already
+      } else {
+        if(hostWay[0] < 0) measureHostPath(s);
+        wi=hostWay[0];
+        wo=hostWay[1];
       }
+      if(!aligned) {                        // the SM copies move 16-byte units
+        if(wi == HOST_COPY) wi=HOST_INPLACE;
+        if(wo == HOST_COPY) wo=HOST_INPLACE;
+      }
+      cudaError_t e=runZeroCopy(min.data(),mout.data(),wi,wo,s);
+      return e != cudaSuccess ? e : cudaStreamSynchronize(s);
     }
-    cudaError_t e=cudaSuccess;
-    if(direct) e=runDirect(min.data(),mout.data(),s);
-    else if(ok && aligned) e=runStaged(min.data(),mout.data(),s);
-    else ok=false;
-    if(ok) return e != cudaSuccess ? e : cudaStreamSynchronize(s);
   }
   if(!hostIn) {
     if(devAlloc((void **) &hostIn,bytes*A) != cudaSuccess) return cudaErrorMemoryAllocation;

@@ -17,6 +17,11 @@ namespace fgb {
 enum AxisKind {KIND_PAD=0, KIND_CENTERED=1, KIND_HERMITIAN=2, KIND_REAL=3};
 // PREC_FF: FP64 data at the interface, float-float arithmetic inside.
 enum Precision {PREC_F64=0, PREC_F32=1, PREC_FF=2};
+// How a side (inputs or outputs) of a host-pointer call crosses the host
+// link: whole arrays copied through device memory, or read / written in
+// place by the first / last kernel with the device-tuned axis-0 tiles or
+// with tiles whose rows span at least 64 bytes.
+enum HostWay {HOST_COPY=0, HOST_INPLACE=1, HOST_INPLACE64=2};
 
 // Integer rules shared with the reference (convolve.cc:114-175, 403-410).
 size_t ceilquotient(size_t a, size_t b);
@@ -67,8 +72,10 @@ public:
   cudaError_t runHost(const void *const *in, void *const *out,
                       cudaStream_t s);
   static void setZeroCopy(bool on);
-  // -1: measure on the first host call, 0: staged copies, 1: in place.
-  static void setHostPath(int mode);
+  // How page-locked inputs and outputs cross the host link (HostWay), set
+  // process-wide; -1 for either lets each plan's first host call time every
+  // combination and keep the fastest.
+  static void setHostPath(int inputs, int outputs);
 
   const ConvInfo& info() const {return I;}
   size_t elemBytes() const;        // bytes per stored element
@@ -104,27 +111,24 @@ private:
   bool normalize;
   static bool autotune;
   static bool zeroCopy;
-  static int hostPath;
+  static int hostPathIn, hostPathOut;
   std::vector<cudaEvent_t> events;
   int marks;
   void tick(cudaStream_t s);
   template<typename T> cudaError_t runT(const void *const *in,
                                         void *const *out, cudaStream_t s);
-  // Axis-0 schedule for runs over page-locked host arrays read and written
+  // Axis-0 schedule for runs that read or write page-locked host arrays
   // in place: the fastest column tiles (and threads) whose rows span at
-  // least 64 bytes, 0 where no candidate does; and which host path the
-  // first such call measured to be faster (-1 not yet measured, 0 whole-
-  // array copies through device memory, 1 in place).
+  // least 64 bytes, 0 where no candidate does; and the ways (HostWay) the
+  // first host call measured fastest for inputs and outputs, -1 before.
   int hostTile, hostThr, hostTileB, hostThrB;
-  int hostDirect;
+  int hostWay[2];
   void allocate();
   void tune();
   bool directSegments() const;
-  cudaError_t runDirect(const void *const *in, void *const *out,
-                        cudaStream_t s);
-  cudaError_t runStaged(const void *const *in, void *const *out,
-                        cudaStream_t s);
-  int measureHostPath(cudaStream_t s);
+  cudaError_t runZeroCopy(const void *const *in, void *const *out,
+                          int wayIn, int wayOut, cudaStream_t s);
+  void measureHostPath(cudaStream_t s);
 };
 
 // Twiddle table W_n^t = exp(2 pi i t/n), t < n, on the current device,

@@ -90,13 +90,16 @@ void fgb_debug_fail_allocation_after(long n);
  * copies page-locked arrays in and out as well. */
 void fgb_set_zero_copy(int on);
 
-/* Process-wide choice of the zero-copy host path for plans whose
- * device-tuned outer column tiles are narrower than 64 bytes: -1 (default)
- * lets each plan's first host call time both paths on page-locked scratch
- * arrays and keep the faster, 0 copies whole arrays through device memory,
- * 1 reads and writes the caller's arrays in place with the fastest tiles of
- * at least 64 bytes.  Results are identical either way. */
-void fgb_set_host_path(int mode);
+/* Process-wide choice of how page-locked inputs and outputs of the
+ * host-pointer entries cross the host link, each side on its own:
+ * 0 copies whole arrays through device memory (SM copies), 1 has the first
+ * kernel read (or the last kernel write) the caller's arrays in place with
+ * the plan's device-tuned outer column tiles, 2 the same with the fastest
+ * tiles whose rows span at least 64 bytes.  -1 for either side (default)
+ * lets each plan's first host call whose device-tuned tiles are narrower
+ * than 64 bytes time every combination on page-locked scratch arrays and
+ * keep the fastest.  Results are identical every way. */
+void fgb_set_host_path(int inputs, int outputs);
 
 /* Plan parameters: for each axis d, info[8d..8d+7] = m, p, q, N, stored
  * length, centred offset, outer tile, rows produced.  info[24] = kernels per

@@ -214,9 +214,9 @@ def test_autotune_changes_schedule_only(native_lib, precision):
     ([H.REAL, H.PAD, H.PAD], [12, 10, 9], [23, 19, 17], "binary")])
 def test_zero_copy_host_path(native_lib, precision, case):
     """Page-locked host arrays are read and written by the kernels in place
-    over the host link, or copied whole by the SMs, whichever the plan
-    measured faster; the result equals the copying path and both forced
-    zero-copy paths bit for bit."""
+    over the host link, or copied whole by the SMs, each side the way the
+    plan measured fastest; the result equals the copying path and every
+    forced combination of ways bit for bit."""
     import torch
     from fftwpp_gb300.gpu import HybridConvolution
     kinds, L, M, mult = case
@@ -240,14 +240,15 @@ def test_zero_copy_host_path(native_lib, precision, case):
     assert np.array_equal(zc[0], cp[0])
     assert np.array_equal(zc[1], cp[1])      # the second input is untouched
     try:
-        for mode in (0, 1):
-            native_lib.fgb_set_host_path(mode)
-            h = pinned()
-            conv.convolve_host(*h)
-            assert np.array_equal(zc[0], h[0])
-            assert np.array_equal(zc[1], h[1])
+        for wi in (0, 1, 2):
+            for wo in (0, 1, 2):
+                native_lib.fgb_set_host_path(wi, wo)
+                h = pinned()
+                conv.convolve_host(*h)
+                assert np.array_equal(zc[0], h[0]), (wi, wo)
+                assert np.array_equal(zc[1], h[1]), (wi, wo)
     finally:
-        native_lib.fgb_set_host_path(-1)
+        native_lib.fgb_set_host_path(-1, -1)
 
 
 def test_host_path_misaligned_pinned(native_lib):
