@@ -615,7 +615,8 @@ def run_ours(args, w):
                "h2d_bytes_per_step": w["A"] * nbytes,
                "d2h_bytes_per_step": w["B"] * nbytes,
                "api": "fgb_convolve_host (page-locked host arrays, "
-                      "zero copy over the host link)"}
+                      "zero copy over the host link)",
+               "host_path": list(conv.host_path())}
 
     cpu_rate, cpu_n, cpu_dt = cpu_oracle_rate(w, args.cpu_budget, 64,
                                               os.cpu_count() or 1)

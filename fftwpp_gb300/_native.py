@@ -105,6 +105,8 @@ def load():
     lib.fgb_debug_fail_allocation_after.argtypes = [ctypes.c_long]
     lib.fgb_set_autotune.restype = None
     lib.fgb_set_autotune.argtypes = [ctypes.c_int]
+    lib.fgb_set_residue_search.restype = None
+    lib.fgb_set_residue_search.argtypes = [ctypes.c_int]
     lib.fgb_set_drop_in_precision.restype = ctypes.c_int
     lib.fgb_set_drop_in_precision.argtypes = [ctypes.c_int]
     lib.fgb_get_drop_in_precision.restype = ctypes.c_int
@@ -113,6 +115,8 @@ def load():
     lib.fgb_set_zero_copy.argtypes = [ctypes.c_int]
     lib.fgb_set_host_path.restype = None
     lib.fgb_set_host_path.argtypes = [ctypes.c_int, ctypes.c_int]
+    lib.fgb_host_path.restype = ctypes.c_int
+    lib.fgb_host_path.argtypes = [vp, P(ctypes.c_int), P(ctypes.c_int)]
     lib.fgb_destroy.restype = None
     lib.fgb_destroy.argtypes = [vp]
     lib.fgb_last_error.restype = ctypes.c_char_p

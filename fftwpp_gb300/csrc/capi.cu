@@ -100,16 +100,15 @@ fgb_conv *make(int dim, const int *kinds, const long *L, const long *M,
                const char *where)
 {
   try {
-    fgb_conv *c=new fgb_conv;
-    c->conv.reset(new Conv(dim,kinds,L,M,m,A,B,mult,prec,batch));
+    std::unique_ptr<fgb_conv> c(new fgb_conv);
+    c->conv.reset(Conv::create(dim,kinds,L,M,m,A,B,mult,prec,batch));
     if(cudaStreamCreateWithFlags(&c->stream,cudaStreamNonBlocking) !=
        cudaSuccess) {
       cudaGetLastError();
-      delete c;
       report(where,"cannot create a CUDA stream");
       return NULL;
     }
-    return c;
+    return c.release();
   } catch(std::exception& e) {
     report(where,e.what());
     return NULL;
@@ -680,6 +679,7 @@ int fgb_info(const fgb_conv *c, long *info)
 }
 
 void fgb_set_autotune(int on) {Conv::setAutotune(on != 0);}
+void fgb_set_residue_search(int on) {Conv::setResidueSearch(on != 0);}
 
 void fgb_debug_fail_allocation_after(long n) {failAllocationAfter(n);}
 
@@ -696,6 +696,13 @@ int fgb_set_drop_in_precision(int precision)
 
 int fgb_get_drop_in_precision(void) {return dropInPrec;}
 void fgb_set_zero_copy(int on) {Conv::setZeroCopy(on != 0);}
+int fgb_host_path(const fgb_conv *c, int *inputs, int *outputs)
+{
+  if(!c) return -1;
+  c->conv->hostPath(inputs,outputs);
+  return 0;
+}
+
 void fgb_set_host_path(int inputs, int outputs)
 {
   Conv::setHostPath(inputs,outputs);

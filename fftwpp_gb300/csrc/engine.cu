@@ -6,7 +6,9 @@
 #include <climits>
 #include <cstring>
 #include <cmath>
+#include <algorithm>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <tuple>
@@ -250,6 +252,27 @@ static int pickRpc(long n, int A, long nrows, F smem)
   return rpc;
 }
 
+// Estimated arithmetic instructions of a row axis with residue blocks of m
+// points and q residues: transforms, the fold (a complex twiddle per term
+// for residues r > 0) and the post-twiddled accumulation.
+static double rowCost(const AxisPlan& a, long m, long q, int A, int B)
+{
+  long p=ceilquotient(a.L,m);
+  return q*(A+B)*fftInstr(m)+A*(double) m*(2.0*p+(q-1)*6.0*p)+
+    B*(double) a.L*(2.0+(q-1)*6.0);
+}
+
+// The same for an outer axis: residue r > 0 folds p terms with a complex
+// twiddle each (forward) and post-twiddles every output (backward); r = 0
+// only adds.
+static double outerCost(const AxisPlan& a, long m, long q, int A, int B)
+{
+  long p=ceilquotient(a.L,m);
+  double fwd=q*fftInstr(m)+m*(2.0*p+(q-1)*6.0*p);
+  double bwd=q*fftInstr(m)+a.L*(2.0+(q-1)*6.0);
+  return A*fwd+B*bwd;
+}
+
 // Inner (row) axis, complex data: residue block m and residue count q.
 static bool planRowComplex(AxisPlan& a, long mForce, int A, int B, int prec)
 {
@@ -266,11 +289,7 @@ static bool planRowComplex(AxisPlan& a, long mForce, int A, int B, int prec)
       long m=nextfftsize(ceilquotient(a.M,q));
       if(m*q < a.M) continue;
       if(rowNeed(prec,a.L,m,A,B) > SMEM_MAX) continue;
-      long p=ceilquotient(a.L,m);
-      // Arithmetic instructions: transforms, the fold (a complex twiddle per
-      // term for residues r > 0) and the post-twiddled accumulation.
-      double cost=q*(A+B)*fftInstr(m)+A*(double) m*(2.0*p+(q-1)*6.0*p)+
-        B*(double) a.L*(2.0+(q-1)*6.0);
+      double cost=rowCost(a,m,q,A,B);
       if(cost < best) {best=cost; bm=m; bq=q;}
     }
     if(!bm) return false;
@@ -375,14 +394,8 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
     long bm=0;
     for(long m=1; m <= N; ++m) {
       if(N % m || !smooth(m)) continue;
-      long q=N/m;
       if(outerNeed(prec,a.L,m,1) > SMEM_MAX) continue;
-      long p=ceilquotient(a.L,m);
-      // Residue r > 0 folds p terms with a complex twiddle each (forward)
-      // and post-twiddles every output (backward); r = 0 only adds.
-      double fwd=q*fftInstr(m)+m*(2.0*p+(q-1)*6.0*p);
-      double bwd=q*fftInstr(m)+a.L*(2.0+(q-1)*6.0);
-      double cost=A*fwd+B*bwd;
+      double cost=outerCost(a,m,N/m,A,B);
       if(cost < best) {best=cost; bm=m;}
     }
     if(!bm) throw std::runtime_error("no outer padding plan fits");
@@ -406,7 +419,8 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
 }
 
 Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
-           const long *mForce, int A, int B, int mult, int prec, long batch)
+           const long *mForce, int A, int B, int mult, int prec, long batch,
+           bool tuneSchedule)
   : batch(batch), staging(0), hostIn(NULL), hostOut(NULL), nlaunch(0),
     timing(false), normalize(true), marks(0), hostTile(0), hostThr(0),
     hostTileB(0), hostThrB(0)
@@ -512,7 +526,7 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
   }
   try {
     allocate();
-    if(autotune) tune();
+    if(autotune && tuneSchedule) tune();
   } catch(...) {
     // A throwing constructor runs no destructor: release what was taken.
     for(void *p : bufs) cudaFree(p);
@@ -523,6 +537,113 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
 
 bool Conv::autotune=true;
 void Conv::setAutotune(bool on) {autotune=on;}
+bool Conv::residueSearch=true;
+void Conv::setResidueSearch(bool on) {residueSearch=on;}
+
+// Candidate residue block lengths of a complex axis for the timed search:
+// at most three, cheapest estimate first, each within 1.5x of the cheapest.
+static std::vector<long> residueCandidates(const AxisPlan& a, bool outer,
+                                           int prec, int A, int B)
+{
+  std::vector<std::pair<double,long>> c;
+  if(outer) {
+    long N=nextfftsize(a.M);
+    for(long m=1; m <= N; ++m)
+      if(N % m == 0 && smooth(m) && outerNeed(prec,a.L,m,1) <= SMEM_MAX)
+        c.push_back({outerCost(a,m,N/m,A,B),m});
+  } else {
+    for(long q=1; q <= 64; ++q) {
+      long m=nextfftsize(ceilquotient(a.M,q));
+      if(m*q < a.M || rowNeed(prec,a.L,m,A,B) > SMEM_MAX) continue;
+      bool seen=false;
+      for(const auto& x : c) seen=seen || x.second == m;
+      if(!seen) c.push_back({rowCost(a,m,q,A,B),m});
+    }
+  }
+  std::sort(c.begin(),c.end());
+  std::vector<long> out;
+  for(const auto& x : c)
+    if(out.size() < 3 && x.first <= 1.5*c[0].first) out.push_back(x.second);
+  return out;
+}
+
+Conv *Conv::create(int dim, const int *kinds, const long *L, const long *M,
+                   const long *mForce, int A, int B, int mult, int prec,
+                   long batch)
+{
+  if(!autotune || !residueSearch)
+    return new Conv(dim,kinds,L,M,mForce,A,B,mult,prec,batch);
+  long mf[3]={0,0,0};
+  for(int d=0; d < dim && d < 3; ++d) mf[d]=mForce ? mForce[d] : 0;
+  std::unique_ptr<Conv> base(new Conv(dim,kinds,L,M,mf,A,B,mult,prec,batch,
+                                      false));
+  const ConvInfo I0=base->info();
+  std::vector<std::vector<long>> cands(dim);
+  bool any=false;
+  for(int d=0; d < dim; ++d) {
+    const AxisPlan& a=I0.axis[d];
+    if(I0.longRow || mf[d] > 0 ||
+       (a.kind != KIND_PAD && a.kind != KIND_CENTERED)) continue;
+    cands[d]=residueCandidates(a,d < dim-1,prec,A,B);
+    any=any || cands[d].size() > 1;
+  }
+  if(!any) {
+    base.reset();
+    return new Conv(dim,kinds,L,M,mf,A,B,mult,prec,batch);
+  }
+
+  // Zero-filled scratch arrays, shared by every candidate (the stored
+  // layout does not depend on m).
+  const size_t bytes=base->elements()*base->elemBytes();
+  std::vector<void *> tin(A,NULL), tout(B,NULL);
+  cudaStream_t s=NULL;
+  cudaEvent_t e0=NULL, e1=NULL;
+  bool ok=cudaStreamCreateWithFlags(&s,cudaStreamNonBlocking) == cudaSuccess &&
+    cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+  for(auto& p : tin)
+    ok=ok && devAlloc((void **) &p,bytes) == cudaSuccess &&
+      cudaMemsetAsync(p,0,bytes,s) == cudaSuccess;
+  for(auto& p : tout) ok=ok && devAlloc((void **) &p,bytes) == cudaSuccess;
+  // Best of two timed convolutions after an untimed one (ms), or "never".
+  auto timeOf=[&](Conv& c) {
+    double best=1e300;
+    for(int rep=0; rep < 3 && ok; ++rep) {
+      float ms=0;
+      if(cudaEventRecord(e0,s) != cudaSuccess ||
+         c.run(tin.data(),tout.data(),s) != cudaSuccess ||
+         cudaEventRecord(e1,s) != cudaSuccess ||
+         cudaStreamSynchronize(s) != cudaSuccess ||
+         cudaEventElapsedTime(&ms,e0,e1) != cudaSuccess) {
+        cudaGetLastError();
+        return 1e300;
+      }
+      if(rep > 0) best=std::min(best,(double) ms);
+    }
+    return best;
+  };
+  double bestT=ok ? timeOf(*base) : 1e300;
+  base.reset();
+  for(int d=0; d < dim && ok && bestT < 1e300; ++d) {
+    if(cands[d].size() < 2) continue;
+    for(long m : cands[d]) {
+      long trial[3]={mf[0],mf[1],mf[2]};
+      trial[d]=m;
+      try {
+        Conv c(dim,kinds,L,M,trial,A,B,mult,prec,batch,false);
+        double t=timeOf(c);
+        if(t < 0.97*bestT) {bestT=t; mf[d]=m;}
+      } catch(std::exception&) {}     // a candidate that does not plan
+    }
+  }
+  if(s) cudaStreamSynchronize(s);
+  cudaGetLastError();
+  for(void *p : tin) if(p) cudaFree(p);
+  for(void *p : tout) if(p) cudaFree(p);
+  if(e0) cudaEventDestroy(e0);
+  if(e1) cudaEventDestroy(e1);
+  if(s) cudaStreamDestroy(s);
+  return new Conv(dim,kinds,L,M,mf,A,B,mult,prec,batch);
+}
 
 void Conv::tune()
 {
@@ -1051,7 +1172,7 @@ cudaError_t Conv::runZeroCopy(const void *const *in, void *const *out,
 }
 
 // Times every combination of input and output ways on page-locked scratch
-// arrays of this plan's size (the best of two runs each, after one
+// arrays of this plan's size (the best of three runs each, after one
 // untimed) and keeps the fastest; whole-array copies both ways if timing
 // fails.
 void Conv::measureHostPath(cudaStream_t s)
@@ -1082,7 +1203,7 @@ void Conv::measureHostPath(cudaStream_t s)
   ok=ok && runZeroCopy(in.data(),out.data(),HOST_COPY,HOST_COPY,s) ==
     cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
   double best=1e300;
-  for(int rep=0; rep < 2 && ok; ++rep)
+  for(int rep=0; rep < 3 && ok; ++rep)
     for(const auto& w : ways) {
       ok=cudaEventRecord(e0,s) == cudaSuccess &&
         runZeroCopy(in.data(),out.data(),w.first,w.second,s) == cudaSuccess &&
@@ -1102,6 +1223,15 @@ void Conv::measureHostPath(cudaStream_t s)
   if(e1) cudaEventDestroy(e1);
   cudaFreeHost(h);
   cudaGetLastError();
+}
+
+void Conv::hostPath(int *inputs, int *outputs) const
+{
+  int wi=hostWay[0], wo=hostWay[1];
+  if(hostPathIn >= 0 && hostPathOut >= 0) {wi=hostPathIn; wo=hostPathOut;}
+  else if(directSegments()) wi=wo=HOST_INPLACE;
+  if(inputs) *inputs=wi;
+  if(outputs) *outputs=wo;
 }
 
 cudaError_t Conv::runHost(const void *const *in, void *const *out,

@@ -57,9 +57,25 @@ class Conv {
 public:
   // kinds/L/M/mForce: per dimension, outermost first.  mForce[d] = 0 lets
   // the planner choose.  Throws std::runtime_error on invalid input.
+  // tuneSchedule = false skips the timed tile and thread search (the cost
+  // model's schedule stays).
   Conv(int dim, const int *kinds, const long *L, const long *M,
-       const long *mForce, int A, int B, int mult, int prec, long batch=1);
+       const long *mForce, int A, int B, int mult, int prec, long batch=1,
+       bool tuneSchedule=true);
   ~Conv();
+
+  // A plan whose residue block lengths are chosen by timing (the GPU
+  // counterpart of the reference's OptBase search over m, convolve.cc:177-
+  // 470): for every complex axis not forced, up to three cost-model
+  // candidates are timed in whole convolutions, axis by axis from the
+  // outermost, and a candidate replaces the current choice only if at least
+  // 3 % faster.  Plain construction when autotuning or the residue search
+  // is off process-wide.  Throws like the constructor.
+  static Conv *create(int dim, const int *kinds, const long *L,
+                      const long *M, const long *mForce, int A, int B,
+                      int mult, int prec, long batch=1);
+  // Residue search in create() on or off, process-wide (default on).
+  static void setResidueSearch(bool on);
 
   // Device pointers: A inputs, B outputs (outputs may alias inputs), each a
   // dense row-major array in the stored layout; `batch` independent
@@ -76,6 +92,9 @@ public:
   // process-wide; -1 for either lets each plan's first host call time every
   // combination and keep the fastest.
   static void setHostPath(int inputs, int outputs);
+  // The ways this plan's host calls take (forced, fixed by the tiles, or
+  // measured), -1 while still to be measured.
+  void hostPath(int *inputs, int *outputs) const;
 
   const ConvInfo& info() const {return I;}
   size_t elemBytes() const;        // bytes per stored element
@@ -110,6 +129,7 @@ private:
   bool timing;
   bool normalize;
   static bool autotune;
+  static bool residueSearch;
   static bool zeroCopy;
   static int hostPathIn, hostPathOut;
   std::vector<cudaEvent_t> events;

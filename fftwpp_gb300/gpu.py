@@ -183,6 +183,14 @@ class HybridConvolution:
             raise RuntimeError(_native.last_error())
         return list(arrays[:self.B])
 
+    def host_path(self) -> tuple[int, int]:
+        """How page-locked inputs and outputs of convolve_host cross the
+        host link: 0 whole-array copies, 1 in place with the device-tuned
+        tiles, 2 in place with 64-byte tiles; -1 before the first call."""
+        wi, wo = ctypes.c_int(), ctypes.c_int()
+        self.lib.fgb_host_path(self.handle, ctypes.byref(wi), ctypes.byref(wo))
+        return wi.value, wo.value
+
     # -- per-kernel timing ---------------------------------------------------
     def launch_names(self) -> list[str]:
         """Kernel launched at each position of one convolve call."""

@@ -50,8 +50,9 @@ typedef struct fgb_conv fgb_conv;
  * per-axis forced residue block length (0 = planner's choice), the
  * Application m of the reference (convolve.h:103-111); a Hermitian axis is
  * always transformed explicitly, at the padded length m q the reference
- * would use for that m.  Plans are then autotuned (fgb_set_autotune); the
- * results do not depend on m, tiles or rows per CTA.  batch > 1 runs
+ * would use for that m.  Plans are then autotuned (fgb_set_autotune,
+ * fgb_set_residue_search); the results do not depend on m (beyond
+ * rounding), tiles or rows per CTA.  batch > 1 runs
  * independent 1D problems stored back to back.  Replaces the constructors
  * fftPad*(L,M,app,...) + Convolution{,2,3}(...) (convolve.h:515-1603).
  * Returns NULL on error. */
@@ -101,6 +102,12 @@ void fgb_set_zero_copy(int on);
  * keep the fastest.  Results are identical every way. */
 void fgb_set_host_path(int inputs, int outputs);
 
+/* The ways (0, 1, 2 as for fgb_set_host_path) this plan's host-pointer
+ * calls take for page-locked inputs and outputs: the measured choice, or
+ * -1 before the first call that measures.  Returns 0, or -1 for a null
+ * handle. */
+int fgb_host_path(const fgb_conv *c, int *inputs, int *outputs);
+
 /* Plan parameters: for each axis d, info[8d..8d+7] = m, p, q, N, stored
  * length, centred offset, outer tile, rows produced.  info[24] = kernels per
  * convolution, info[25] = staging bytes, info[26] = 1 if the 1D long path
@@ -112,10 +119,22 @@ int fgb_info(const fgb_conv *c, long *info);
 
 /* Plan-time autotuning, process-wide (default on): fgb_create times the
  * candidate rows-per-CTA of the innermost-axis kernel and column tiles of
- * the outer-axis kernels on scratch data and keeps the fastest, the GPU
- * counterpart of FFTW++'s optimiser (convolve.cc:177-470).  0 keeps the
- * planner's cost-model choice. */
+ * the outer-axis kernels (each with 128 or 256 threads) on scratch data and
+ * keeps the fastest, the GPU counterpart of FFTW++'s optimiser
+ * (convolve.cc:177-470).  0 keeps the planner's cost-model choice and turns
+ * the residue search below off as well.  Schedules regroup work across CTAs
+ * only: results are bit-identical either way. */
 void fgb_set_autotune(int on);
+
+/* Timed residue search, process-wide (default on, effective while
+ * autotuning is on): for every fftPad / fftPadCentered axis whose m is not
+ * forced, fgb_create times whole convolutions with up to three residue
+ * block lengths m the cost model ranks best (within 1.5x of its estimate),
+ * axis by axis from the outermost, and keeps a candidate only if it is at
+ * least 3 % faster, as the reference's OptBase times its candidate m
+ * (convolve.cc:177-470).  Like the reference's choice of m, it changes the
+ * rounding of the results (within the same error bounds), not the values. */
+void fgb_set_residue_search(int on);
 
 /* Normalisation switch: 1 (default) scales the result by 1/prod(m q) as
  * Convolution::convolve does; 0 returns the unnormalised sum of

@@ -199,11 +199,15 @@ def test_autotune_changes_schedule_only(native_lib, precision):
     kinds, L, M = [H.REAL, H.PAD, H.PAD], [12, 10, 9], [23, 19, 17]
     fs = _inputs(kinds, L, 2, seed=17)
     try:
-        native_lib.fgb_set_autotune(0)
-        plain, c0 = run_gpu(kinds, L, M, fs, "binary", precision)
+        native_lib.fgb_set_residue_search(0)
+        try:
+            native_lib.fgb_set_autotune(0)
+            plain, c0 = run_gpu(kinds, L, M, fs, "binary", precision)
+        finally:
+            native_lib.fgb_set_autotune(1)
+        tuned, c1 = run_gpu(kinds, L, M, fs, "binary", precision)
     finally:
-        native_lib.fgb_set_autotune(1)
-    tuned, c1 = run_gpu(kinds, L, M, fs, "binary", precision)
+        native_lib.fgb_set_residue_search(1)
     assert np.array_equal(plain[0], tuned[0])
 
 
