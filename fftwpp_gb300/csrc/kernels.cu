@@ -304,6 +304,10 @@ __device__ __forceinline__ void cpAsyncWait()
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
+// Global loads a thread issues back to back in the row kernels' load loops
+// (more bytes in flight per thread than one dependent load per iteration).
+#define FGB_LOADS 4
+
 // One group of P.rpc rows of the complex row convolution (all residues),
 // using the block's shared memory.  The A x rpc input rows are transformed
 // together as interleaved columns col = a*rpc + rho, so the B x rpc output
@@ -326,18 +330,27 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
   const UDiv dR(R);
   const long long row0=group*R;
 
-  for(int i=tid; i < ld*L; i += nthr) {
-    int col=dL(i), s=i-col*L;
-    int a=dR(col);
-    long long row=row0+col-a*R;
-    cplx<T> v=mk((T) 0,(T) 0);
-    if(row < P.nrows) {
-      long long off=row*P.rowStride+s;
-      if(P.realIO) v=mk(loadIOr((const T *) P.in[a]+off,P.io64 & 1),(T) 0);
-      else if(P.io64 & 1) v=loadIO(P.in[a]+off,true);
-      else v=ldx<CG>(P.in[a]+off);
+  // The loads of FGB_LOADS iterations are issued before any is used.
+  for(int i0=tid; i0 < ld*L; i0 += FGB_LOADS*nthr) {
+    cplx<T> v[FGB_LOADS];
+#pragma unroll
+    for(int u=0; u < FGB_LOADS; ++u) {
+      const int i=i0+u*nthr;
+      v[u]=mk((T) 0,(T) 0);
+      if(i >= ld*L) continue;
+      int col=dL(i), s=i-col*L;
+      int a=dR(col);
+      long long row=row0+col-a*R;
+      if(row < P.nrows) {
+        long long off=row*P.rowStride+s;
+        if(P.realIO) v[u]=mk(loadIOr((const T *) P.in[a]+off,P.io64 & 1),(T) 0);
+        else if(P.io64 & 1) v[u]=loadIO(P.in[a]+off,true);
+        else v[u]=ldx<CG>(P.in[a]+off);
+      }
     }
-    fin[i]=v;
+#pragma unroll
+    for(int u=0; u < FGB_LOADS; ++u)
+      if(i0+u*nthr < ld*L) fin[i0+u*nthr]=v[u];
   }
   for(int i=tid; i < lb*L; i += nthr) acc[i]=mk((T) 0,(T) 0);
   __syncthreads();
@@ -437,20 +450,33 @@ hermRowKernel(const HermRowPlan<T> P)
     // Z read from the row itself (the two reads of an element are L1/L2
     // hits; every read of the group precedes its writes, so in = out is
     // safe).
-    for(int i=tid; i < Nh*ld; i += nthr) {
-      int k=dLd(i), col=i-k*ld;
-      int a=dR(col);
-      long long row=row0+col-a*R;
-      const cplx<T> *zr=P.in[a]+row*P.rowStride;
-      const bool live=row < P.nrows;
-      cplx<T> zk=live && k < H ? loadIO(zr+k,P.io64 & 1) : mk((T) 0,(T) 0);
-      if(k == 0) zk.y=(T) 0;
-      int kk=Nh-k;
-      cplx<T> zc=live && kk < H ? conjg(loadIO(zr+kk,P.io64 & 1)) :
-        mk((T) 0,(T) 0);
-      cplx<T> s=zk+zc;
-      cplx<T> d=twmul<1>(zk-zc,tw[k]);
-      x[sp(i)]=mk(s.x-d.y,s.y+d.x);
+    // The loads of FGB_LOADS iterations are issued before any is used.
+    for(int i0=tid; i0 < Nh*ld; i0 += FGB_LOADS*nthr) {
+      cplx<T> zk[FGB_LOADS], zc[FGB_LOADS];
+#pragma unroll
+      for(int u=0; u < FGB_LOADS; ++u) {
+        const int i=i0+u*nthr;
+        int k=dLd(i), col=i-k*ld;       // col < ld: a < A for every i
+        int a=dR(col);
+        long long row=row0+col-a*R;
+        const cplx<T> *zr=P.in[a]+row*P.rowStride;
+        const bool live=i < Nh*ld && row < P.nrows;
+        const int kk=Nh-k;
+        zk[u]=live && k < H ? loadIO(zr+k,P.io64 & 1) : mk((T) 0,(T) 0);
+        zc[u]=live && kk < H ? loadIO(zr+kk,P.io64 & 1) : mk((T) 0,(T) 0);
+      }
+#pragma unroll
+      for(int u=0; u < FGB_LOADS; ++u) {
+        const int i=i0+u*nthr;
+        if(i >= Nh*ld) break;
+        const int k=dLd(i);
+        cplx<T> a=zk[u];
+        if(k == 0) a.y=(T) 0;
+        cplx<T> b=conjg(zc[u]);
+        cplx<T> s=a+b;
+        cplx<T> d=twmul<1>(a-b,tw[k]);
+        x[sp(i)]=mk(s.x-d.y,s.y+d.x);
+      }
     }
     __syncthreads();
     const cplx<T> *Z;

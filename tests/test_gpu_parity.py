@@ -369,3 +369,23 @@ def test_full_size_properties_3d_real(native_lib, precision, tol):
     h2 = run(f, g2)
     assert rel_l2(h12, h1 + 3.0 * h2) <= tol
     assert rel_l2(run(g1, f), h1) <= tol
+
+
+@pytest.mark.parametrize("precision", ["f64", "ff", "f32"])
+def test_residue_search(native_lib, precision):
+    """The timed residue search may pick another m than the cost model; the
+    result stays within the tolerance of the oracle either way, and with the
+    search off the plan is the cost model's."""
+    kinds, L, M = [H.PAD], [1024], [2047]
+    fs = _inputs(kinds, L, 2, seed=47)
+    want = H.convolve(fs, kinds, L, M, mult="binary")[0]
+    try:
+        native_lib.fgb_set_residue_search(0)
+        plain, c0 = run_gpu(kinds, L, M, fs, "binary", precision)
+    finally:
+        native_lib.fgb_set_residue_search(1)
+    searched, c1 = run_gpu(kinds, L, M, fs, "binary", precision)
+    assert rel_l2(plain[0], want) <= TOL[precision]
+    assert rel_l2(searched[0], want) <= TOL[precision]
+    a0, a1 = c0.axes[0], c1.axes[0]
+    assert a0["m"] * a0["q"] >= 2047 and a1["m"] * a1["q"] >= 2047
