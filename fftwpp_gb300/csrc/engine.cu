@@ -423,7 +423,7 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
            bool tuneSchedule)
   : batch(batch), staging(0), hostIn(NULL), hostOut(NULL), nlaunch(0),
     timing(false), normalize(true), marks(0), hostTile(0), hostThr(0),
-    hostTileB(0), hostThrB(0)
+    hostTileB(0), hostThrB(0), side(NULL), inputReady(NULL)
 {
   hostWay[0]=hostWay[1]=-1;
   if(dim < 1 || dim > 3) throw std::runtime_error("dimension must be 1, 2 or 3");
@@ -783,6 +783,8 @@ void Conv::tune()
 Conv::~Conv()
 {
   for(cudaEvent_t ev : events) cudaEventDestroy(ev);
+  for(cudaEvent_t ev : ready) cudaEventDestroy(ev);
+  if(side) cudaStreamDestroy(side);
   for(void *p : bufs) cudaFree(p);
   if(hostIn) cudaFree(hostIn);
   if(hostOut) cudaFree(hostOut);
@@ -904,6 +906,31 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   // Float-float mode: the first launch reads the caller's FP64 arrays and
   // the last one writes them.
   const int IN64=std::is_same<T,ff>::value ? 1 : 0, OUT64=2*IN64;
+  // The first outer-axis launch: one per input, each after its input's
+  // ready event, when a host call copies the inputs in one by one (with
+  // per-launch timing on, one launch after all of them).
+  auto firstOuter=[&](OuterPlan<T>& O, const AxisPlan& a) {
+    auto go=[&](OuterPlan<T>& Q) {
+      return a.kind == KIND_REAL ? launchOuterRealFwd<T>(Q,a.thr,s) :
+        launchOuterFwd<T>(Q,a.thr,s);
+    };
+    if(!inputReady) return go(O);
+    cudaError_t e;
+    if(timing) {
+      for(int i=0; i < A; ++i)
+        if((e=cudaStreamWaitEvent(s,inputReady[i],0)) != cudaSuccess) return e;
+      return go(O);
+    }
+    OuterPlan<T> Q=O;
+    Q.count=1;
+    for(int i=0; i < A; ++i) {
+      if((e=cudaStreamWaitEvent(s,inputReady[i],0)) != cudaSuccess) return e;
+      Q.in[0]=O.in[i];
+      Q.out[0]=O.out[i];
+      if((e=go(Q)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  };
 
   if(I.dim == 1 && !I.longRow) {
     const AxisPlan& a=I.axis[0];
@@ -982,8 +1009,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.scale=(T) 1;
     O.io64=IN64;
     for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) bufs[i];}
-    e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(O,ax.thr,s) :
-      launchOuterFwd<T>(O,ax.thr,s);
+    e=firstOuter(O,ax);
     tick(s);
     if(e != cudaSuccess) return e;
     if(ay.kind == KIND_HERMITIAN) {
@@ -1030,8 +1056,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   X.scale=(T) 1;
   X.io64=IN64;
   for(int i=0; i < A; ++i) {X.in[i]=(const Cx *) in[i]; X.out[i]=(Cx *) bx[i];}
-  e=ax.kind == KIND_REAL ? launchOuterRealFwd<T>(X,ax.thr,s) :
-    launchOuterFwd<T>(X,ax.thr,s);
+  e=firstOuter(X,ax);
   tick(s);
   if(e != cudaSuccess) return e;
 
@@ -1151,7 +1176,38 @@ cudaError_t Conv::runZeroCopy(const void *const *in, void *const *out,
   CopyArgs C;
   C.bytes=bytes;
   cudaError_t e;
-  if(copyIn) {
+  // With two or more inputs and an outer axis, each input is copied on a
+  // side stream and its first transform starts as soon as it has arrived.
+  const bool pipeline=copyIn && A > 1 && I.dim > 1 && !I.longRow;
+  if(pipeline) {
+    if(!side && cudaStreamCreateWithFlags(&side,cudaStreamNonBlocking) !=
+       cudaSuccess) {
+      side=NULL;
+      return cudaErrorMemoryAllocation;
+    }
+    while((int) ready.size() < A+1) {
+      cudaEvent_t ev;
+      if((e=cudaEventCreateWithFlags(&ev,cudaEventDisableTiming)) !=
+         cudaSuccess) return e;
+      ready.push_back(ev);
+    }
+    // The copies follow the work already queued on s (ready[A] marks it).
+    if((e=cudaEventRecord(ready[A],s)) != cudaSuccess ||
+       (e=cudaStreamWaitEvent(side,ready[A],0)) != cudaSuccess) return e;
+    // The first input moves with the SMs (nothing else runs yet); the
+    // later ones with the copy engines, which leave the SMs to the
+    // transforms they overlap.
+    C.count=1;
+    C.src[0]=in[0];
+    C.dst[0]=(void *) src[0];
+    if((e=launchBulkCopy(C,side)) != cudaSuccess ||
+       (e=cudaEventRecord(ready[0],side)) != cudaSuccess) return e;
+    for(int a=1; a < A; ++a)
+      if((e=cudaMemcpyAsync((void *) src[a],in[a],bytes,
+                            cudaMemcpyDefault,side)) != cudaSuccess ||
+         (e=cudaEventRecord(ready[a],side)) != cudaSuccess) return e;
+    inputReady=ready.data();
+  } else if(copyIn) {
     C.count=A;
     for(int a=0; a < A; ++a) {C.src[a]=in[a]; C.dst[a]=(void *) src[a];}
     if((e=launchBulkCopy(C,s)) != cudaSuccess) return e;
@@ -1163,6 +1219,7 @@ cudaError_t Conv::runZeroCopy(const void *const *in, void *const *out,
     a0.tileB=hostTileB; a0.thrB=hostThrB;
   }
   e=run(src.data(),dst.data(),s);
+  inputReady=NULL;
   a0.tile=keep[0]; a0.thr=keep[1];
   a0.tileB=keep[2]; a0.thrB=keep[3];
   if(e != cudaSuccess || !copyOut) return e;

@@ -143,6 +143,12 @@ private:
   // first host call measured fastest for inputs and outputs, -1 before.
   int hostTile, hostThr, hostTileB, hostThrB;
   int hostWay[2];
+  // Inputs copied one by one on a side stream: the first outer transform of
+  // input a waits for ready[a] (set while a host call copies inputs in,
+  // NULL otherwise), so the copies of later inputs overlap it.
+  cudaStream_t side;
+  std::vector<cudaEvent_t> ready;
+  const cudaEvent_t *inputReady;
   void allocate();
   void tune();
   bool directSegments() const;
