@@ -790,6 +790,7 @@ def run_batched(args):
     if clocks:
         clocks.begin()
     total = 0.0
+    torch.cuda.nvtx.range_push("timed")
     for _ in range(args.steps):
         flush.zero_()
         start.record(stream)
@@ -797,6 +798,7 @@ def run_batched(args):
         stop.record(stream)
         stop.synchronize()
         total += start.elapsed_time(stop)
+    torch.cuda.nvtx.range_pop()
     barrier_sync(world)
     if clocks:
         clocks.end()
@@ -891,6 +893,26 @@ def run_batched(args):
                "sample": f"a stride-{stride} sample of the 512 problems ({k} "
                          f"convolutions, {dt:.1f} s; numpy/scipy.fft "
                          f"restatement of FFTW++'s hybrid convolution)"}
+    # Compute roofline of the persistent launch: its FP64 (FP32)
+    # instructions per launch from the committed ncu summary over the live
+    # step, against the issue rate measured on this GPU.
+    compute = None
+    dfma, ffma = measured_fma_rates()
+    tag, rate, bound = (("DPINST", dfma, "fp64_issue") if prec == "f64" else
+                        ("SPINST", ffma, "fp32_issue"))
+    if rate:
+        compute = {"fp64_tflops_peak_measured": 2 * dfma / 1e12,
+                   "fp32_tflops_peak_measured": 2 * ffma / 1e12}
+        cnt = profile_figure(tag, "batched1d", "batch", prec)
+        if cnt:
+            per = total / args.steps * 1e-3
+            compute.update({
+                "bound": bound, "kernel": "batchKernel",
+                "achieved": cnt / per, "peak": rate,
+                "unit": ("FP64" if tag == "DPINST" else "FP32") + " inst/s",
+                "frac": cnt / per / rate,
+                "source": f"{tag} line (instructions per launch, ncu) "
+                          "under profiles/, peak from fgb_measure_fma_rate"})
     line = {
         "metric": METRIC, "value": value, "unit": "convs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -911,6 +933,7 @@ def run_batched(args):
                                                       prec),
                      "kernel": "batchKernel", "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": abytes},
+        "compute_roofline": compute,
         "rel_l2_vs_fp64_oracle_max_sample": max(errs),
         "separate_plain_launches": {"value": sep_same, "unit": "convs/s",
                                     "launches_per_step": sep_launches,
