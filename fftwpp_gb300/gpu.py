@@ -21,7 +21,29 @@ from ._native import (CENTERED, F32, F64, FF, HERMITIAN, MULT, PAD,
                       PRECISIONS, REAL)
 
 __all__ = ["HybridConvolution", "BatchedConvolution", "PaddedTransform",
-           "PAD", "CENTERED", "HERMITIAN", "REAL", "default_M"]
+           "PAD", "CENTERED", "HERMITIAN", "REAL", "default_M",
+           "set_autotune", "set_residue_search", "set_host_path"]
+
+
+def set_autotune(on: bool = True) -> None:
+    """Plan-time timing of schedules and of m, process-wide (fgb_set_autotune)."""
+    _native.load().fgb_set_autotune(int(bool(on)))
+
+
+def set_residue_search(on: bool = True) -> None:
+    """Timed choice of the residue block length m per axis, process-wide
+    (fgb_set_residue_search; the counterpart of FFTW++'s OptBase search)."""
+    _native.load().fgb_set_residue_search(int(bool(on)))
+
+
+def set_host_path(inputs: int = -1, outputs: int = -1) -> None:
+    """How page-locked host arrays cross the host link (fgb_set_host_path):
+    0 copies through device memory, 1 in place, 2 in place with 64-byte
+    column tiles, -1 measured per plan."""
+    for w in (inputs, outputs):
+        if w not in (-1, 0, 1, 2):
+            raise ValueError("host path ways are -1, 0, 1 or 2")
+    _native.load().fgb_set_host_path(int(inputs), int(outputs))
 
 
 def default_M(kind: int, L: int, A: int = 2) -> int:

@@ -203,3 +203,14 @@ def test_drop_in_precision_switch(native_lib):
     assert lib.fgb_get_drop_in_precision() == 2
     assert lib.fgb_set_drop_in_precision(0) == 0
     assert lib.fgb_get_drop_in_precision() == 0
+
+
+def test_python_switches(native_lib):
+    """The process-wide planning switches are reachable from Python and
+    validate their arguments (no GPU work)."""
+    from fftwpp_gb300 import gpu
+    gpu.set_autotune(True)
+    gpu.set_residue_search(True)
+    gpu.set_host_path(-1, -1)
+    with pytest.raises(ValueError):
+        gpu.set_host_path(3, 0)
