@@ -120,7 +120,7 @@ def synth_inputs(w, seed=1):
 # Clock sampling during the timed region.
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples every 50 ms; only samples stamped
+    """nvidia-smi clock/throttle samples every 20 ms; only samples stamped
     inside the timed window (begin() .. end()) are summarised.  start()
     returns once the first sample has arrived, so the sampler is running
     before the window opens."""
@@ -142,7 +142,7 @@ class ClockSampler:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}",
                  f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "50"], stdout=subprocess.PIPE,
+                 "-lms", "20"], stdout=subprocess.PIPE,
                 stderr=subprocess.DEVNULL, text=True, bufsize=1)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -347,13 +347,13 @@ def run_reference(args, w):
     fs = synth_inputs(w, seed=7)
     if w.get("batch", 1) > 1:
         fs = [f[0] for f in fs]
-    # Bound the run: about 20 s of warm-up and 120 s of timed work at most.
+    # Bound the run: about 15 s of warm-up and 60 s of timed work at most.
     t0 = time.perf_counter()
     H.convolve(fs, w["kinds"], w["L"], w["M"], ms=w.get("m"), mult=w["mult"],
                workers=workers)
     est = time.perf_counter() - t0
-    nwarm = min(args.warmup, max(1, int(20.0 / est))) - 1
-    ntimed = min(args.steps, max(1, int(120.0 / est)))
+    nwarm = min(args.warmup, max(1, int(15.0 / est))) - 1
+    ntimed = min(args.steps, max(1, int(60.0 / est)))
     for _ in range(nwarm):
         H.convolve(fs, w["kinds"], w["L"], w["M"], ms=w.get("m"), mult=w["mult"],
                    workers=workers)
@@ -983,7 +983,7 @@ def override(w, args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hconv2d",
