@@ -423,8 +423,12 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
            bool tuneSchedule)
   : batch(batch), staging(0), hostIn(NULL), hostOut(NULL), nlaunch(0),
     timing(false), normalize(true), marks(0), hostTile(0), hostThr(0),
-    hostTileB(0), hostThrB(0), side(NULL), inputReady(NULL)
+    hostTileB(0), hostThrB(0), side(NULL), chunks(0)
 {
+  for(int k=0; k < CHUNKS; ++k) {
+    lanes[k]=NULL;
+    chunkReady[k]=chunkDone[k]=NULL;
+  }
   hostWay[0]=hostWay[1]=-1;
   if(dim < 1 || dim > 3) throw std::runtime_error("dimension must be 1, 2 or 3");
   if(A < 1 || A > FGB_MAXA || B < 1 || B > A)
@@ -784,6 +788,11 @@ Conv::~Conv()
 {
   for(cudaEvent_t ev : events) cudaEventDestroy(ev);
   for(cudaEvent_t ev : ready) cudaEventDestroy(ev);
+  for(int k=0; k < CHUNKS; ++k) {
+    if(chunkReady[k]) cudaEventDestroy(chunkReady[k]);
+    if(chunkDone[k]) cudaEventDestroy(chunkDone[k]);
+    if(k > 0 && lanes[k]) cudaStreamDestroy(lanes[k]);
+  }
   if(side) cudaStreamDestroy(side);
   for(void *p : bufs) cudaFree(p);
   if(hostIn) cudaFree(hostIn);
@@ -906,29 +915,47 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   // Float-float mode: the first launch reads the caller's FP64 arrays and
   // the last one writes them.
   const int IN64=std::is_same<T,ff>::value ? 1 : 0, OUT64=2*IN64;
-  // The first outer-axis launch: one per input, each after its input's
-  // ready event, when a host call copies the inputs in one by one (with
-  // per-launch timing on, one launch after all of them).
+  // The first outer-axis launch.  While a host call copies the inputs in
+  // (chunks > 0): input 0 one launch per column range, each on its own
+  // stream after its range has landed, and every other input one launch
+  // after its copy; the call's stream then joins the range streams.  With
+  // per-launch timing on, one launch after every copy.
   auto firstOuter=[&](OuterPlan<T>& O, const AxisPlan& a) {
-    auto go=[&](OuterPlan<T>& Q) {
-      return a.kind == KIND_REAL ? launchOuterRealFwd<T>(Q,a.thr,s) :
-        launchOuterFwd<T>(Q,a.thr,s);
+    auto go=[&](OuterPlan<T>& Q, cudaStream_t st) {
+      return a.kind == KIND_REAL ? launchOuterRealFwd<T>(Q,a.thr,st) :
+        launchOuterFwd<T>(Q,a.thr,st);
     };
-    if(!inputReady) return go(O);
+    if(!chunks) return go(O,s);
     cudaError_t e;
     if(timing) {
-      for(int i=0; i < A; ++i)
-        if((e=cudaStreamWaitEvent(s,inputReady[i],0)) != cudaSuccess) return e;
-      return go(O);
+      for(int k=0; k < chunks; ++k)
+        if((e=cudaStreamWaitEvent(s,chunkReady[k],0)) != cudaSuccess) return e;
+      for(int i=1; i < A; ++i)
+        if((e=cudaStreamWaitEvent(s,ready[i],0)) != cudaSuccess) return e;
+      return go(O,s);
     }
     OuterPlan<T> Q=O;
     Q.count=1;
-    for(int i=0; i < A; ++i) {
-      if((e=cudaStreamWaitEvent(s,inputReady[i],0)) != cudaSuccess) return e;
+    const size_t eb=elemBytes();       // the caller's element on the input side
+    for(int k=0; k < chunks; ++k) {
+      cudaStream_t st=k == 0 ? s : lanes[k];
+      const long c0=chunkCol[k];
+      if((e=cudaStreamWaitEvent(st,chunkReady[k],0)) != cudaSuccess) return e;
+      Q.in[0]=(const Cx *) ((const char *) O.in[0]+c0*eb);
+      Q.out[0]=O.out[0]+c0;
+      Q.C=(int) (chunkCol[k+1]-c0);
+      if((e=go(Q,st)) != cudaSuccess) return e;
+      if(k > 0 && (e=cudaEventRecord(chunkDone[k],st)) != cudaSuccess) return e;
+    }
+    Q.C=O.C;
+    for(int i=1; i < A; ++i) {
+      if((e=cudaStreamWaitEvent(s,ready[i],0)) != cudaSuccess) return e;
       Q.in[0]=O.in[i];
       Q.out[0]=O.out[i];
-      if((e=go(Q)) != cudaSuccess) return e;
+      if((e=go(Q,s)) != cudaSuccess) return e;
     }
+    for(int k=1; k < chunks; ++k)
+      if((e=cudaStreamWaitEvent(s,chunkDone[k],0)) != cudaSuccess) return e;
     return cudaSuccess;
   };
 
@@ -1151,14 +1178,81 @@ bool Conv::directSegments() const
   return (size_t) a.tile*e >= 64 && (size_t) a.tileB*e >= 64;
 }
 
-// One convolution over page-locked arrays (mapped device addresses).  Each
+// Queues the copies of the inputs (host addresses) into device memory on
+// the side stream, after the work already queued on s: input 0 in column ranges (2D copies,
+// copy engines) so that its first transform starts on the first range,
+// the other inputs whole.  Sets chunks, chunkCol and the events the first
+// outer launch waits for.
+cudaError_t Conv::pipeInputs(const void *const *in, void *const *dev,
+                             cudaStream_t s)
+{
+  cudaError_t e;
+  const int A=I.A;
+  auto event=[](cudaEvent_t& ev) {
+    return ev ? cudaSuccess :
+      cudaEventCreateWithFlags(&ev,cudaEventDisableTiming);
+  };
+  if(!side && (e=cudaStreamCreateWithFlags(&side,cudaStreamNonBlocking)) !=
+     cudaSuccess) {
+    side=NULL;
+    return e;
+  }
+  while((int) ready.size() < A+1) {
+    cudaEvent_t ev=NULL;
+    if((e=event(ev)) != cudaSuccess) return e;
+    ready.push_back(ev);
+  }
+  // Column ranges of input 0, whole forward tiles each.
+  const size_t eb=elemBytes(), bytes=elements()*eb;
+  const long rows=I.axis[0].L, C=(long) elements()/rows;
+  const long unit=std::max(1,I.axis[0].tile);
+  const long units=(C+unit-1)/unit;
+  const long per=(units+CHUNKS-1)/CHUNKS;
+  int n=0;
+  chunkCol[0]=0;
+  while(chunkCol[n] < C) {
+    chunkCol[n+1]=std::min(C,chunkCol[n]+per*unit);
+    ++n;
+  }
+  for(int k=0; k < n; ++k) {
+    if((e=event(chunkReady[k])) != cudaSuccess ||
+       (e=event(chunkDone[k])) != cudaSuccess) return e;
+    if(k > 0 && !lanes[k] &&
+       (e=cudaStreamCreateWithFlags(&lanes[k],cudaStreamNonBlocking)) !=
+       cudaSuccess) {
+      lanes[k]=NULL;
+      return e;
+    }
+  }
+  // Copies (and the range streams) follow the work already queued on s.
+  if((e=cudaEventRecord(ready[A],s)) != cudaSuccess ||
+     (e=cudaStreamWaitEvent(side,ready[A],0)) != cudaSuccess) return e;
+  for(int k=0; k < n; ++k) {
+    const size_t off=chunkCol[k]*eb;
+    if((e=cudaMemcpy2DAsync((char *) dev[0]+off,C*eb,
+                            (const char *) in[0]+off,C*eb,
+                            (chunkCol[k+1]-chunkCol[k])*eb,rows,
+                            cudaMemcpyDefault,side)) != cudaSuccess ||
+       (e=cudaEventRecord(chunkReady[k],side)) != cudaSuccess) return e;
+  }
+  for(int a=1; a < A; ++a)
+    if((e=cudaMemcpyAsync(dev[a],in[a],bytes,cudaMemcpyDefault,side)) !=
+       cudaSuccess ||
+       (e=cudaEventRecord(ready[a],side)) != cudaSuccess) return e;
+  chunks=n;
+  return cudaSuccess;
+}
+
+// One convolution over page-locked arrays: hin the inputs' host addresses
+// (for the copy engines), in and out the mapped device addresses.  Each
 // side takes its own way over the host link: wayIn for the inputs, wayOut
-// for the outputs, HOST_COPY (whole arrays moved by the SMs through device
-// memory, 16-byte aligned), HOST_INPLACE (the first kernel reads, or the
+// for the outputs, HOST_COPY (whole arrays moved through device memory,
+// 16-byte aligned), HOST_INPLACE (the first kernel reads, or the
 // last one writes, the caller's arrays with the device-tuned axis-0 tiles)
 // or HOST_INPLACE64 (the same with the fastest tiles whose rows span at
 // least 64 bytes, whole lines of the link).
-cudaError_t Conv::runZeroCopy(const void *const *in, void *const *out,
+cudaError_t Conv::runZeroCopy(const void *const *hin, const void *const *in,
+                              void *const *out,
                               int wayIn, int wayOut, cudaStream_t s)
 {
   const size_t bytes=elements()*elemBytes();
@@ -1176,37 +1270,16 @@ cudaError_t Conv::runZeroCopy(const void *const *in, void *const *out,
   CopyArgs C;
   C.bytes=bytes;
   cudaError_t e;
-  // With two or more inputs and an outer axis, each input is copied on a
-  // side stream and its first transform starts as soon as it has arrived.
-  const bool pipeline=copyIn && A > 1 && I.dim > 1 && !I.longRow;
+  // With an outer axis, the inputs are copied on a side stream and the
+  // first transform of each piece starts as soon as it has arrived.
+  const bool pipeline=copyIn && I.dim > 1 && !I.longRow;
   if(pipeline) {
-    if(!side && cudaStreamCreateWithFlags(&side,cudaStreamNonBlocking) !=
-       cudaSuccess) {
-      side=NULL;
-      return cudaErrorMemoryAllocation;
+    std::vector<void *> dev(A);
+    for(int a=0; a < A; ++a) dev[a]=(void *) src[a];
+    if((e=pipeInputs(hin,dev.data(),s)) != cudaSuccess) {
+      chunks=0;
+      return e;
     }
-    while((int) ready.size() < A+1) {
-      cudaEvent_t ev;
-      if((e=cudaEventCreateWithFlags(&ev,cudaEventDisableTiming)) !=
-         cudaSuccess) return e;
-      ready.push_back(ev);
-    }
-    // The copies follow the work already queued on s (ready[A] marks it).
-    if((e=cudaEventRecord(ready[A],s)) != cudaSuccess ||
-       (e=cudaStreamWaitEvent(side,ready[A],0)) != cudaSuccess) return e;
-    // The first input moves with the SMs (nothing else runs yet); the
-    // later ones with the copy engines, which leave the SMs to the
-    // transforms they overlap.
-    C.count=1;
-    C.src[0]=in[0];
-    C.dst[0]=(void *) src[0];
-    if((e=launchBulkCopy(C,side)) != cudaSuccess ||
-       (e=cudaEventRecord(ready[0],side)) != cudaSuccess) return e;
-    for(int a=1; a < A; ++a)
-      if((e=cudaMemcpyAsync((void *) src[a],in[a],bytes,
-                            cudaMemcpyDefault,side)) != cudaSuccess ||
-         (e=cudaEventRecord(ready[a],side)) != cudaSuccess) return e;
-    inputReady=ready.data();
   } else if(copyIn) {
     C.count=A;
     for(int a=0; a < A; ++a) {C.src[a]=in[a]; C.dst[a]=(void *) src[a];}
@@ -1219,7 +1292,7 @@ cudaError_t Conv::runZeroCopy(const void *const *in, void *const *out,
     a0.tileB=hostTileB; a0.thrB=hostThrB;
   }
   e=run(src.data(),dst.data(),s);
-  inputReady=NULL;
+  chunks=0;
   a0.tile=keep[0]; a0.thr=keep[1];
   a0.tileB=keep[2]; a0.thrB=keep[3];
   if(e != cudaSuccess || !copyOut) return e;
@@ -1245,9 +1318,12 @@ void Conv::measureHostPath(cudaStream_t s)
   }
   std::memset(h,0,stride*n);
   void *d=mappedAddress(h);
-  std::vector<const void *> in(I.A);
+  std::vector<const void *> hin(I.A), in(I.A);
   std::vector<void *> out(I.B);
-  for(int a=0; a < I.A; ++a) in[a]=(char *) d+a*stride;
+  for(int a=0; a < I.A; ++a) {
+    hin[a]=(char *) h+a*stride;
+    in[a]=(char *) d+a*stride;
+  }
   for(int b=0; b < I.B; ++b) out[b]=(char *) d+b*stride;
   std::vector<std::pair<int,int>> ways;
   for(int wi=HOST_COPY; wi <= HOST_INPLACE64; ++wi)
@@ -1257,13 +1333,14 @@ void Conv::measureHostPath(cudaStream_t s)
   cudaEvent_t e0=NULL, e1=NULL;
   bool ok=d && cudaEventCreate(&e0) == cudaSuccess &&
     cudaEventCreate(&e1) == cudaSuccess;
-  ok=ok && runZeroCopy(in.data(),out.data(),HOST_COPY,HOST_COPY,s) ==
+  ok=ok && runZeroCopy(hin.data(),in.data(),out.data(),HOST_COPY,HOST_COPY,s) ==
     cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
   double best=1e300;
   for(int rep=0; rep < 3 && ok; ++rep)
     for(const auto& w : ways) {
       ok=cudaEventRecord(e0,s) == cudaSuccess &&
-        runZeroCopy(in.data(),out.data(),w.first,w.second,s) == cudaSuccess &&
+        runZeroCopy(hin.data(),in.data(),out.data(),w.first,w.second,s) ==
+        cudaSuccess &&
         cudaEventRecord(e1,s) == cudaSuccess &&
         cudaStreamSynchronize(s) == cudaSuccess;
       float ms=0;
@@ -1324,7 +1401,7 @@ cudaError_t Conv::runHost(const void *const *in, void *const *out,
         if(wi == HOST_COPY) wi=HOST_INPLACE;
         if(wo == HOST_COPY) wo=HOST_INPLACE;
       }
-      cudaError_t e=runZeroCopy(min.data(),mout.data(),wi,wo,s);
+      cudaError_t e=runZeroCopy(in,min.data(),mout.data(),wi,wo,s);
       return e != cudaSuccess ? e : cudaStreamSynchronize(s);
     }
   }

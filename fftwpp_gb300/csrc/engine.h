@@ -143,17 +143,27 @@ private:
   // first host call measured fastest for inputs and outputs, -1 before.
   int hostTile, hostThr, hostTileB, hostThrB;
   int hostWay[2];
-  // Inputs copied one by one on a side stream: the first outer transform of
-  // input a waits for ready[a] (set while a host call copies inputs in,
-  // NULL otherwise), so the copies of later inputs overlap it.
+  // Inputs copied in from the host on a side stream while the first outer
+  // transform runs.  Input 0 arrives in `chunks` column ranges
+  // [chunkCol[k], chunkCol[k+1]); the transform of range k runs on lanes[k]
+  // (lanes[0]: the call's stream) after chunkReady[k], so the ranges run
+  // concurrently as they land.  Input a > 0 arrives whole; its transform
+  // waits for ready[a].  chunks = 0 outside such a host call.
+  static const int CHUNKS=4;
   cudaStream_t side;
-  std::vector<cudaEvent_t> ready;
-  const cudaEvent_t *inputReady;
+  cudaStream_t lanes[CHUNKS];
+  std::vector<cudaEvent_t> ready;            // per input, then a start mark
+  cudaEvent_t chunkReady[CHUNKS], chunkDone[CHUNKS];
+  int chunks;
+  long chunkCol[CHUNKS+1];
+  cudaError_t pipeInputs(const void *const *in, void *const *dev,
+                         cudaStream_t s);
   void allocate();
   void tune();
   bool directSegments() const;
-  cudaError_t runZeroCopy(const void *const *in, void *const *out,
-                          int wayIn, int wayOut, cudaStream_t s);
+  cudaError_t runZeroCopy(const void *const *hin, const void *const *in,
+                          void *const *out, int wayIn, int wayOut,
+                          cudaStream_t s);
   void measureHostPath(cudaStream_t s);
 };
 
