@@ -1179,10 +1179,10 @@ bool Conv::directSegments() const
 }
 
 // Queues the copies of the inputs (host addresses) into device memory on
-// the side stream, after the work already queued on s: input 0 in column ranges (2D copies,
-// copy engines) so that its first transform starts on the first range,
-// the other inputs whole.  Sets chunks, chunkCol and the events the first
-// outer launch waits for.
+// the side stream, after the work already queued on s: input 0 in column
+// ranges (2D copies, copy engines) so that its first transform starts on
+// the first range, the other inputs whole.  Sets chunks, chunkCol and the
+// events the first outer launch waits for.
 cudaError_t Conv::pipeInputs(const void *const *in, void *const *dev,
                              cudaStream_t s)
 {
