@@ -717,6 +717,326 @@ def oracle_batch_rate(Ls, f, g, budget_s, workers, stride=None):
     return len(idx) / dt, len(idx), dt, stride
 
 
+GRAD_DESC = ("differentiable 2D advection Jacobian on 1023x512 "
+             "centred-Hermitian modes (Lx=Ly=1023), 2/3 rule (M=1534): one "
+             "step = J(psi, omega) from the four derivative fields, loss = "
+             "sum |J|^2, backward through the adjoint convolution (A=5, B=4); "
+             "2 dealiased convolutions per step; psi, omega with amplitude "
+             "|k|^-2 and seeded random phases")
+
+
+def grad_spectra(Lx, Ly, seed):
+    """psi, omega with amplitude |k|^-2 (0 at k=0) and uniform random
+    phases, Hermitian-symmetrised on the k_y = 0 column."""
+    from oracle import hybrid as H
+    Hy = (Ly + 1) // 2
+    rng = np.random.default_rng(seed)
+    kx = (np.arange(Lx) - Lx // 2)[:, None]
+    ky = np.arange(Hy)[None, :]
+    k2 = (kx ** 2 + ky ** 2).astype(float)
+    amp = np.where(k2 > 0, 1.0 / np.where(k2 > 0, k2, 1.0), 0.0)
+    out = []
+    for _ in range(2):
+        f = amp * np.exp(2j * np.pi * rng.uniform(size=(Lx, Hy)))
+        H.hermitian_symmetrize_x(f, (Lx + 1) // 2, Hy, Lx // 2)
+        out.append(np.ascontiguousarray(f))
+    return out
+
+
+def oracle_grad_step(psi, omega, Lx, Ly, workers):
+    """One gradient step of loss = sum |J|^2 on the CPU restatement: the
+    forward Jacobian convolution and the adjoint convolution (the same
+    algebra as fftwpp_gb300.autograd), numpy elsewhere."""
+    from oracle import hybrid as H
+    kinds = [H.CENTERED, H.HERMITIAN]
+    M = [H.default_M(k, l) for k, l in zip(kinds, [Lx, Ly])]
+    Hy = (Ly + 1) // 2
+    kx = (np.arange(Lx) - Lx // 2)[:, None]
+    ky = np.arange(Hy)[None, :]
+    a = [1j * kx * psi, 1j * ky * psi, 1j * kx * omega, 1j * ky * omega]
+    J = H.convolve(a, kinds, [Lx, Ly], M, mult="realjacobian",
+                   workers=workers)[0]
+    w = np.ones((1, Hy))
+    w[0, 1:] = 2.0
+    G = 2 * J / w
+    g = H.convolve(a + [G], kinds, [Lx, Ly], M, mult="realjacadj", B=4,
+                   workers=workers)
+    g = [w * x for x in g]
+    # Chain rule through a = (i kx psi, i ky psi, i kx omega, i ky omega).
+    gp = np.conj(1j * kx) * g[0] + np.conj(1j * ky) * g[1]
+    go = np.conj(1j * kx) * g[2] + np.conj(1j * ky) * g[3]
+    return float(np.sum(np.abs(J) ** 2)), gp, go
+
+
+def run_jacobian_grad(args):
+    """C5: forward + loss + adjoint backward of the differentiable 2D
+    advection Jacobian through torch.autograd, timed per step on the
+    device; the adjoint checked at full size against central differences
+    (FP64, float-float) or against the FP64 gradient (FP32)."""
+    import torch
+    world, rank, local = dist_setup()
+    if world > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from fftwpp_gb300.autograd import AdvectionJacobian
+    prec = args.precision
+    Lx = Ly = 1023
+    op = AdvectionJacobian(Lx, Ly, precision=prec)
+    cdt = op.dtype
+    p0, o0 = grad_spectra(Lx, Ly, seed=11)
+    psi = torch.from_numpy(p0).to(cdt).cuda().requires_grad_(True)
+    omega = torch.from_numpy(o0).to(cdt).cuda().requires_grad_(True)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step(p, o):
+        J = op(p, o)
+        loss = (J.real ** 2 + J.imag ** 2).sum()
+        loss.backward()
+        return loss
+
+    for _ in range(args.warmup):
+        psi.grad = omega.grad = None
+        step(psi, omega)
+    clocks = ClockSampler(local) if rank == 0 else None
+    if clocks:
+        clocks.start()
+    barrier_sync(world)
+    if clocks:
+        clocks.begin()
+    torch.cuda.nvtx.range_push("timed")
+    # The backward pass runs on autograd's device thread, outside this
+    # thread's NVTX range: profiler start/stop (process-wide) brackets the
+    # timed steps for a profiler run with profiling off at start.
+    torch.cuda.profiler.start()
+    op.fwd.enable_timing(True)
+    op.adj.enable_timing(True)
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    total = 0.0
+    for _ in range(args.steps):
+        psi.grad = omega.grad = None
+        flush.zero_()
+        start.record(stream)
+        step(psi, omega)
+        stop.record(stream)
+        stop.synchronize()
+        total += start.elapsed_time(stop)
+        op.fwd.collect_timing()
+        op.adj.collect_timing()
+    torch.cuda.profiler.stop()
+    torch.cuda.nvtx.range_pop()
+    barrier_sync(world)
+    if clocks:
+        clocks.end()
+    clk = clocks.stop() if clocks else None
+    kf = [t / args.steps for t in op.fwd.kernel_ms()]
+    ka = [t / args.steps for t in op.adj.kernel_ms()]
+    op.fwd.enable_timing(False)
+    op.adj.enable_timing(False)
+    if world > 1:
+        t = torch.tensor([total], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total = float(t.item())
+    ms = total / args.steps
+    value = world * 2 * args.steps / (total * 1e-3)
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return 0
+
+    # Roofline of the dominant kernel: its convolution's compulsory bytes
+    # (inputs read + outputs written at the stored size) over its launch.
+    names = [f"fwd/{n}" for n in op.fwd.launch_names()] + \
+        [f"adj/{n}" for n in op.adj.launch_names()]
+    per = kf + ka
+    dom = int(np.argmax(per))
+    nmodes = Lx * ((Ly + 1) // 2)
+    elem = 8 if prec == "f32" else 16
+    conv_bytes = ((4 + 1) if dom < len(kf) else (5 + 4)) * elem * nmodes
+    peaks = {}
+    pfile = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pfile):
+        peaks = json.load(open(pfile))
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured"
+    if not peak:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = conv_bytes / (per[dom] * 1e-3) / 1e9
+    step_bytes = (5 + 9) * elem * nmodes
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic_from_profiles("jacobian2d_grad",
+                                                 names[dom], prec),
+                "kernel": names[dom], "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": conv_bytes,
+                "whole_step_frac": step_bytes / (ms * 1e-3) / 1e9 / peak}
+    compute = None
+    dfma, ffma = measured_fma_rates()
+    tag, rate, bound = (("DPINST", dfma, "fp64_issue") if prec == "f64" else
+                        ("SPINST", ffma, "fp32_issue"))
+    if rate:
+        compute = {"fp64_tflops_peak_measured": 2 * dfma / 1e12,
+                   "fp32_tflops_peak_measured": 2 * ffma / 1e12}
+        cnt = profile_figure(tag, "jacobian2d_grad", names[dom], prec)
+        if cnt:
+            compute.update({
+                "bound": bound, "kernel": names[dom],
+                "achieved": cnt / (per[dom] * 1e-3), "peak": rate,
+                "unit": ("FP64" if tag == "DPINST" else "FP32") + " inst/s",
+                "frac": cnt / (per[dom] * 1e-3) / rate,
+                "source": f"{tag} line (instructions per launch, ncu) "
+                          "under profiles/, peak from fgb_measure_fma_rate"})
+
+    # The adjoint at full size: central differences along random directions
+    # (FP64 and float-float), or the FP32 gradient against the FP64 one.
+    def loss_of(p, o):
+        J = op(p, o)
+        return (J.real ** 2 + J.imag ** 2).sum()
+    psi.grad = omega.grad = None
+    loss = loss_of(psi, omega)
+    gp, go = torch.autograd.grad(loss, (psi, omega))
+    check = {}
+    if prec == "f32":
+        ref = AdvectionJacobian(Lx, Ly, precision="f64")
+        p64 = psi.detach().to(torch.complex128).requires_grad_(True)
+        o64 = omega.detach().to(torch.complex128).requires_grad_(True)
+        l64 = (lambda J: (J.real ** 2 + J.imag ** 2).sum())(ref(p64, o64))
+        gp64, go64 = torch.autograd.grad(l64, (p64, o64))
+        num = float((gp.to(torch.complex128) - gp64).abs().pow(2).sum() +
+                    (go.to(torch.complex128) - go64).abs().pow(2).sum())
+        den = float(gp64.abs().pow(2).sum() + go64.abs().pow(2).sum())
+        check = {"fp32_gradient_rel_l2_vs_fp64": (num / den) ** 0.5}
+        del ref
+    else:
+        # Directions with the spectra's |k|^-2 amplitude, so that h v is a
+        # relative perturbation of every mode (white-noise directions would
+        # swamp the ~1e-6 high-k modes and measure the h^2 term instead).
+        rng = np.random.default_rng(17)
+        h, worst, ndir = 1e-6, 0.0, 16
+        kx = (np.arange(Lx) - Lx // 2)[:, None]
+        ky = np.arange((Ly + 1) // 2)[None, :]
+        k2 = (kx ** 2 + ky ** 2).astype(float)
+        amp = np.where(k2 > 0, 1.0 / np.where(k2 > 0, k2, 1.0), 0.0)
+        with torch.no_grad():
+            for _ in range(ndir):
+                vp = torch.from_numpy(amp * (rng.normal(size=p0.shape) + 1j *
+                                             rng.normal(size=p0.shape))
+                                      ).to(cdt).cuda()
+                vo = torch.from_numpy(amp * (rng.normal(size=p0.shape) + 1j *
+                                             rng.normal(size=p0.shape))
+                                      ).to(cdt).cuda()
+                lp = loss_of(psi + h * vp, omega + h * vo)
+                lm = loss_of(psi - h * vp, omega - h * vo)
+                fd = float((lp - lm) / (2 * h))
+                an = float((torch.conj(gp) * vp).real.sum() +
+                           (torch.conj(go) * vo).real.sum())
+                worst = max(worst, abs(fd - an) / max(abs(an), 1e-300))
+        check = {"adjoint_vs_central_differences": {
+            "directions": ndir, "h": h, "max_rel_err": worst}}
+
+    # End to end: page-locked spectra copied in, the step, the loss read
+    # back, every step.
+    hp = torch.from_numpy(p0).to(cdt).pin_memory()
+    ho = torch.from_numpy(o0).to(cdt).pin_memory()
+    dp = torch.empty_like(psi)
+    do = torch.empty_like(omega)
+    for _ in range(args.warmup):
+        dp.copy_(hp, non_blocking=True)
+        do.copy_(ho, non_blocking=True)
+        x = dp.detach().requires_grad_(True)
+        y = do.detach().requires_grad_(True)
+        float(step(x, y).detach())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dp.copy_(hp, non_blocking=True)
+        do.copy_(ho, non_blocking=True)
+        x = dp.detach().requires_grad_(True)
+        y = do.detach().requires_grad_(True)
+        float(step(x, y).detach())
+    e2e_dt = time.perf_counter() - t0
+    e2e = {"value": 2 * args.steps / e2e_dt, "unit": "convs/s",
+           "grad_steps_per_s": args.steps / e2e_dt,
+           "h2d_bytes_per_step": hp.nbytes + ho.nbytes,
+           "d2h_bytes_per_step": 8 if prec != "f32" else 4,
+           "api": "fftwpp_gb300.autograd.AdvectionJacobian (page-locked "
+                  "spectra copied in, the loss read back)"}
+
+    # CPU: the same step on the restatement, a bounded sample.
+    workers = os.cpu_count() or 1
+    n, t0 = 0, time.perf_counter()
+    while True:
+        oracle_grad_step(p0, o0, Lx, Ly, workers)
+        n += 1
+        if time.perf_counter() - t0 > args.cpu_budget:
+            break
+    cdt_s = time.perf_counter() - t0
+    cpu = {"value": 2 * n / cdt_s, "unit": "convs/s", "cores": workers,
+           "kind": "port",
+           "sample": f"{n} gradient steps ({2 * n} convolutions) in "
+                     f"{cdt_s:.1f} s (numpy/scipy.fft restatement of "
+                     "FFTW++'s hybrid convolution, forward and adjoint)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "convs/s",
+        "grad_steps_per_s": value / 2, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": prec,
+        "data": "synthetic (seeded)",
+        "config": {"workload": GRAD_DESC,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "flushed (256 MB write) before every timed step"},
+        "roofline": roofline, "compute_roofline": compute,
+        "kernels_ms_per_step": dict(zip(names, per)),
+        **check,
+        "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": args.steps * (op.fwd.launches + op.adj.launches + 5),
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_reference_grad(args):
+    """--impl reference for the gradient step: the CPU restatement's
+    forward and adjoint convolutions on every host core."""
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    workers = os.cpu_count() or 1
+    Lx = Ly = 1023
+    p0, o0 = grad_spectra(Lx, Ly, seed=11)
+    t0 = time.perf_counter()
+    oracle_grad_step(p0, o0, Lx, Ly, workers)
+    est = time.perf_counter() - t0
+    nwarm = min(args.warmup, max(1, int(15.0 / est))) - 1
+    ntimed = min(args.steps, max(1, int(60.0 / est)))
+    for _ in range(nwarm):
+        oracle_grad_step(p0, o0, Lx, Ly, workers)
+    t0 = time.perf_counter()
+    for _ in range(ntimed):
+        oracle_grad_step(p0, o0, Lx, Ly, workers)
+    dt = time.perf_counter() - t0
+    value = 2 * ntimed / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value,
+        "unit": "convs/s", "grad_steps_per_s": value / 2,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / ntimed * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": GRAD_DESC, "parallelism": "cpu"},
+        "cpu_baseline": {"value": value, "unit": "convs/s", "cores": workers,
+                         "kind": "port",
+                         "sample": f"{ntimed} timed gradient steps"},
+        "e2e": {"value": value, "unit": "convs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference_batched(args):
     """--impl reference for the batched workload: the CPU restatement over
     the same problem distribution, one bounded strided sample per step."""
@@ -987,7 +1307,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hconv2d",
-                    choices=sorted(WORKLOADS) + ["batched1d"])
+                    choices=sorted(WORKLOADS) + ["batched1d",
+                                                 "jacobian2d_grad"])
     ap.add_argument("--precision", default="f64", choices=["f64", "f32", "ff"])
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--L", help="comma-separated data lengths per axis, "
@@ -1005,6 +1326,10 @@ def main():
         if args.impl == "reference":
             return run_reference_batched(args)
         return run_batched(args)
+    if args.workload == "jacobian2d_grad":
+        if args.impl == "reference":
+            return run_reference_grad(args)
+        return run_jacobian_grad(args)
     w = override(WORKLOADS[args.workload], args)
     if args.impl == "reference":
         return run_reference(args, w)
