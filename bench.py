@@ -780,7 +780,7 @@ def run_jacobian_grad(args):
         torch.distributed.init_process_group("nccl")
     else:
         torch.cuda.set_device(0)
-    from fftwpp_gb300.autograd import AdvectionJacobian
+    from fftwpp_gb300.autograd import AdvectionJacobian, GraphedLossStep
     prec = args.precision
     Lx = Ly = 1023
     op = AdvectionJacobian(Lx, Ly, precision=prec)
@@ -804,8 +804,6 @@ def run_jacobian_grad(args):
     if clocks:
         clocks.start()
     barrier_sync(world)
-    if clocks:
-        clocks.begin()
     torch.cuda.nvtx.range_push("timed")
     # The backward pass runs on autograd's device thread, outside this
     # thread's NVTX range: profiler start/stop (process-wide) brackets the
@@ -829,13 +827,33 @@ def run_jacobian_grad(args):
     torch.cuda.profiler.stop()
     torch.cuda.nvtx.range_pop()
     barrier_sync(world)
-    if clocks:
-        clocks.end()
-    clk = clocks.stop() if clocks else None
     kf = [t / args.steps for t in op.fwd.kernel_ms()]
     ka = [t / args.steps for t in op.adj.kernel_ms()]
     op.fwd.enable_timing(False)
     op.adj.enable_timing(False)
+    eager_total = total
+
+    # The same step captured once in a CUDA graph and replayed: the value.
+    graphed = GraphedLossStep(op, psi.detach(), omega.detach())
+    for _ in range(args.warmup):
+        graphed()
+    barrier_sync(world)
+    if clocks:
+        clocks.begin()
+    torch.cuda.nvtx.range_push("timed")
+    total = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        start.record(stream)
+        graphed()
+        stop.record(stream)
+        stop.synchronize()
+        total += start.elapsed_time(stop)
+    torch.cuda.nvtx.range_pop()
+    barrier_sync(world)
+    if clocks:
+        clocks.end()
+    clk = clocks.stop() if clocks else None
     if world > 1:
         t = torch.tensor([total], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -936,33 +954,30 @@ def run_jacobian_grad(args):
         check = {"adjoint_vs_central_differences": {
             "directions": ndir, "h": h, "max_rel_err": worst}}
 
-    # End to end: page-locked spectra copied in, the step, the loss read
-    # back, every step.
+    # End to end: page-locked spectra copied into the graph's inputs, the
+    # graphed step, the loss read back, every step.
     hp = torch.from_numpy(p0).to(cdt).pin_memory()
     ho = torch.from_numpy(o0).to(cdt).pin_memory()
-    dp = torch.empty_like(psi)
-    do = torch.empty_like(omega)
+
+    def e2e_step():
+        with torch.no_grad():
+            graphed.psi.copy_(hp, non_blocking=True)
+            graphed.omega.copy_(ho, non_blocking=True)
+        return float(graphed()[0])
     for _ in range(args.warmup):
-        dp.copy_(hp, non_blocking=True)
-        do.copy_(ho, non_blocking=True)
-        x = dp.detach().requires_grad_(True)
-        y = do.detach().requires_grad_(True)
-        float(step(x, y).detach())
+        e2e_step()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        dp.copy_(hp, non_blocking=True)
-        do.copy_(ho, non_blocking=True)
-        x = dp.detach().requires_grad_(True)
-        y = do.detach().requires_grad_(True)
-        float(step(x, y).detach())
+        e2e_step()
     e2e_dt = time.perf_counter() - t0
     e2e = {"value": 2 * args.steps / e2e_dt, "unit": "convs/s",
            "grad_steps_per_s": args.steps / e2e_dt,
            "h2d_bytes_per_step": hp.nbytes + ho.nbytes,
            "d2h_bytes_per_step": 8 if prec != "f32" else 4,
-           "api": "fftwpp_gb300.autograd.AdvectionJacobian (page-locked "
-                  "spectra copied in, the loss read back)"}
+           "api": "fftwpp_gb300.autograd.GraphedLossStep over "
+                  "AdvectionJacobian (page-locked spectra copied in, the "
+                  "loss read back)"}
 
     # CPU: the same step on the restatement, a bounded sample.
     workers = os.cpu_count() or 1
@@ -989,6 +1004,12 @@ def run_jacobian_grad(args):
                    "l2": "flushed (256 MB write) before every timed step"},
         "roofline": roofline, "compute_roofline": compute,
         "kernels_ms_per_step": dict(zip(names, per)),
+        "eager_autograd": {"value": world * 2 * args.steps /
+                           (eager_total * 1e-3), "unit": "convs/s",
+                           "ms_per_step": eager_total / args.steps,
+                           "note": "the same step launched op by op; "
+                                   "kernel times above are from it"},
+        "graph": "the step is one CUDA graph replay (GraphedLossStep)",
         **check,
         "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": args.steps * (op.fwd.launches + op.adj.launches + 5),

@@ -31,7 +31,7 @@ import torch
 from . import _native
 from .gpu import CENTERED, HERMITIAN, HybridConvolution
 
-__all__ = ["AdvectionJacobian", "wavenumbers"]
+__all__ = ["AdvectionJacobian", "GraphedLossStep", "wavenumbers"]
 
 
 def wavenumbers(Lx: int, Ly: int, device=None, dtype=torch.float64):
@@ -103,3 +103,48 @@ class AdvectionJacobian:
         ikx = 1j * kx
         iky = 1j * ky
         return self.jacobian(ikx * psi, iky * psi, ikx * omega, iky * omega)
+
+
+def _sum_sq(J):
+    return (J.real ** 2 + J.imag ** 2).sum()
+
+
+class GraphedLossStep:
+    """A training step (J from psi and omega, loss, gradients) captured
+    once in a CUDA graph and replayed: the forward Jacobian convolution,
+    the loss, the adjoint convolution and the chain rule run as one graph
+    launch, without the per-operation launch cost of eager autograd.
+
+    psi and omega are the static input tensors (CUDA, the operator's dtype):
+    write new values into them (copy_) between calls.  Each call returns
+    the static (loss, dL/dpsi, dL/domega) tensors, overwritten by the next
+    call.  loss_fn maps J to a scalar (default: sum |J|^2)."""
+
+    def __init__(self, op: AdvectionJacobian, psi, omega, loss_fn=None):
+        if psi.dtype != op.dtype or omega.dtype != op.dtype:
+            raise ValueError(f"psi and omega must be {op.dtype} tensors")
+        loss_fn = loss_fn or _sum_sq
+        self.psi = psi.detach().requires_grad_(True)
+        self.omega = omega.detach().requires_grad_(True)
+
+        def body():
+            loss = loss_fn(op(self.psi, self.omega))
+            gp, go = torch.autograd.grad(loss, (self.psi, self.omega))
+            return loss.detach(), gp, go
+
+        # Warm-up on a side stream (allocator pools, plan caches), then
+        # capture on it.
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                body()
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.out = body()
+
+    def __call__(self):
+        self.graph.replay()
+        return self.out
+

@@ -156,3 +156,35 @@ def test_float_float_gradient_matches_fp64(native_lib):
                        for g in torch.autograd.grad(loss, (psi, omega))]
     for gff, g64 in zip(grads["ff"], grads["f64"]):
         assert rel_l2(gff, g64) <= 1e-12
+
+
+@pytest.mark.parametrize("precision", ["f64", "ff", "f32"])
+def test_graphed_loss_step(native_lib, precision):
+    """The CUDA-graph training step (forward, loss, adjoint backward in one
+    replay) gives the eager autograd loss and gradients, and recomputes
+    from new values written into its static inputs."""
+    import torch
+    from fftwpp_gb300.autograd import AdvectionJacobian, GraphedLossStep
+    Lx = Ly = 63
+    op = AdvectionJacobian(Lx, Ly, precision)
+    dt = op.dtype
+    psi, omega = spectra(Lx, Ly, 5, dt)
+    p2, o2 = spectra(Lx, Ly, 6, dt)
+
+    def eager(p, o):
+        p = p.detach().requires_grad_(True)
+        o = o.detach().requires_grad_(True)
+        loss = _loss(op, p, o)
+        gp, go = torch.autograd.grad(loss, (p, o))
+        return loss.detach(), gp, go
+
+    step = GraphedLossStep(op, psi.clone(), omega.clone())
+    for p, o in ((psi, omega), (p2, o2)):
+        with torch.no_grad():
+            step.psi.copy_(p)
+            step.omega.copy_(o)
+        got = [t.clone() for t in step()]
+        want = eager(p, o)
+        torch.cuda.synchronize()
+        for g, w in zip(got, want):
+            assert torch.equal(g, w)
