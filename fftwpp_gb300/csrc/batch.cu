@@ -277,6 +277,7 @@ void BatchConv::build()
       R.A=A; R.B=B; R.mult=mult; R.realIO=0; R.rpc=1;
       R.scale=(T) (1.0/(double) (m*q));
       R.fp=fftPlanPublic(m,prec,prec != PREC_F64);   // in-place rows in FP32
+      R.direct=0;
       R.twN=(const Tw *) twiddles(m*q,prec);
       R.rowStride=L; R.nrows=1;
       for(int a=0; a < A; ++a) R.in[a]=(const cplx<T> *) (offsets[i]*e);
@@ -321,6 +322,7 @@ void BatchConv::build()
       R.L=(int) m; R.m=(int) m; R.q=1; R.N=(int) m; R.cshift=0;
       R.A=A; R.B=B; R.mult=mult; R.realIO=0; R.rpc=rpc; R.scale=(T) 1;
       R.fp=fftPlanPublic(m,prec,prec != PREC_F64);   // in-place rows in FP32
+      R.direct=0;
       R.twN=(const Tw *) twiddles(m,prec);
       R.rowStride=m; R.nrows=qc;
       P.rel=4|8;

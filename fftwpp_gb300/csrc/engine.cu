@@ -218,9 +218,11 @@ static bool wide(int prec) {return prec != PREC_F32;}
   (prec) == PREC_FF ? F<ff>(__VA_ARGS__) : F<float>(__VA_ARGS__))
 static size_t elem(int prec) {return wide(prec) ? 16 : 8;}
 
-static size_t rowNeed(int prec, long L, long m, int A, int B, int rpc=1)
+// direct: a row plan with one residue and one fold (RowPlan::direct).
+static size_t rowNeed(int prec, long L, long m, int A, int B, int rpc=1,
+                      int direct=0)
 {
-  return FGB_BY_PREC(prec,rowSmem,L,m,A,B,rpc);
+  return FGB_BY_PREC(prec,rowSmem,L,m,A,B,rpc,direct);
 }
 
 static size_t hermNeed(int prec, long H, long Nh, int A, int rpc=1)
@@ -520,13 +522,14 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
   for(int d=0; d < dim-1; ++d) nrows *= I.axis[d].rows;
   if(I.longRow) {
     in.rpc=pickRpc(I.rowM,A,I.rowQ,[&](int r) {
-      return rowNeed(prec,I.rowM,I.rowM,A,B,r);});
+      return rowNeed(prec,I.rowM,I.rowM,A,B,r,1);});
   } else if(in.kind == KIND_HERMITIAN) {
     in.rpc=pickRpc(in.N/2,A,nrows,[&](int r) {
       return hermNeed(prec,in.stored,in.N/2,A,r);});
   } else {
     in.rpc=pickRpc(in.m,A,nrows,[&](int r) {
-      return rowNeed(prec,in.stored,in.m,A,B,r);});
+      return rowNeed(prec,in.stored,in.m,A,B,r,
+                     in.q == 1 && in.stored <= in.m);});
   }
   try {
     allocate();
@@ -674,9 +677,9 @@ void Conv::tune()
     long avail=I.longRow ? I.rowQ : nrows;
     for(int r : {1,2,3,4,6,8}) {
       if(r > avail) break;
-      size_t need=I.longRow ? rowNeed(prec,I.rowM,I.rowM,A,B,r) :
+      size_t need=I.longRow ? rowNeed(prec,I.rowM,I.rowM,A,B,r,1) :
         in.kind == KIND_HERMITIAN ? hermNeed(prec,in.stored,in.N/2,A,r) :
-        rowNeed(prec,in.stored,in.m,A,B,r);
+        rowNeed(prec,in.stored,in.m,A,B,r,in.q == 1 && in.stored <= in.m);
       if(need <= SMEM_MAX)
         for(int th : thrs) t.cands.push_back({r,th});
     }
@@ -891,6 +894,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.realIO=a.kind == KIND_REAL && I.dim == 1;
     P.rpc=I.axis[I.dim-1].rpc;
     P.io64=0;
+    P.direct=a.q == 1 && a.stored <= a.m;
     P.fp=fftPlan(a.m,I.prec,inplaceFFT<T>());
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };

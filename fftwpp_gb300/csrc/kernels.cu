@@ -313,7 +313,7 @@ __device__ __forceinline__ void cpAsyncWait()
 // together as interleaved columns col = a*rpc + rho, so the B x rpc output
 // columns are a contiguous prefix for the inverse transforms.  Every thread
 // of the block calls it.
-template<typename T, bool CG, int K>
+template<typename T, bool CG, int K, bool D=false>
 __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
                                            long long group,
                                            unsigned char *smemRaw)
@@ -329,6 +329,74 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
   const UDiv dL(L), dLd(ld);
   const UDiv dR(R);
   const long long row0=group*R;
+
+  if constexpr(D) {
+    // One residue, one fold (RowPlan::direct; its own instantiation, so
+    // that the staged path's registers do not weigh on it or it on them): slot t of column col holds f[(t + c) mod m]
+    // (zero beyond L).  Reads run along each row (coalesced), FGB_LOADS
+    // iterations of loads issued before any is used.
+    cplx<T> *x=(cplx<T> *) smemRaw;
+    cplx<T> *y=x+padded(m*ld);
+    const UDiv dM(m);
+    for(int i0=tid; i0 < m*ld; i0 += FGB_LOADS*nthr) {
+      cplx<T> v[FGB_LOADS];
+#pragma unroll
+      for(int u=0; u < FGB_LOADS; ++u) {
+        const int i=i0+u*nthr;
+        v[u]=mk((T) 0,(T) 0);
+        if(i >= m*ld) continue;
+        int col=dM(i), s=i-col*m;
+        int a=dR(col);
+        long long row=row0+col-a*R;
+        if(s < L && row < P.nrows) {
+          long long off=row*P.rowStride+s;
+          if(P.realIO) v[u]=mk(loadIOr((const T *) P.in[a]+off,P.io64 & 1),(T) 0);
+          else if(P.io64 & 1) v[u]=loadIO(P.in[a]+off,true);
+          else v[u]=ldx<CG>(P.in[a]+off);
+        }
+      }
+#pragma unroll
+      for(int u=0; u < FGB_LOADS; ++u) {
+        const int i=i0+u*nthr;
+        if(i >= m*ld) break;
+        int col=dM(i), s=i-col*m;
+        x[sp(posmod(s-c,m)*ld+col)]=v[u];
+      }
+    }
+    __syncthreads();
+    const cplx<T> *Z;
+    if constexpr(inplaceFFT<T>()) {
+      fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
+      for(int i=tid; i < m*R; i += nthr) {
+        int j=dR(i), rho=i-j*R;
+        multiplySlot<K>(x,j*ld+rho,R,A,B,P.mult);
+      }
+      __syncthreads();
+      fftDIT<T,-1>(x,P.fp,lb,ld,tid,nthr);
+      Z=x;
+    } else {
+      cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
+      cplx<T> *Y=X == x ? y : x;
+      for(int i=tid; i < m*R; i += nthr) {
+        int j=dR(i), rho=i-j*R;
+        multiplySlot<K>(X,j*ld+rho,R,A,B,P.mult);
+      }
+      __syncthreads();
+      Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
+    }
+    for(int i=tid; i < lb*L; i += nthr) {
+      int col=dL(i), s=i-col*L;
+      int b=dR(col);
+      long long row=row0+col-b*R;
+      if(row >= P.nrows) continue;
+      cplx<T> v=Z[sp(posmod(s-c,m)*ld+col)];
+      long long off=row*P.rowStride+s;
+      if(P.realIO) storeIOr((T *) P.out[b]+off,v.x*P.scale,P.io64 & 2);
+      else storeIO(P.out[b]+off,v*P.scale,P.io64 & 2);
+    }
+    __syncthreads();
+    return;
+  }
 
   // The loads of FGB_LOADS iterations are issued before any is used.
   for(int i0=tid; i0 < ld*L; i0 += FGB_LOADS*nthr) {
@@ -410,14 +478,14 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
   __syncthreads();
 }
 
-template<typename T, int K>
+template<typename T, int K, bool D>
 __global__ void __launch_bounds__(256)
 rowConvKernel(const RowPlan<T> P)
 {
   extern __shared__ __align__(16) unsigned char smemRaw[];
   const long long groups=(P.nrows+P.rpc-1)/P.rpc;
   for(long long g=blockIdx.x; g < groups; g += gridDim.x)
-    rowConvRow<T,false,K>(P,g,smemRaw);
+    rowConvRow<T,false,K,D>(P,g,smemRaw);
 }
 
 // ---------------------------------------------------------------------------
@@ -989,10 +1057,12 @@ int batchBlocksPerSM(int threads, size_t smem, int mult, int A, int B)
 
 // Shared-memory bytes: FFT ping-pong buffers are padded (sp()); the forward
 // outer kernel also stages its L x tile input block in the second buffer.
-template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc)
+template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc,
+                                    int direct)
 {
   size_t nbuf=inplaceFFT<T>() ? 1 : 2;
-  return sizeof(cplx<T>)*((size_t) (A+B)*rpc*L+nbuf*(size_t) padded(m*A*rpc));
+  size_t stage=direct ? 0 : (size_t) (A+B)*rpc*L;
+  return sizeof(cplx<T>)*(stage+nbuf*(size_t) padded(m*A*rpc));
 }
 template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc)
 {
@@ -1031,7 +1101,7 @@ template<typename T>
 cudaError_t launchRow(const RowPlan<T>& P, int threads, long long grid,
                       cudaStream_t s)
 {
-  size_t sm=rowSmem<T>(P.L,P.m,P.A,P.B,P.rpc);
+  size_t sm=rowSmem<T>(P.L,P.m,P.A,P.B,P.rpc,P.direct);
   long long groups=(P.nrows+P.rpc-1)/P.rpc;
   grid=std::min(std::min(grid,groups),(long long) INT_MAX);
   auto go=[&](auto kernel) {
@@ -1040,10 +1110,16 @@ cudaError_t launchRow(const RowPlan<T>& P, int threads, long long grid,
     kernel<<<(unsigned) grid,threads,sm,s>>>(P);
     return cudaGetLastError();
   };
+  if(P.direct)
+    switch(multVariant(P.mult,P.A,P.B)) {
+      case MULT_BINARY: return go(rowConvKernel<T,MULT_BINARY,true>);
+      case MULT_REALBINARY: return go(rowConvKernel<T,MULT_REALBINARY,true>);
+      default: return go(rowConvKernel<T,MULT_GENERIC,true>);
+    }
   switch(multVariant(P.mult,P.A,P.B)) {
-    case MULT_BINARY: return go(rowConvKernel<T,MULT_BINARY>);
-    case MULT_REALBINARY: return go(rowConvKernel<T,MULT_REALBINARY>);
-    default: return go(rowConvKernel<T,MULT_GENERIC>);
+    case MULT_BINARY: return go(rowConvKernel<T,MULT_BINARY,false>);
+    case MULT_REALBINARY: return go(rowConvKernel<T,MULT_REALBINARY,false>);
+    default: return go(rowConvKernel<T,MULT_GENERIC,false>);
   }
 }
 
@@ -1121,7 +1197,7 @@ cudaError_t launchOuterRealBwd(const OuterPlan<T>& P, int threads,
   template cudaError_t launchOuterBwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
   template cudaError_t launchOuterRealFwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
   template cudaError_t launchOuterRealBwd<T>(const OuterPlan<T>&,int,cudaStream_t); \
-  template size_t rowSmem<T>(int,int,int,int,int); \
+  template size_t rowSmem<T>(int,int,int,int,int,int); \
   template size_t hermRowSmem<T>(int,int,int,int); \
   template size_t outerFwdSmem<T>(int,int,int,int); \
   template size_t outerBwdSmem<T>(int,int,int,int,int); \

@@ -59,6 +59,10 @@ struct RowPlan {
   int rpc;                 // rows per CTA (their columns are interleaved)
   int io64;                // float-float mode: bit 0, in[] holds FP64
                            // values; bit 1, out[] takes FP64 values
+  int direct;              // one residue and one fold (q = 1, L <= m): rows
+                           // load straight into the transform buffer and
+                           // store straight from it (no staging, no
+                           // accumulator)
   T scale;
   FFTPlanDev fp;           // length-m complex FFT
   const typename TwT<T>::type *twN;   // W_N^t, t < N
@@ -182,7 +186,8 @@ struct CopyArgs {
 cudaError_t launchBulkCopy(const CopyArgs& P, cudaStream_t s);
 
 // Shared-memory bytes each kernel needs (for plan-time sizing).
-template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc=1);
+template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc=1,
+                                    int direct=0);
 template<typename T> size_t hermRowSmem(int H, int Nh, int A, int rpc=1);
 template<typename T> size_t outerFwdSmem(int L, int m, int tile,
                                          int inplace=0);
