@@ -895,7 +895,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.rpc=I.axis[I.dim-1].rpc;
     P.io64=0;
     P.direct=a.q == 1 && a.stored <= a.m;
-    P.fp=fftPlan(a.m,I.prec,inplaceFFT<T>());
+    P.fp=fftPlan(a.m,I.prec,inplaceFFT<T>() || P.direct);
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };
   auto hermPlan=[&](HermRowPlan<T>& P, const AxisPlan& a) {

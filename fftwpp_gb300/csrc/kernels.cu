@@ -365,7 +365,7 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
     }
     __syncthreads();
     const cplx<T> *Z;
-    if constexpr(inplaceFFT<T>()) {
+    if constexpr(inplaceFFT<T>() || D) {
       fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
       for(int i=tid; i < m*R; i += nthr) {
         int j=dR(i), rho=i-j*R;
@@ -1060,7 +1060,7 @@ int batchBlocksPerSM(int threads, size_t smem, int mult, int A, int B)
 template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc,
                                     int direct)
 {
-  size_t nbuf=inplaceFFT<T>() ? 1 : 2;
+  size_t nbuf=inplaceFFT<T>() || direct ? 1 : 2;
   size_t stage=direct ? 0 : (size_t) (A+B)*rpc*L;
   return sizeof(cplx<T>)*(stage+nbuf*(size_t) padded(m*A*rpc));
 }
