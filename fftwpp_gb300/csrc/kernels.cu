@@ -606,35 +606,72 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
   const typename TwT<T>::type *tw=P.twN;
   const UDiv dTile(tile);
 
-  if constexpr(inplaceFFT<T>()) {
-    if(P.inplace) {
-      // One term per output (L <= m): fold straight from memory into the
-      // transform buffer, transform in place (digit-reversed j; the row
-      // kernels do not depend on row order and the backward undoes it).
-      // Asynchronous copies straight to each value's slot, then the
-      // conversion and residue twiddle in place by the same thread.
+  if(L <= m) {
+    // One term per output: asynchronous copies straight to each value's
+    // transform slot, then the conversion and residue twiddle in place by
+    // the same thread.
+    for(int i=tid; i < m*tile; i += nthr) {
+      int t=dTile(i), cc=i-t*tile;
+      int col=col0+cc;
+      int s=posmod(t+c,m);
+      long long off=(long long) s*P.inRow+col;
+      if(s < L && col < P.C && off < P.Ltot) cpAsync(x+sp(i),src+off);
+      else x[sp(i)]=mk((T) 0,(T) 0);
+    }
+    cpAsyncWait();
+    if(r != 0 || (P.io64 & 1)) {
       for(int i=tid; i < m*tile; i += nthr) {
         int t=dTile(i), cc=i-t*tile;
         int col=col0+cc;
         int s=posmod(t+c,m);
         long long off=(long long) s*P.inRow+col;
-        if(s < L && col < P.C && off < P.Ltot) cpAsync(x+sp(i),src+off);
-        else x[sp(i)]=mk((T) 0,(T) 0);
-      }
-      cpAsyncWait();
-      if(r != 0 || (P.io64 & 1)) {
-        for(int i=tid; i < m*tile; i += nthr) {
-          int t=dTile(i), cc=i-t*tile;
-          int col=col0+cc;
-          int s=posmod(t+c,m);
-          long long off=(long long) s*P.inRow+col;
-          if(s < L && col < P.C && off < P.Ltot) {
-            if(P.io64 & 1) convertStaged(x,sp(i));
-            if(r != 0) x[sp(i)]=twmul<1>(x[sp(i)],tw[twExp(s,c,r,N)]);
-          }
+        if(s < L && col < P.C && off < P.Ltot) {
+          if(P.io64 & 1) convertStaged(x,sp(i));
+          if(r != 0) x[sp(i)]=twmul<1>(x[sp(i)],tw[twExp(s,c,r,N)]);
         }
       }
-      __syncthreads();
+    }
+    __syncthreads();
+  } else {
+    // Stage the L x tile input block in y with asynchronous copies (many
+    // loads in flight per thread instead of one dependent load per
+    // output), then fold it into x with the residue twiddles.
+    for(int i=tid; i < L*tile; i += nthr) {
+      int s=dTile(i), cc=i-s*tile;
+      int col=col0+cc;
+      long long off=(long long) s*P.inRow+col;
+      if(col < P.C && off < P.Ltot) cpAsync(y+i,src+off);
+      else y[i]=mk((T) 0,(T) 0);
+    }
+    cpAsyncWait();
+    if(std::is_same<T,ff>::value && (P.io64 & 1)) {
+      // The caller's FP64 values were staged as they are: convert them.
+      for(int i=tid; i < L*tile; i += nthr) {
+        int s=dTile(i), cc=i-s*tile;
+        int col=col0+cc;
+        long long off=(long long) s*P.inRow+col;
+        if(col < P.C && off < P.Ltot) convertStaged(y,i);
+      }
+    }
+    __syncthreads();
+    for(int i=tid; i < m*tile; i += nthr) {
+      int t=dTile(i), cc=i-t*tile;
+      cplx<T> sum=mk((T) 0,(T) 0);
+      int s0=posmod(t+c,m);
+      for(int s=s0; s < L; s += m) {
+        cplx<T> v=y[s*tile+cc];
+        if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
+        sum=accum(sum,v);
+      }
+      x[sp(i)]=sum;
+    }
+    __syncthreads();
+  }
+
+  if constexpr(inplaceFFT<T>()) {
+    if(P.inplace) {
+      // Transform in place (digit-reversed j; the row kernels do not
+      // depend on row order and the backward undoes it).
       fftDIF<T,1>(x,P.fp,tile,tile,tid,nthr);
       for(int i=tid; i < m*tile; i += nthr) {
         int j=dTile(i), cc=i-j*tile;
@@ -646,38 +683,6 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
     }
   }
 
-  // Stage the L x tile input block in y with asynchronous copies (many
-  // loads in flight per thread instead of one dependent load per output).
-  for(int i=tid; i < L*tile; i += nthr) {
-    int s=dTile(i), cc=i-s*tile;
-    int col=col0+cc;
-    long long off=(long long) s*P.inRow+col;
-    if(col < P.C && off < P.Ltot) cpAsync(y+i,src+off);
-    else y[i]=mk((T) 0,(T) 0);
-  }
-  cpAsyncWait();
-  if(std::is_same<T,ff>::value && (P.io64 & 1)) {
-    // The caller's FP64 values were staged as they are: convert them.
-    for(int i=tid; i < L*tile; i += nthr) {
-      int s=dTile(i), cc=i-s*tile;
-      int col=col0+cc;
-      long long off=(long long) s*P.inRow+col;
-      if(col < P.C && off < P.Ltot) convertStaged(y,i);
-    }
-  }
-  __syncthreads();
-  for(int i=tid; i < m*tile; i += nthr) {
-    int t=dTile(i), cc=i-t*tile;
-    cplx<T> sum=mk((T) 0,(T) 0);
-    int s0=posmod(t+c,m);
-    for(int s=s0; s < L; s += m) {
-      cplx<T> v=y[s*tile+cc];
-      if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
-      sum=accum(sum,v);
-    }
-    x[sp(i)]=sum;
-  }
-  __syncthreads();
   cplx<T> *X=fftSmem<T,1>(x,y,P.fp,tile,tile,tid,nthr);
   for(int i=tid; i < m*tile; i += nthr) {
     int j=dTile(i), cc=i-j*tile;
