@@ -29,10 +29,11 @@ static const int THREADS=256;
 
 static size_t elemBytes(int prec) {return prec == PREC_F64 ? 16 : 8;}
 
-static size_t rowNeedB(int prec, long L, long m, int A, int B, int rpc=1)
+static size_t rowNeedB(int prec, long L, long m, int A, int B, int rpc=1,
+                       int direct=0)
 {
-  return prec == PREC_F64 ? rowSmem<double>(L,m,A,B,rpc) :
-    rowSmem<float>(L,m,A,B,rpc);
+  return prec == PREC_F64 ? rowSmem<double>(L,m,A,B,rpc,direct) :
+    rowSmem<float>(L,m,A,B,rpc,direct);
 }
 
 static size_t outerNeedB(int prec, long L, long m, int tile)
@@ -315,20 +316,22 @@ void BatchConv::build()
       G.scale=(T) (1.0/(double) N);
       for(int b=0; b < B; ++b) G.out[b]=(cplx<T> *) (offsets[i]*e);
       // Several rows per row task where they fit the budget.
+      // The rows hold one residue of one fold: the direct row variant
+      // (no staging, in-place transforms).
       int rpc=1;
       while(rpc < 8 && rpc < qc &&
-            rowNeedB(prec,m,m,A,B,rpc+1) <= budget) ++rpc;
+            rowNeedB(prec,m,m,A,B,rpc+1,1) <= budget) ++rpc;
       RowPlan<T>& R=P.row;
       R.L=(int) m; R.m=(int) m; R.q=1; R.N=(int) m; R.cshift=0;
       R.A=A; R.B=B; R.mult=mult; R.realIO=0; R.rpc=rpc; R.scale=(T) 1;
-      R.fp=fftPlanPublic(m,prec,prec != PREC_F64);   // in-place rows in FP32
-      R.direct=0;
+      R.fp=fftPlanPublic(m,prec,true);
+      R.direct=1;
       R.twN=(const Tw *) twiddles(m,prec);
       R.rowStride=m; R.nrows=qc;
       P.rel=4|8;
       P.nfwd=(int) (ceilquotient(m,tile)*A);
       P.nrows=(int) ceilquotient(qc,rpc);   // row tasks the backward waits for
-      smem=std::max(smem,rowNeedB(prec,m,m,A,B,rpc));
+      smem=std::max(smem,rowNeedB(prec,m,m,A,B,rpc,1));
       smem=std::max(smem,outerNeedB(prec,pc,qc,tile));
       lng.push_back({(double) N*std::log2((double) N),i});
       ++nlong;

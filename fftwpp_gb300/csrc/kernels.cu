@@ -987,6 +987,7 @@ batchKernel(const BatchArgs<T> P)
         rebase(R,R.A,rel & 1,rel & 2,P.inBase,P.outBase);
       __syncthreads();
       if(tk.type == TASK_SMALL) rowConvRow<T,false,K>(R,tk.i,smemRaw);
+      else if(R.direct) rowConvRow<T,true,K,true>(R,tk.i,smemRaw);
       else rowConvRow<T,true,K>(R,tk.i,smemRaw);
     } else {
       const bool fwd=tk.type == TASK_COLFWD;
