@@ -237,7 +237,6 @@ static size_t outerNeed(int prec, long L, long m, int tile)
   return std::max(f,b);
 }
 
-static double fftCost(long m) {return m*std::log2((double) std::max(m,2L));}
 
 static double fftInstr(long n);
 
