@@ -395,87 +395,86 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
       else storeIO(P.out[b]+off,v*P.scale,P.io64 & 2);
     }
     __syncthreads();
-    return;
-  }
-
-  // The loads of FGB_LOADS iterations are issued before any is used.
-  for(int i0=tid; i0 < ld*L; i0 += FGB_LOADS*nthr) {
-    cplx<T> v[FGB_LOADS];
+  } else {
+    // The loads of FGB_LOADS iterations are issued before any is used.
+    for(int i0=tid; i0 < ld*L; i0 += FGB_LOADS*nthr) {
+      cplx<T> v[FGB_LOADS];
 #pragma unroll
-    for(int u=0; u < FGB_LOADS; ++u) {
-      const int i=i0+u*nthr;
-      v[u]=mk((T) 0,(T) 0);
-      if(i >= ld*L) continue;
-      int col=dL(i), s=i-col*L;
-      int a=dR(col);
-      long long row=row0+col-a*R;
-      if(row < P.nrows) {
-        long long off=row*P.rowStride+s;
-        if(P.realIO) v[u]=mk(loadIOr((const T *) P.in[a]+off,P.io64 & 1),(T) 0);
-        else if(P.io64 & 1) v[u]=loadIO(P.in[a]+off,true);
-        else v[u]=ldx<CG>(P.in[a]+off);
+      for(int u=0; u < FGB_LOADS; ++u) {
+        const int i=i0+u*nthr;
+        v[u]=mk((T) 0,(T) 0);
+        if(i >= ld*L) continue;
+        int col=dL(i), s=i-col*L;
+        int a=dR(col);
+        long long row=row0+col-a*R;
+        if(row < P.nrows) {
+          long long off=row*P.rowStride+s;
+          if(P.realIO) v[u]=mk(loadIOr((const T *) P.in[a]+off,P.io64 & 1),(T) 0);
+          else if(P.io64 & 1) v[u]=loadIO(P.in[a]+off,true);
+          else v[u]=ldx<CG>(P.in[a]+off);
+        }
       }
-    }
 #pragma unroll
-    for(int u=0; u < FGB_LOADS; ++u)
-      if(i0+u*nthr < ld*L) fin[i0+u*nthr]=v[u];
-  }
-  for(int i=tid; i < lb*L; i += nthr) acc[i]=mk((T) 0,(T) 0);
-  __syncthreads();
-
-  for(int r=0; r < P.q; ++r) {
-    // Fold the data into one length-m block with the residue twiddles.
-    for(int i=tid; i < m*ld; i += nthr) {
-      int t=dLd(i), col=i-t*ld;
-      int s0=posmod(t+c,m);
-      cplx<T> sum=mk((T) 0,(T) 0);
-      for(int s=s0; s < L; s += m) {
-        cplx<T> v=fin[col*L+s];
-        if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
-        sum=accum(sum,v);
-      }
-      x[sp(i)]=sum;
+      for(int u=0; u < FGB_LOADS; ++u)
+        if(i0+u*nthr < ld*L) fin[i0+u*nthr]=v[u];
     }
+    for(int i=tid; i < lb*L; i += nthr) acc[i]=mk((T) 0,(T) 0);
     __syncthreads();
-    const cplx<T> *Z;
-    if constexpr(inplaceFFT<T>()) {
-      fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
-      for(int i=tid; i < m*R; i += nthr) {
-        int j=dR(i), rho=i-j*R;
-        multiplySlot<K>(x,j*ld+rho,R,A,B,P.mult);
+
+    for(int r=0; r < P.q; ++r) {
+      // Fold the data into one length-m block with the residue twiddles.
+      for(int i=tid; i < m*ld; i += nthr) {
+        int t=dLd(i), col=i-t*ld;
+        int s0=posmod(t+c,m);
+        cplx<T> sum=mk((T) 0,(T) 0);
+        for(int s=s0; s < L; s += m) {
+          cplx<T> v=fin[col*L+s];
+          if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
+          sum=accum(sum,v);
+        }
+        x[sp(i)]=sum;
       }
       __syncthreads();
-      fftDIT<T,-1>(x,P.fp,lb,ld,tid,nthr);
-      Z=x;
-    } else {
-      cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
-      cplx<T> *Y=X == x ? y : x;
-      for(int i=tid; i < m*R; i += nthr) {
-        int j=dR(i), rho=i-j*R;
-        multiplySlot<K>(X,j*ld+rho,R,A,B,P.mult);
+      const cplx<T> *Z;
+      if constexpr(inplaceFFT<T>()) {
+        fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
+        for(int i=tid; i < m*R; i += nthr) {
+          int j=dR(i), rho=i-j*R;
+          multiplySlot<K>(x,j*ld+rho,R,A,B,P.mult);
+        }
+        __syncthreads();
+        fftDIT<T,-1>(x,P.fp,lb,ld,tid,nthr);
+        Z=x;
+      } else {
+        cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
+        cplx<T> *Y=X == x ? y : x;
+        for(int i=tid; i < m*R; i += nthr) {
+          int j=dR(i), rho=i-j*R;
+          multiplySlot<K>(X,j*ld+rho,R,A,B,P.mult);
+        }
+        __syncthreads();
+        Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
+      }
+      for(int i=tid; i < lb*L; i += nthr) {
+        int col=dL(i), s=i-col*L;
+        int t=posmod(s-c,m);
+        cplx<T> v=Z[sp(t*ld+col)];
+        if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
+        acc[i]=accum(acc[i],v);
       }
       __syncthreads();
-      Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
     }
     for(int i=tid; i < lb*L; i += nthr) {
       int col=dL(i), s=i-col*L;
-      int t=posmod(s-c,m);
-      cplx<T> v=Z[sp(t*ld+col)];
-      if(r != 0) v=twmul<-1>(v,tw[twExp(s,c,r,N)]);
-      acc[i]=accum(acc[i],v);
+      int b=dR(col);
+      long long row=row0+col-b*R;
+      if(row >= P.nrows) continue;
+      long long off=row*P.rowStride+s;
+      if(P.realIO) storeIOr((T *) P.out[b]+off,acc[i].x*P.scale,P.io64 & 2);
+      else storeIO(P.out[b]+off,acc[i]*P.scale,P.io64 & 2);
     }
     __syncthreads();
   }
-  for(int i=tid; i < lb*L; i += nthr) {
-    int col=dL(i), s=i-col*L;
-    int b=dR(col);
-    long long row=row0+col-b*R;
-    if(row >= P.nrows) continue;
-    long long off=row*P.rowStride+s;
-    if(P.realIO) storeIOr((T *) P.out[b]+off,acc[i].x*P.scale,P.io64 & 2);
-    else storeIO(P.out[b]+off,acc[i]*P.scale,P.io64 & 2);
-  }
-  __syncthreads();
 }
 
 template<typename T, int K, bool D>
