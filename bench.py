@@ -440,6 +440,31 @@ def run_ours(args, w):
         dist.init_process_group("nccl")
     else:
         torch.cuda.set_device(0)
+    line = measure(args, w, args.workload, args.steps, args.warmup, world,
+                   rank, local)
+    if (args.workload == "hconv2d" and args.precision == "f64" and
+            not args.quick and not args.no_real3d):
+        # The largest single-GPU configuration, the 3D real convolution,
+        # measured in the same run with its own roofline, CPU baseline and
+        # end-to-end rate (fewer steps: one FP64 convolution is ~20 ms).
+        w3 = WORKLOADS["real3d"]
+        sub = measure(args, w3, "real3d", min(args.steps, 40),
+                      max(3, min(args.warmup, 5)), world, rank, local)
+        if line is not None:
+            line["real3d"] = sub
+    if line is not None:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def measure(args, w, workload, steps, warmup, world, rank, local):
+    """One workload on this rank's GPU: device-timed rate, per-kernel times,
+    roofline, accuracy against the oracle, the other precisions, end to
+    end through the host entry and the CPU baselines.  Returns the JSON
+    line on rank 0, None elsewhere."""
+    import torch
     from fftwpp_gb300 import _native
     from fftwpp_gb300.gpu import HybridConvolution
 
@@ -454,7 +479,7 @@ def run_ours(args, w):
     clocks = ClockSampler(local) if rank == 0 else None
     if clocks:
         clocks.start()
-    total_ms, outs = time_device(conv, ts, args.steps, args.warmup, flush,
+    total_ms, outs = time_device(conv, ts, steps, warmup, flush,
                                  clocks=clocks, world=world)
     clk = clocks.stop() if clocks else None
     if world > 1:
@@ -463,18 +488,17 @@ def run_ours(args, w):
         total_ms = float(t.item())
         torch.distributed.barrier()
     nb = w.get("batch", 1)          # convolutions per step
-    value = world * nb * args.steps / (total_ms * 1e-3)
+    value = world * nb * steps / (total_ms * 1e-3)
 
     names = conv.launch_names()
     kms = conv.kernel_ms()
-    per_launch = [k / args.steps for k in kms]
+    per_launch = [k / steps for k in kms]
     dom = int(np.argmax(per_launch))
     elem = (8 if conv.real else 16) if prec != "f32" else (4 if conv.real else 8)
     abytes = algorithmic_bytes(w, elem)
 
     if rank != 0:
-        torch.distributed.destroy_process_group()
-        return 0
+        return None
 
     peaks = {}
     pfile = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -488,12 +512,12 @@ def run_ours(args, w):
         raise RuntimeError("per-kernel timing recorded nothing")
     achieved = abytes / (per_launch[dom] * 1e-3) / 1e9
     traffic = (None if w.get("custom") else
-               traffic_from_profiles(args.workload, names[dom], prec))
+               traffic_from_profiles(workload, names[dom], prec))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "kernel": names[dom], "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": abytes,
-                "whole_step_frac": abytes / (total_ms / args.steps * 1e-3)
+                "whole_step_frac": abytes / (total_ms / steps * 1e-3)
                 / 1e9 / peak}
 
     # Compute roofline of the FP64 kernels: FP64 instructions per launch
@@ -509,7 +533,7 @@ def run_ours(args, w):
                         ("SPINST", ffma, "fp32_issue"))
     if rate:
         cnt = [None if w.get("custom") else
-               profile_figure(tag, args.workload, n, prec) for n in names]
+               profile_figure(tag, workload, n, prec) for n in names]
         compute = {"fp64_tflops_peak_measured": 2 * dfma / 1e12,
                    "fp32_tflops_peak_measured": 2 * ffma / 1e12}
         if cnt[dom]:
@@ -520,7 +544,7 @@ def run_ours(args, w):
                 "peak": rate,
                 "unit": ("FP64" if tag == "DPINST" else "FP32") + " inst/s",
                 "frac": cnt[dom] / (per_launch[dom] * 1e-3) / rate,
-                "whole_step_frac": (total / (total_ms / args.steps * 1e-3)
+                "whole_step_frac": (total / (total_ms / steps * 1e-3)
                                     / rate) if total else None,
                 "source": f"{tag} lines (instructions per launch, ncu) "
                           "under profiles/, peak from fgb_measure_fma_rate"})
@@ -550,7 +574,7 @@ def run_ours(args, w):
                                    B=w["B"], mult=w["mult"], precision=other,
                                    batch=w.get("batch", 1))
             to = [torch.from_numpy(f).to(co.dtype).cuda() for f in fs]
-            mso, oo = time_device(co, to, args.steps, args.warmup, flush,
+            mso, oo = time_device(co, to, steps, warmup, flush,
                                   timing=False)
             if want is not None:
                 eo = rel_l2(oo[0].cpu().numpy(), want)
@@ -559,14 +583,14 @@ def run_ours(args, w):
                                 n=12)
             else:
                 eo = None
-            extra[key] = {"value": nb * args.steps / (mso * 1e-3),
+            extra[key] = {"value": nb * steps / (mso * 1e-3),
                           "unit": "convs/s", "rel_l2_vs_fp64_oracle": eo,
                           "speedup_vs_fp64": total_ms / mso}
             del co, to, oo
 
     # End to end through the reference-facing C ABI on host buffers.
     e2e = None
-    if args.workload == "hconv2d" and prec == "f64":
+    if workload == "hconv2d" and prec == "f64":
         lib = _native.load()
         import ctypes
         h = lib.fftwpp_create_hconv2d(w["L"][0], w["L"][1])
@@ -577,17 +601,17 @@ def run_ours(args, w):
         B_ = np.ctypeslib.as_array((ctypes.c_double * (2 * n)).from_address(pb))
         src0 = fs[0].view(np.float64).ravel()
         B_[:] = fs[1].view(np.float64).ravel()
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             A_[:] = src0
             lib.fftwpp_hconv2d_convolve(h, pa, pb)
         tot = 0.0
-        for _ in range(args.steps):
+        for _ in range(steps):
             A_[:] = src0
             t0 = time.perf_counter()
             lib.fftwpp_hconv2d_convolve(h, pa, pb)
             tot += time.perf_counter() - t0
         e2e_err = rel_l2(A_.view(np.complex128).reshape(fs[0].shape), want)
-        e2e = {"value": nb * args.steps / tot, "unit": "convs/s",
+        e2e = {"value": nb * steps / tot, "unit": "convs/s",
                "h2d_bytes_per_step": 2 * n * 16, "d2h_bytes_per_step": n * 16,
                "api": "fftwpp_hconv2d_convolve (create_complexAlign "
                       "page-locked buffers, zero copy over the host link)",
@@ -601,17 +625,17 @@ def run_ours(args, w):
         host = [torch.from_numpy(np.ascontiguousarray(f)).to(conv.dtype)
                 .pin_memory().numpy() for f in fs]
         src0 = host[0].copy()
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             host[0][...] = src0
             conv.convolve_host(*host)
         tot = 0.0
-        for _ in range(args.steps):
+        for _ in range(steps):
             host[0][...] = src0
             t0 = time.perf_counter()
             conv.convolve_host(*host)
             tot += time.perf_counter() - t0
         nbytes = host[0].nbytes
-        e2e = {"value": nb * args.steps / tot, "unit": "convs/s",
+        e2e = {"value": nb * steps / tot, "unit": "convs/s",
                "h2d_bytes_per_step": w["A"] * nbytes,
                "d2h_bytes_per_step": w["B"] * nbytes,
                "api": "fgb_convolve_host (page-locked host arrays, "
@@ -634,8 +658,8 @@ def run_ours(args, w):
             sp_first)}
     line = {
         "metric": METRIC, "value": value, "unit": "convs/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "steps": steps, "warmup": warmup,
+        "ms_per_step": total_ms / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": prec,
         "data": "synthetic (seeded)",
         "config": {"workload": w["desc"], "precision": prec,
@@ -654,14 +678,11 @@ def run_ours(args, w):
                                    f"restatement of FFTW++'s hybrid convolution)"},
         "cpu_scipy_explicit": scipy_point,
         "e2e": e2e,
-        "gpu_launches": conv.launches * args.steps,
+        "gpu_launches": conv.launches * steps,
         "clocks": clk,
     }
     line.update(extra)
-    print(json.dumps(line))
-    if world > 1:
-        torch.distributed.destroy_process_group()
-    return 0
+    return line
 
 
 def batched_lengths(n=512, lo=64, hi=65536, seed=2024):
@@ -1338,6 +1359,8 @@ def main():
                     "(-M; default: the workload's dealiasing rule)")
     ap.add_argument("--m", help="comma-separated forced residue block "
                     "lengths (-m; 0 = planner's choice)")
+    ap.add_argument("--no-real3d", action="store_true",
+                    help="skip the 3D real block of the default line")
     ap.add_argument("--quick", action="store_true",
                     help="skip the FP32 comparison leg")
     args = ap.parse_args()

@@ -116,9 +116,11 @@ class GraphedLossStep:
     launch, without the per-operation launch cost of eager autograd.
 
     psi and omega are the static input tensors (CUDA, the operator's dtype):
-    write new values into them (copy_) between calls.  Each call returns
-    the static (loss, dL/dpsi, dL/domega) tensors, overwritten by the next
-    call.  loss_fn maps J to a scalar (default: sum |J|^2)."""
+    give new values with set_inputs() between calls (they are leaves that
+    require grad, so a plain copy_ into step.psi outside torch.no_grad()
+    raises).  Each call returns the static (loss, dL/dpsi, dL/domega)
+    tensors, overwritten by the next call.  loss_fn maps J to a scalar
+    (default: sum |J|^2)."""
 
     def __init__(self, op: AdvectionJacobian, psi, omega, loss_fn=None):
         if psi.dtype != op.dtype or omega.dtype != op.dtype:
@@ -143,6 +145,15 @@ class GraphedLossStep:
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             self.out = body()
+
+    def set_inputs(self, psi=None, omega=None):
+        """Copy new spectra into the captured input tensors (either may be
+        None to keep its current values)."""
+        with torch.no_grad():
+            if psi is not None:
+                self.psi.copy_(psi)
+            if omega is not None:
+                self.omega.copy_(omega)
 
     def __call__(self):
         self.graph.replay()

@@ -21,7 +21,10 @@
 //    serialised by the caller;
 //  * the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (host code cannot use the array's name as a device
-//    address); make that first call before any stream capture;
+//    address); make that first call before any stream capture.  The address
+//    is kept for the life of the process: after cudaDeviceReset the module
+//    is loaded again, possibly elsewhere, so an application that resets a
+//    device must not call this entry point on it again;
 //  * sizes whose staging does not fit in the array are rejected with an
 //    error before anything is launched.
 //
@@ -165,7 +168,8 @@ extern "C" int fgb_hconv2d_convolve_noalloc(const void *f, const void *g,
     return t;
   };
 
-  OuterPlan<double> O;
+  OuterPlan<double> O{};
+  O.io64=0; O.inplace=0; O.conj=0;
   O.L=(int) Lx; O.m=(int) Nx; O.q=1; O.N=(int) Nx;
   O.cshift=(int) (Lx/2);
   O.fp=radixPlan(Nx,tx);
@@ -179,7 +183,8 @@ extern "C" int fgb_hconv2d_convolve_noalloc(const void *f, const void *g,
   e=launchOuterFwd<double>(O,256,s);
   if(e != cudaSuccess) return fail(cudaGetErrorString(e));
 
-  HermRowPlan<double> P;
+  HermRowPlan<double> P{};
+  P.io64=0;
   P.H=(int) Hy; P.N=(int) Ny; P.Nh=(int) Nyh;
   P.A=2; P.B=1; P.mult=MULT_REALBINARY; P.rpc=1;
   P.fp=radixPlan(Nyh,tyh);

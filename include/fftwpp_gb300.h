@@ -269,7 +269,9 @@ size_t fgb_index(int kind, size_t m, size_t p, size_t q, size_t n, size_t D,
  * device and keeps the last call's contents; each call rewrites everything
  * it reads.  Calls that overlap on the GPU race on it.  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress); make
- * it before any stream capture.  Returns 0, or -1 with fgb_last_error(). */
+ * it before any stream capture.  That address is kept until the process
+ * exits, so do not call this entry point again on a device after
+ * cudaDeviceReset.  Returns 0, or -1 with fgb_last_error(). */
 int fgb_hconv2d_convolve_noalloc(const void *f, const void *g, void *h,
                                  size_t Lx, size_t Ly, void *stream);
 

@@ -145,6 +145,19 @@ def directconvh3(f: np.ndarray, g: np.ndarray, xcompact: bool,
     return h
 
 
+def directconv3_at(f: np.ndarray, g: np.ndarray, points) -> np.ndarray:
+    """Entries h[i, j, k] of the 3D direct convolution (tests/direct.h:
+    118-133, h[i,j,k] = sum f[a,b,c] g[i-a,j-b,k-c] over a <= i, b <= j,
+    c <= k) at the given index triples only, for sizes whose full O(L^6)
+    sum is out of reach; each entry is one vectorised FP64 sum."""
+    out = []
+    for idx in points:
+        i, j, k = (int(t) for t in idx)
+        out.append(np.sum(f[:i + 1, :j + 1, :k + 1] *
+                          g[i::-1, j::-1, k::-1]))
+    return np.asarray(out)
+
+
 def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
     """Relative L2 error |a-b|/|b| as in the reference's tests
     (tests/hybridconv.cc:118-129)."""

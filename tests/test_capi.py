@@ -214,3 +214,44 @@ def test_python_switches(native_lib):
     gpu.set_host_path(-1, -1)
     with pytest.raises(ValueError):
         gpu.set_host_path(3, 0)
+
+
+def _reference_wrapper_dir():
+    ref = (os.environ.get("FFTWPP_REFERENCE") or
+           os.path.join(os.sep, "root", "reference"))
+    path = os.path.join(ref, "wrappers", "fftwpp.py")
+    return path if os.path.exists(path) else None
+
+
+def test_unchanged_reference_wrapper_binds(native_lib, tmp_path):
+    """The reference's own wrappers/fftwpp.py, unmodified, loads this
+    library from its own directory and binds every prototype it declares;
+    its thread-count calls and host-side Hermitian symmetrisers run (no GPU
+    needed) and agree with the oracle.  Skipped where the reference
+    checkout is absent (it is not shipped with this package)."""
+    import importlib.util
+    import shutil
+    from fftwpp_gb300 import _native
+    from oracle import hybrid as H
+    src = _reference_wrapper_dir()
+    if src is None:
+        pytest.skip("reference checkout not present")
+    shutil.copy(src, tmp_path / "fftwpp.py")
+    os.symlink(_native.LIB_PATH, tmp_path / "lib_fftwpp.so")
+    spec = importlib.util.spec_from_file_location("ref_fftwpp",
+                                                  tmp_path / "fftwpp.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    assert hasattr(mod, "Convolution") and hasattr(mod, "HConvolution")
+    old = mod.fftwpp_get_maxthreads()
+    mod.fftwpp_set_maxthreads(3)
+    assert mod.fftwpp_get_maxthreads() == 3
+    mod.fftwpp_set_maxthreads(old)
+    rng = np.random.default_rng(8)
+    Lx, Hy = 9, 5
+    f = mod.complex_align([Lx, Hy])
+    f[...] = rng.normal(size=(Lx, Hy)) + 1j * rng.normal(size=(Lx, Hy))
+    g = f.copy()
+    mod.clib.fftwpp_HermitianSymmetrizeX((Lx + 1) // 2, Hy, Lx // 2, f)
+    H.hermitian_symmetrize_x(g, (Lx + 1) // 2, Hy, Lx // 2)
+    assert np.array_equal(f, g)

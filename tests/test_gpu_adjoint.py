@@ -180,9 +180,7 @@ def test_graphed_loss_step(native_lib, precision):
 
     step = GraphedLossStep(op, psi.clone(), omega.clone())
     for p, o in ((psi, omega), (p2, o2)):
-        with torch.no_grad():
-            step.psi.copy_(p)
-            step.omega.copy_(o)
+        step.set_inputs(p, o)
         got = [t.clone() for t in step()]
         want = eager(p, o)
         torch.cuda.synchronize()

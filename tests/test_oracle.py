@@ -205,3 +205,15 @@ def test_dot_multiplier_is_sum_of_products(kinds, L, mult, single):
     want = sum(H.convolve([fs[k], fs[K + k]], kinds, L, M, mult=single)[0]
                for k in range(K))
     assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+
+
+def test_sampled_direct_sum_3d():
+    """directconv3_at, the per-entry form the 256^3 parity test uses,
+    equals the full direct sum of tests/direct.h:118-133."""
+    from oracle.direct import directconv3, directconv3_at
+    rng = np.random.default_rng(12)
+    f, g = rng.normal(size=(5, 4, 6)), rng.normal(size=(5, 4, 6))
+    h = directconv3(f, g)
+    pts = [(4, 3, 5), (0, 0, 0), (2, 1, 3), (4, 0, 5), (1, 3, 2)]
+    np.testing.assert_allclose(directconv3_at(f, g, pts),
+                               [h[p] for p in pts], rtol=0, atol=1e-13)

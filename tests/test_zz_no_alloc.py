@@ -34,11 +34,15 @@ def _rel(a, b):
 
 
 def test_noalloc_matches_plan_entry_two_calls(native_lib):
+    """Two calls in a row (small, then the largest accepted size), then a
+    third, small and odd-shaped, that starts on the scratch array the large
+    call left dirty."""
     import torch
     from fftwpp_gb300.gpu import HybridConvolution, CENTERED, HERMITIAN
     lib = native_lib
     stream = torch.cuda.current_stream()
-    for call, (Lx, Ly, seed) in enumerate([(63, 63, 1), (1023, 1023, 2)]):
+    for call, (Lx, Ly, seed) in enumerate([(63, 63, 1), (1023, 1023, 2),
+                                           (65, 31, 3)]):
         f, g = _inputs(Lx, Ly, seed)
         tf = torch.from_numpy(f).cuda()
         tg = torch.from_numpy(g).cuda()
