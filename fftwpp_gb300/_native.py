@@ -17,7 +17,7 @@ F64, F32, FF = 0, 1, 2
 PRECISIONS = {"f64": F64, "f32": F32, "ff": FF}
 MULT = {"none": 0, "binary": 1, "realbinary": 2, "correlation": 3,
         "realjacobian": 4, "jacobian": 5, "realjacadj": 6, "dot": 7,
-        "realdot": 8}
+        "realdot": 8, "user": 9}
 
 _lib = None
 

@@ -639,6 +639,12 @@ int fgb_convolve_device(fgb_conv *c, void *const *in, void *const *out,
            "size ("+std::to_string(c->conv->elemBytes())+" bytes)");
     return -1;
   }
+  if(I.mult == MULT_USER) {
+    report("fgb_convolve_device","this plan multiplies with a caller's "
+           "device functor: convolve through fgb::convolveWith "
+           "(fftwpp_gb300_mult.cuh)");
+    return -1;
+  }
   cudaError_t e=c->conv->run(in,out,(cudaStream_t) stream);
   if(e != cudaSuccess) {
     report("fgb_convolve_device",cudaGetErrorString(e));
@@ -650,10 +656,55 @@ int fgb_convolve_device(fgb_conv *c, void *const *in, void *const *out,
 int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out)
 {
   if(!c || !in || !out) {report("fgb_convolve_host","bad arguments"); return -1;}
+  if(c->conv->info().mult == MULT_USER) {
+    report("fgb_convolve_host","this plan multiplies with a caller's "
+           "device functor: convolve through fgb::convolveHostWith "
+           "(fftwpp_gb300_mult.cuh)");
+    return -1;
+  }
   cudaError_t e=c->conv->runHost(in,out,c->stream);
   if(e != cudaSuccess) {
     report("fgb_convolve_host",cudaGetErrorString(e));
     return -2;
+  }
+  return 0;
+}
+
+int fgb_convolve_device_with(fgb_conv *c, const void *launchers,
+                             void *const *in, void *const *out, void *stream)
+{
+  const char *where="fgb_convolve_device_with";
+  if(!c || !launchers || !in || !out) {report(where,"bad arguments"); return -1;}
+  const ConvInfo& I=c->conv->info();
+  if(!alignedAll(in,I.A,c->conv->elemBytes()) ||
+     !alignedAll(out,I.B,c->conv->elemBytes())) {
+    report(where,"arrays must be aligned to their element size ("+
+           std::to_string(c->conv->elemBytes())+" bytes)");
+    return -1;
+  }
+  setLastError("");
+  cudaError_t e=c->conv->runWith((const RowLaunchers *) launchers,in,out,
+                                 (cudaStream_t) stream);
+  if(e != cudaSuccess) {
+    std::string why=lastError();
+    report(where,why.empty() ? cudaGetErrorString(e) : why);
+    return e == cudaErrorInvalidValue ? -1 : -2;
+  }
+  return 0;
+}
+
+int fgb_convolve_host_with(fgb_conv *c, const void *launchers,
+                           void *const *in, void *const *out)
+{
+  const char *where="fgb_convolve_host_with";
+  if(!c || !launchers || !in || !out) {report(where,"bad arguments"); return -1;}
+  setLastError("");
+  cudaError_t e=c->conv->runHostWith((const RowLaunchers *) launchers,in,out,
+                                     c->stream);
+  if(e != cudaSuccess) {
+    std::string why=lastError();
+    report(where,why.empty() ? cudaGetErrorString(e) : why);
+    return e == cudaErrorInvalidValue ? -1 : -2;
   }
   return 0;
 }

@@ -422,7 +422,8 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
 Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
            const long *mForce, int A, int B, int mult, int prec, long batch,
            bool tuneSchedule)
-  : batch(batch), staging(0), hostIn(NULL), hostOut(NULL), nlaunch(0),
+  : batch(batch), user(NULL), tuning(false), staging(0), hostIn(NULL),
+    hostOut(NULL), nlaunch(0),
     timing(false), normalize(true), marks(0), hostTile(0), hostThr(0),
     hostTileB(0), hostThrB(0), side(NULL), chunks(0)
 {
@@ -454,6 +455,7 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
         throw std::runtime_error("a dot-product multiplier needs an even A "
                                  "and B = 1");
       break;
+    case MULT_USER: break;
     default: throw std::runtime_error("unknown multiplier");
   }
   I.dim=dim; I.A=A; I.B=B; I.mult=mult; I.prec=prec;
@@ -577,7 +579,9 @@ Conv *Conv::create(int dim, const int *kinds, const long *L, const long *M,
                    const long *mForce, int A, int B, int mult, int prec,
                    long batch)
 {
-  if(!autotune || !residueSearch)
+  // A caller's functor is not available at plan time: its plans keep the
+  // cost model's residue blocks (the tiles are still timed).
+  if(!autotune || !residueSearch || mult == MULT_USER)
     return new Conv(dim,kinds,L,M,mForce,A,B,mult,prec,batch);
   long mf[3]={0,0,0};
   for(int d=0; d < dim && d < 3; ++d) mf[d]=mForce ? mForce[d] : 0;
@@ -716,6 +720,12 @@ void Conv::tune()
     }
   }
   if(tn.empty()) return;
+  // A MULT_USER plan is timed without its functor (no multiplication).
+  struct Tuning {
+    bool& f;
+    explicit Tuning(bool& f) : f(f) {f=true;}
+    ~Tuning() {f=false;}
+  } tuningScope(tuning);
 
   // Scratch arrays (zeros: the kernels' timing does not depend on values).
   const size_t bytes=elements()*elemBytes();
@@ -887,7 +897,29 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   double scale=1.0;
   if(normalize)
     for(int d=0; d < I.dim; ++d) scale /= (double) I.axis[d].N;
+  // Slot positions for position-dependent (caller's) multipliers.
+  IndexMap im;
+  std::memset(&im,0,sizeof(im));
+  im.dim=I.dim;
+  for(int d=0; d < I.dim; ++d) im.N[d]=(int) I.axis[d].N;
+  im.real0=I.dim > 1 && I.axis[0].kind == KIND_REAL;
+  im.rowsY=I.dim == 3 ? I.axis[1].rows : 1;
+  if(I.mult == MULT_USER) {
+    for(int d=0; d < I.dim-1; ++d) {
+      const AxisPlan& a=I.axis[d];
+      im.m[d]=(int) a.m;
+      im.q[d]=(int) a.q;
+      im.rev[d]=inplaceFFT<T>() && a.kind != KIND_REAL && a.p == 1;
+      if(im.rev[d]) {
+        FFTPlanDev f=fftPlan(a.m,I.prec,true);
+        im.nst[d]=f.nst;
+        for(int k=0; k < f.nst; ++k) im.radix[d][k]=(unsigned char) f.radix[k];
+      }
+    }
+    if(I.longRow) im.q[0]=(int) I.rowQ;     // long 1D rows: k = row + q k2
+  }
   auto rowPlan=[&](RowPlan<T>& P, const AxisPlan& a) {
+    P.im=im;
     P.L=(int) a.stored; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
     P.cshift=a.cshift; P.A=A; P.B=B; P.mult=I.mult;
     P.realIO=a.kind == KIND_REAL && I.dim == 1;
@@ -898,6 +930,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };
   auto hermPlan=[&](HermRowPlan<T>& P, const AxisPlan& a) {
+    P.im=im;
     P.H=(int) a.stored; P.N=(int) a.N; P.Nh=(int) (a.N/2);
     P.A=A; P.B=B; P.mult=I.mult;
     P.rpc=a.rpc;
@@ -971,7 +1004,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
       P.rowStride=a.stored; P.nrows=batch; P.scale=(T) scale;
       P.io64=IN64 | OUT64;
-      e=launchHermRow<T>(P,a.thr,batch,s);
+      e=hermLaunch<T>(P,a.thr,batch,s);
       tick(s);
       return e;
     }
@@ -981,7 +1014,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
     P.rowStride=a.stored; P.nrows=batch; P.scale=(T) scale;
     P.io64=IN64 | OUT64;
-    e=launchRow<T>(P,a.thr,batch,s);
+    e=rowLaunch<T>(P,a.thr,batch,s);
     tick(s);
     return e;
   }
@@ -1014,7 +1047,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
     P.rowStride=m; P.nrows=q; P.scale=(T) 1;
-    e=launchRow<T>(P,a.thr,q,s);
+    e=rowLaunch<T>(P,a.thr,q,s);
     tick(s);
     if(e != cudaSuccess) return e;
     O.count=B;
@@ -1048,14 +1081,14 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
       for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
       P.rowStride=C; P.nrows=ax.rows; P.scale=(T) 1;
-      e=launchHermRow<T>(P,ay.thr,ax.rows,s);
+      e=hermLaunch<T>(P,ay.thr,ax.rows,s);
     } else {
       RowPlan<T> P;
       rowPlan(P,ay);
       for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
       P.rowStride=C; P.nrows=ax.rows; P.scale=(T) 1;
-      e=launchRow<T>(P,ay.thr,ax.rows,s);
+      e=rowLaunch<T>(P,ay.thr,ax.rows,s);
     }
     tick(s);
     if(e != cudaSuccess) return e;
@@ -1108,14 +1141,14 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) by[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) by[i];
     P.rowStride=nz; P.nrows=nrows; P.scale=(T) 1;
-    e=launchHermRow<T>(P,az.thr,nrows,s);
+    e=hermLaunch<T>(P,az.thr,nrows,s);
   } else {
     RowPlan<T> P;
     rowPlan(P,az);
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) by[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) by[i];
     P.rowStride=nz; P.nrows=nrows; P.scale=(T) 1;
-    e=launchRow<T>(P,az.thr,nrows,s);
+    e=rowLaunch<T>(P,az.thr,nrows,s);
   }
   tick(s);
   if(e != cudaSuccess) return e;
@@ -1139,8 +1172,65 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   return e;
 }
 
+template<typename T>
+cudaError_t Conv::rowLaunch(const RowPlan<T>& P, int thr, long long grid,
+                            cudaStream_t s)
+{
+  return user ? user->row(P,thr,grid,s) : launchRow<T>(P,thr,grid,s);
+}
+
+template<typename T>
+cudaError_t Conv::hermLaunch(const HermRowPlan<T>& P, int thr, long long grid,
+                             cudaStream_t s)
+{
+  return user ? user->herm(P,thr,grid,s) : launchHermRow<T>(P,thr,grid,s);
+}
+
+cudaError_t Conv::checkUser(const RowLaunchers *L)
+{
+  if(I.mult != MULT_USER) {
+    setLastError("this plan has a built-in multiplier; a device functor "
+                 "needs a plan made with the user multiplier");
+    return cudaErrorInvalidValue;
+  }
+  if(!L || L->inputs() != I.A || L->outputs() != I.B) {
+    setLastError("the functor's inputs and outputs (A, B) differ from the "
+                 "plan's");
+    return cudaErrorInvalidValue;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t Conv::runWith(const RowLaunchers *L, const void *const *in,
+                          void *const *out, cudaStream_t s)
+{
+  cudaError_t e=checkUser(L);
+  if(e != cudaSuccess) return e;
+  user=L;
+  e=run(in,out,s);
+  user=NULL;
+  return e;
+}
+
+cudaError_t Conv::runHostWith(const RowLaunchers *L, const void *const *in,
+                              void *const *out, cudaStream_t s)
+{
+  cudaError_t e=checkUser(L);
+  if(e != cudaSuccess) return e;
+  user=L;
+  e=runHost(in,out,s);
+  user=NULL;
+  return e;
+}
+
 cudaError_t Conv::run(const void *const *in, void *const *out, cudaStream_t s)
 {
+  if(I.mult == MULT_USER && !user && !tuning) {
+    setLastError("this plan multiplies with a caller's device functor: "
+                 "convolve through fgb::convolveWith "
+                 "(fftwpp_gb300_mult.cuh)");
+    return cudaErrorInvalidValue;
+  }
   marks=0;
   tick(s);
   if(I.prec == PREC_F64) return runT<double>(in,out,s);

@@ -14,6 +14,10 @@
 
 namespace fgb {
 
+struct RowLaunchers;       // kernels.cuh
+template<typename T> struct RowPlan;
+template<typename T> struct HermRowPlan;
+
 enum AxisKind {KIND_PAD=0, KIND_CENTERED=1, KIND_HERMITIAN=2, KIND_REAL=3};
 // PREC_FF: FP64 data at the interface, float-float arithmetic inside.
 enum Precision {PREC_F64=0, PREC_F32=1, PREC_FF=2};
@@ -82,6 +86,14 @@ public:
   // problems back to back in every array.
   cudaError_t run(const void *const *in, void *const *out, cudaStream_t s);
 
+  // The same for a plan made with MULT_USER: the innermost-axis launches go
+  // through the caller's instantiation of the row kernels with its own
+  // device functor (fftwpp_gb300_mult.cuh), whose arity must match A and B.
+  cudaError_t runWith(const RowLaunchers *L, const void *const *in,
+                      void *const *out, cudaStream_t s);
+  cudaError_t runHostWith(const RowLaunchers *L, const void *const *in,
+                          void *const *out, cudaStream_t s);
+
   // Host pointers (synchronous on s).  Page-locked arrays are read and
   // written by the kernels in place (zero copy) unless disabled
   // process-wide; other host memory is copied in and out.
@@ -122,6 +134,15 @@ public:
 private:
   ConvInfo I;
   long batch;
+  const RowLaunchers *user;        // row launches of a MULT_USER plan
+  bool tuning;                     // inside tune(): MULT_USER runs without
+                                   // a functor (no multiplication)
+  template<typename T> cudaError_t rowLaunch(const RowPlan<T>& P, int thr,
+                                             long long grid, cudaStream_t s);
+  template<typename T> cudaError_t hermLaunch(const HermRowPlan<T>& P,
+                                              int thr, long long grid,
+                                              cudaStream_t s);
+  cudaError_t checkUser(const RowLaunchers *L);
   std::vector<void *> bufs;        // device staging buffers
   size_t staging;
   void *hostIn, *hostOut;          // device copies for runHost

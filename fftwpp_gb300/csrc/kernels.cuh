@@ -42,7 +42,30 @@ template<typename T> __host__ __device__ constexpr bool inplaceFFT()
 enum MultKind {
   MULT_NONE=0, MULT_BINARY=1, MULT_REALBINARY=2, MULT_CORRELATION=3,
   MULT_REALJACOBIAN=4, MULT_JACOBIAN=5, MULT_REALJACADJ=6, MULT_DOT=7,
-  MULT_REALDOT=8
+  MULT_REALDOT=8,
+  MULT_USER=9              // a device functor compiled by the caller
+                           // (fftwpp_gb300_mult.cuh); the built-in kernels
+                           // treat it as no multiplication
+};
+
+// Where every multiplier slot of the innermost-axis kernels lies on the
+// padded grid, for multipliers that depend on position (the counterpart of
+// the reference's Indices, convolve.h:48-82, whose index[] holds the outer
+// axes' transformed indices and whose fft->index(r, i) gives the inner
+// one, convolve.h:297-326).  A row of the innermost kernel is a staging row
+// of the outer axes: in 2D the row of axis 0, in 3D row0 * rowsY + row1.
+// A complex outer axis stores residue r, entry j in row r*m + j (entries
+// in mixed-radix digit-reversed order when rev is set), transformed index
+// q*j + r; a real outer axis stores frequency k in row k.
+struct IndexMap {
+  int dim;                 // axes of the convolution
+  int N[3];                // padded length of each axis
+  int m[2], q[2];          // outer axes: residue block length and count
+  int real0;               // axis 0 is real (rows are frequencies)
+  int rev[2];              // outer axis rows digit-reversed within a block
+  int nst[2];              // ... over these radices (fftDIF order)
+  unsigned char radix[2][FGB_MAXSTAGES];
+  long long rowsY;         // 3D: staging rows of axis 1 per row of axis 0
 };
 
 template<typename T>
@@ -66,6 +89,7 @@ struct RowPlan {
   T scale;
   FFTPlanDev fp;           // length-m complex FFT
   const typename TwT<T>::type *twN;   // W_N^t, t < N
+  IndexMap im;             // slot positions (position-dependent multipliers)
 };
 
 template<typename T>
@@ -82,6 +106,7 @@ struct HermRowPlan {
   T scale;
   FFTPlanDev fp;           // length-Nh complex FFT
   const typename TwT<T>::type *twN;   // W_N^t, t < N
+  IndexMap im;             // slot positions (position-dependent multipliers)
 };
 
 template<typename T>
@@ -184,6 +209,29 @@ struct CopyArgs {
   size_t bytes;
 };
 cudaError_t launchBulkCopy(const CopyArgs& P, cudaStream_t s);
+
+// The innermost-axis launches of a convolution whose multiplier is a
+// caller's device functor: the functor's header (fftwpp_gb300_mult.cuh)
+// implements this interface by instantiating the row kernels with it, and
+// Conv routes its row launches through it.  Unsupported precisions return
+// cudaErrorNotSupported.
+struct RowLaunchers {
+  virtual ~RowLaunchers() {}
+  virtual int inputs() const=0;       // the functor's A
+  virtual int outputs() const=0;      // and B
+  virtual cudaError_t row(const RowPlan<double>& P, int threads,
+                          long long grid, cudaStream_t s) const=0;
+  virtual cudaError_t row(const RowPlan<float>& P, int threads,
+                          long long grid, cudaStream_t s) const=0;
+  virtual cudaError_t row(const RowPlan<ff>& P, int threads,
+                          long long grid, cudaStream_t s) const=0;
+  virtual cudaError_t herm(const HermRowPlan<double>& P, int threads,
+                           long long grid, cudaStream_t s) const=0;
+  virtual cudaError_t herm(const HermRowPlan<float>& P, int threads,
+                           long long grid, cudaStream_t s) const=0;
+  virtual cudaError_t herm(const HermRowPlan<ff>& P, int threads,
+                           long long grid, cudaStream_t s) const=0;
+};
 
 // Shared-memory bytes each kernel needs (for plan-time sizing).
 template<typename T> size_t rowSmem(int L, int m, int A, int B, int rpc=1,

@@ -39,6 +39,9 @@ extern "C" {
 #define FGB_MULT_REALJACADJ 6      /* adjoint of FGB_MULT_REALJACOBIAN */
 #define FGB_MULT_DOT 7             /* F0 = sum_k F_k F_{A/2+k} */
 #define FGB_MULT_REALDOT 8         /* the same, lane-wise on doubles */
+#define FGB_MULT_USER 9            /* a caller's device functor, compiled
+                                      into the row kernels by
+                                      fftwpp_gb300_mult.cuh */
 
 #define FGB_F64 0
 #define FGB_F32 1                  /* FP32 data, split hi+lo twiddles */
@@ -73,6 +76,22 @@ int fgb_convolve_device(fgb_conv *c, void *const *in, void *const *out,
  * transfers overlap the transforms); other host memory is copied in and
  * out.  This is also the path of the FFTW++-compatible convolve calls. */
 int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out);
+
+/* Convolve with a caller's device multiplier (the reference's user
+ * multiplier hook, typedef multiplier in convolve.h:78-79, with the slot
+ * positions of its Indices, convolve.h:48-82).  The plan is made by
+ * fgb_create with mult = FGB_MULT_USER; `launchers` is the row-kernel
+ * instantiation for the functor that fgb::convolveWith /
+ * fgb::convolveHostWith (fftwpp_gb300_mult.cuh, a CUDA C++ header) build
+ * and pass here -- C callers use those templates rather than these entry
+ * points directly.  Device arrays on `stream`, or host arrays
+ * (synchronous), as fgb_convolve_device / fgb_convolve_host; -1 when the
+ * plan's multiplier is not FGB_MULT_USER or the functor's A, B differ from
+ * the plan's. */
+int fgb_convolve_device_with(fgb_conv *c, const void *launchers,
+                             void *const *in, void *const *out, void *stream);
+int fgb_convolve_host_with(fgb_conv *c, const void *launchers,
+                           void *const *in, void *const *out);
 
 /* Arithmetic of the FFTW++-compatible entry points (cfftw++.h creators,
  * the _dot forms and include/convolve.h), whose arrays are FP64: FGB_F64

@@ -217,3 +217,46 @@ def test_sampled_direct_sum_3d():
     pts = [(4, 3, 5), (0, 0, 0), (2, 1, 3), (4, 0, 5), (1, 3, 2)]
     np.testing.assert_allclose(directconv3_at(f, g, pts),
                                [h[p] for p in pts], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("case", [
+    ([0], [9], [17], "binary"),
+    ([1], [9], [13], "binary"),
+    ([2], [15], [22], "realbinary"),
+    ([3], [9], [17], "binary"),
+    ([1, 2], [9, 7], [13, 10], "realbinary"),
+    ([0, 0], [6, 5], [11, 9], "binary"),
+    ([3, 0, 0], [4, 5, 3], [7, 9, 5], "binary"),
+    ([1, 1, 2], [5, 5, 5], [7, 7, 7], "realbinary")])
+def test_explicit_oracle_matches_hybrid(case):
+    """The explicit N-grid oracle (the checker of position-dependent
+    multipliers) equals the hybrid restatement for position-independent
+    multipliers, on padded grids larger than M as well."""
+    from oracle import explicit as E
+    from oracle import hybrid as H
+    kinds, L, M, mult = case
+    rng = np.random.default_rng(sum(L))
+    shape = [(l + 1) // 2 if k == H.HERMITIAN else l for k, l in zip(kinds, L)]
+    fs = []
+    for _ in range(2):
+        if kinds[0] == H.REAL:
+            f = rng.normal(size=shape)
+        else:
+            f = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        if kinds[-1] == H.HERMITIAN:
+            if len(kinds) == 1:
+                f[0] = f[0].real
+            elif len(kinds) == 2:
+                H.hermitian_symmetrize_x(f, (L[0] + 1) // 2, shape[1],
+                                         L[0] // 2)
+            else:
+                H.hermitian_symmetrize_xy(f, (L[0] + 1) // 2, (L[1] + 1) // 2,
+                                          shape[2], L[0] // 2, L[1] // 2)
+        fs.append(f)
+    want = H.convolve(fs, kinds, L, M, mult=mult)[0]
+    for extra in (0, 3):
+        Ns = [m + extra + ((m + extra) % 2 if k in (H.HERMITIAN, H.REAL)
+                           else 0) for k, m in zip(kinds, M)]
+        got = E.convolve(fs, kinds, L, Ns, lambda v, ix: [v[0] * v[1]])[0]
+        err = Dr.rel_l2(got, want)
+        assert err <= 1e-13, (Ns, err)
