@@ -49,6 +49,12 @@ def load():
     lib.fgb_convolve_device.argtypes = [vp, P(vp), P(vp), vp]
     lib.fgb_convolve_host.restype = ctypes.c_int
     lib.fgb_convolve_host.argtypes = [vp, P(vp), P(vp)]
+    lib.fgb_convolve_device_with.restype = ctypes.c_int
+    lib.fgb_convolve_device_with.argtypes = [vp, vp, P(vp), P(vp), vp]
+    lib.fgb_convolve_host_with.restype = ctypes.c_int
+    lib.fgb_convolve_host_with.argtypes = [vp, vp, P(vp), P(vp)]
+    lib.fgb_set_strides.restype = ctypes.c_int
+    lib.fgb_set_strides.argtypes = [vp, P(sz)]
     lib.fgb_info.restype = ctypes.c_int
     lib.fgb_info.argtypes = [vp, P(ctypes.c_long)]
     lib.fgb_timing.restype = ctypes.c_int

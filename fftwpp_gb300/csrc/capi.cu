@@ -670,6 +670,23 @@ int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out)
   return 0;
 }
 
+int fgb_set_strides(fgb_conv *c, const size_t *stride)
+{
+  if(!c) {report("fgb_set_strides","bad arguments"); return -1;}
+  try {
+    if(!stride) c->conv->setStrides(NULL);
+    else {
+      long S[3]={0,0,0};
+      for(int d=0; d+1 < c->conv->info().dim; ++d) S[d]=(long) stride[d];
+      c->conv->setStrides(S);
+    }
+  } catch(std::exception& e) {
+    report("fgb_set_strides",e.what());
+    return -1;
+  }
+  return 0;
+}
+
 int fgb_convolve_device_with(fgb_conv *c, const void *launchers,
                              void *const *in, void *const *out, void *stream)
 {

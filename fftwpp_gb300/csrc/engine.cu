@@ -422,7 +422,8 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
 Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
            const long *mForce, int A, int B, int mult, int prec, long batch,
            bool tuneSchedule)
-  : batch(batch), user(NULL), tuning(false), staging(0), hostIn(NULL),
+  : batch(batch), user(NULL), isStrided(false), tuning(false), staging(0),
+    hostIn(NULL),
     hostOut(NULL), nlaunch(0),
     timing(false), normalize(true), marks(0), hostTile(0), hostThr(0),
     hostTileB(0), hostThrB(0), side(NULL), chunks(0)
@@ -824,6 +825,38 @@ size_t Conv::elements() const
   return n;
 }
 
+void Conv::setStrides(const long *S)
+{
+  if(!S) {
+    isStrided=false;
+    return;
+  }
+  if(I.dim < 2 || batch != 1)
+    throw std::runtime_error("strides apply to the outer axes of 2D and 3D "
+                             "convolutions");
+  const long inner=I.axis[I.dim-1].stored;
+  if(S[I.dim-2] < inner)
+    throw std::runtime_error("the stride of axis "+std::to_string(I.dim-2)+
+                             " is less than the "+std::to_string(inner)+
+                             " entries of the axis inside it");
+  if(I.dim == 3 && S[0] < I.axis[1].L*S[1])
+    throw std::runtime_error("the stride of axis 0 is less than Ly times "
+                             "the stride of axis 1");
+  bool dense=S[I.dim-2] == inner && (I.dim == 2 || S[0] == I.axis[1].L*S[1]);
+  for(int d=0; d < I.dim-1; ++d) strideS[d]=S[d];
+  isStrided=!dense;
+  if(hostIn) {                     // host copies are now sized by the span
+    cudaFree(hostIn);
+    hostIn=NULL;
+  }
+}
+
+size_t Conv::spanElements() const
+{
+  if(!isStrided) return elements();
+  return (size_t) I.axis[0].L*(size_t) strideS[0];
+}
+
 void Conv::allocate()
 {
   size_t e=elem(I.prec);
@@ -998,7 +1031,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   if(I.dim == 1 && !I.longRow) {
     const AxisPlan& a=I.axis[0];
     if(a.kind == KIND_HERMITIAN) {
-      HermRowPlan<T> P;
+      HermRowPlan<T> P{};
       hermPlan(P,a);
       for(int i=0; i < A; ++i) P.in[i]=(const Cx *) in[i];
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
@@ -1008,7 +1041,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
       tick(s);
       return e;
     }
-    RowPlan<T> P;
+    RowPlan<T> P{};
     rowPlan(P,a);
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) in[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) out[i];
@@ -1022,7 +1055,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   if(I.dim == 1) {  // long 1D complex
     const AxisPlan& a=I.axis[0];
     long m=I.rowM, q=I.rowQ;
-    OuterPlan<T> O;
+    OuterPlan<T> O{};
     O.L=(int) a.p; O.m=(int) q; O.q=1; O.N=(int) q; O.cshift=0;
     O.tile=a.tile;
     O.fp=fftPlan(q,I.prec);
@@ -1042,7 +1075,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     if(e != cudaSuccess) return e;
     AxisPlan ra=a;
     ra.stored=m; ra.L=m; ra.m=m; ra.q=1; ra.N=m; ra.cshift=0;
-    RowPlan<T> P;
+    RowPlan<T> P{};
     rowPlan(P,ra);
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
@@ -1065,10 +1098,14 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     const AxisPlan& ax=I.axis[0];
     const AxisPlan& ay=I.axis[1];
     long C=ay.stored;
-    OuterPlan<T> O;
+    OuterPlan<T> O{};
     outerPlan(O,ax);
     O.count=A; O.nbatch=1; O.inBatch=O.outBatch=0;
     O.inRow=C; O.outRow=C; O.C=(int) C; O.Ltot=(long long) ax.L*C;
+    if(isStrided) {                 // data side (the caller's arrays)
+      O.inRow=strideS[0];
+      O.Ltot=LLONG_MAX;
+    }
     O.scale=(T) 1;
     O.io64=IN64;
     for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) bufs[i];}
@@ -1076,14 +1113,14 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     tick(s);
     if(e != cudaSuccess) return e;
     if(ay.kind == KIND_HERMITIAN) {
-      HermRowPlan<T> P;
+      HermRowPlan<T> P{};
       hermPlan(P,ay);
       for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
       P.rowStride=C; P.nrows=ax.rows; P.scale=(T) 1;
       e=hermLaunch<T>(P,ay.thr,ax.rows,s);
     } else {
-      RowPlan<T> P;
+      RowPlan<T> P{};
       rowPlan(P,ay);
       for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
@@ -1096,6 +1133,8 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.tile=ax.tileB;
     O.scale=(T) scale;
     O.io64=OUT64;
+    O.inRow=C;                                  // staging side
+    O.outRow=isStrided ? strideS[0] : C;        // data side
     for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) bufs[i]; O.out[i]=(Cx *) out[i];}
     e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(O,ax.thrB,s) :
       launchOuterBwd<T>(O,ax.thrB,s);
@@ -1112,18 +1151,23 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   void **bx=bufs.data();
   void **by=bufs.data()+A;
 
-  OuterPlan<T> X;
+  OuterPlan<T> X{};
   outerPlan(X,ax);
   X.count=A; X.nbatch=1; X.inBatch=X.outBatch=0;
   X.inRow=Cx_; X.outRow=Cx_; X.C=(int) Cx_; X.Ltot=(long long) ax.L*Cx_;
   X.scale=(T) 1;
   X.io64=IN64;
+  if(isStrided) {                   // data side (the caller's arrays)
+    X.inRow=strideS[0];
+    X.Ltot=LLONG_MAX;
+    if(strideS[1] != nz) {X.cz=(int) nz; X.cs=strideS[1];}
+  }
   for(int i=0; i < A; ++i) {X.in[i]=(const Cx *) in[i]; X.out[i]=(Cx *) bx[i];}
   e=firstOuter(X,ax);
   tick(s);
   if(e != cudaSuccess) return e;
 
-  OuterPlan<T> Y;
+  OuterPlan<T> Y{};
   outerPlan(Y,ay);
   Y.count=A; Y.nbatch=(int) ax.rows;
   Y.inBatch=ay.L*nz; Y.outBatch=ay.rows*nz;
@@ -1136,14 +1180,14 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
 
   long nrows=ax.rows*ay.rows;
   if(az.kind == KIND_HERMITIAN) {
-    HermRowPlan<T> P;
+    HermRowPlan<T> P{};
     hermPlan(P,az);
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) by[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) by[i];
     P.rowStride=nz; P.nrows=nrows; P.scale=(T) 1;
     e=hermLaunch<T>(P,az.thr,nrows,s);
   } else {
-    RowPlan<T> P;
+    RowPlan<T> P{};
     rowPlan(P,az);
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) by[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) by[i];
@@ -1165,6 +1209,8 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   X.tile=ax.tileB;
   X.scale=(T) scale;
   X.io64=OUT64;
+  X.inRow=Cx_;                                  // staging side
+  X.outRow=isStrided ? strideS[0] : Cx_;        // data side
   for(int i=0; i < B; ++i) {X.in[i]=(const Cx *) bx[i]; X.out[i]=(Cx *) out[i];}
   e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(X,ax.thrB,s) :
     launchOuterBwd<T>(X,ax.thrB,s);
@@ -1461,9 +1507,55 @@ void Conv::hostPath(int *inputs, int *outputs) const
   if(outputs) *outputs=wo;
 }
 
+// Host arrays in a strided layout: page-locked ones are read and written
+// in place by the first and last kernels; other host memory is copied in
+// whole (gaps included) and the stored entries copied back row by row, so
+// that the gaps of separate output arrays stay untouched.
+cudaError_t Conv::runHostStrided(const void *const *in, void *const *out,
+                                 cudaStream_t s)
+{
+  const int A=I.A, B=I.B;
+  const size_t eb=elemBytes(), span=spanElements()*eb;
+  if(zeroCopy) {
+    std::vector<const void *> min(A);
+    std::vector<void *> mout(B);
+    bool ok=true;
+    for(int a=0; a < A && ok; ++a) ok=(min[a]=mappedAddress(in[a])) != NULL;
+    for(int b=0; b < B && ok; ++b) ok=(mout[b]=mappedAddress(out[b])) != NULL;
+    if(ok) {
+      cudaError_t e=run(min.data(),mout.data(),s);
+      return e != cudaSuccess ? e : cudaStreamSynchronize(s);
+    }
+  }
+  if(!hostIn && devAlloc((void **) &hostIn,span*A) != cudaSuccess)
+    return cudaErrorMemoryAllocation;
+  std::vector<void *> din(A);
+  cudaError_t e;
+  for(int a=0; a < A; ++a) {
+    din[a]=(char *) hostIn+a*span;
+    if((e=cudaMemcpyAsync(din[a],in[a],span,cudaMemcpyHostToDevice,s)) !=
+       cudaSuccess) return e;
+  }
+  if((e=run(din.data(),din.data(),s)) != cudaSuccess) return e;
+  // Stored rows: of the innermost axis (3D: per plane of axis 0).
+  const size_t inner=(size_t) I.axis[I.dim-1].stored*eb;
+  const long planes=I.dim == 3 ? I.axis[0].L : 1;
+  const long rows=I.dim == 3 ? I.axis[1].L : I.axis[0].L;
+  const size_t pitch=(size_t) strideS[I.dim-2]*eb;
+  const size_t plane=(size_t) strideS[0]*eb;
+  for(int b=0; b < B; ++b)
+    for(long k=0; k < planes; ++k)
+      if((e=cudaMemcpy2DAsync((char *) out[b]+k*plane,pitch,
+                              (const char *) din[b]+k*plane,pitch,inner,rows,
+                              cudaMemcpyDeviceToHost,s)) != cudaSuccess)
+        return e;
+  return cudaStreamSynchronize(s);
+}
+
 cudaError_t Conv::runHost(const void *const *in, void *const *out,
                           cudaStream_t s)
 {
+  if(isStrided) return runHostStrided(in,out,s);
   size_t bytes=elements()*elemBytes();
   int A=I.A, B=I.B;
   if(zeroCopy) {
@@ -1553,7 +1645,7 @@ cudaError_t PadTransform::runT(const void *in, void *out, bool fwd,
                                cudaStream_t s)
 {
   typedef cplx<T> Cx;
-  OuterPlan<T> P;
+  OuterPlan<T> P{};
   P.L=(int) a.L; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
   P.cshift=a.cshift; P.tile=fwd ? a.tile : a.tileB;
   P.fp=fftPlan(a.kind == KIND_REAL ? a.N/2 : a.m,prec);
@@ -1627,7 +1719,7 @@ template<typename T>
 cudaError_t PlainFFT::runT(const void *in, void *out, cudaStream_t s)
 {
   typedef cplx<T> Cx;
-  OuterPlan<T> P;
+  OuterPlan<T> P{};
   const bool real=kind != FFT_C2C;
   P.L=(int) n; P.m=(int) n; P.q=1; P.N=(int) n; P.cshift=0;
   P.tile=tile;

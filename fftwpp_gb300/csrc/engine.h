@@ -108,6 +108,17 @@ public:
   // measured), -1 while still to be measured.
   void hostPath(int *inputs, int *outputs) const;
 
+  // Strided layouts of the caller's arrays (fftPad(L,M,app,C,S) with S > C,
+  // convolve.h:515-536; the Sx / Sy strides of Convolution2/3,
+  // convolve.h:1274, 1556): S[d], d < dim-1, elements between consecutive
+  // entries of outer axis d; the innermost axis stays contiguous.  NULL
+  // restores the dense layout.  Throws std::runtime_error on strides
+  // smaller than the data they step over.
+  void setStrides(const long *S);
+  bool strided() const {return isStrided;}
+  // Elements a strided array spans (the dense count otherwise).
+  size_t spanElements() const;
+
   const ConvInfo& info() const {return I;}
   size_t elemBytes() const;        // bytes per stored element
   size_t elements() const;         // stored elements per array (x batch)
@@ -135,6 +146,10 @@ private:
   ConvInfo I;
   long batch;
   const RowLaunchers *user;        // row launches of a MULT_USER plan
+  bool isStrided;
+  long strideS[3];                 // outer-axis strides (setStrides)
+  cudaError_t runHostStrided(const void *const *in, void *const *out,
+                             cudaStream_t s);
   bool tuning;                     // inside tune(): MULT_USER runs without
                                    // a functor (no multiplication)
   template<typename T> cudaError_t rowLaunch(const RowPlan<T>& P, int thr,

@@ -13,6 +13,19 @@ namespace fgb {
 
 
 // ---------------------------------------------------------------------------
+// Offset of column col on the data side of an outer kernel (the caller's
+// arrays): col itself for dense layouts, (col / cz) cs + col % cz for the
+// strided layouts of fftPad(L, M, app, C, S) with S > C (convolve.h:515-536;
+// Convolution2/3's Sx, Sy, convolve.h:1274, 1556).
+template<typename T>
+__device__ __forceinline__ long long dataCol(const OuterPlan<T>& P, int col)
+{
+  if(P.cz <= 0) return col;
+  const int g=col/P.cz;
+  return (long long) g*P.cs+(col-g*P.cz);
+}
+
+// ---------------------------------------------------------------------------
 // Outer forward, complex data: residue block r of the padded transform along
 // a strided axis for `tile` adjacent columns.
 template<typename T, bool CG>
@@ -40,7 +53,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
       int t=dTile(i), cc=i-t*tile;
       int col=col0+cc;
       int s=posmod(t+c,m);
-      long long off=(long long) s*P.inRow+col;
+      long long off=(long long) s*P.inRow+dataCol(P,col);
       if(s < L && col < P.C && off < P.Ltot) cpAsync(x+sp(i),src+off);
       else x[sp(i)]=mk((T) 0,(T) 0);
     }
@@ -50,7 +63,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
         int t=dTile(i), cc=i-t*tile;
         int col=col0+cc;
         int s=posmod(t+c,m);
-        long long off=(long long) s*P.inRow+col;
+        long long off=(long long) s*P.inRow+dataCol(P,col);
         if(s < L && col < P.C && off < P.Ltot) {
           if(P.io64 & 1) convertStaged(x,sp(i));
           if(r != 0) x[sp(i)]=twmul<1>(x[sp(i)],tw[twExp(s,c,r,N)]);
@@ -65,7 +78,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
     for(int i=tid; i < L*tile; i += nthr) {
       int s=dTile(i), cc=i-s*tile;
       int col=col0+cc;
-      long long off=(long long) s*P.inRow+col;
+      long long off=(long long) s*P.inRow+dataCol(P,col);
       if(col < P.C && off < P.Ltot) cpAsync(y+i,src+off);
       else y[i]=mk((T) 0,(T) 0);
     }
@@ -75,7 +88,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
       for(int i=tid; i < L*tile; i += nthr) {
         int s=dTile(i), cc=i-s*tile;
         int col=col0+cc;
-        long long off=(long long) s*P.inRow+col;
+        long long off=(long long) s*P.inRow+dataCol(P,col);
         if(col < P.C && off < P.Ltot) convertStaged(y,i);
       }
     }
@@ -199,7 +212,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
       for(int i=tid; i < L*tile; i += nthr) {
         int s=dTile(i), cc=i-s*tile;
         int col=col0+cc;
-        long long off=(long long) s*P.outRow+col;
+        long long off=(long long) s*P.outRow+dataCol(P,col);
         if(col < P.C && off < P.Ltot)
           storeIO(dst+off,X[sp(posmod(s-c,m)*tile+cc)]*P.scale,P.io64 & 2);
       }
@@ -218,7 +231,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
   for(int i=tid; i < L*tile; i += nthr) {
     int s=dTile(i), cc=i-s*tile;
     int col=col0+cc;
-    long long off=(long long) s*P.outRow+col;
+    long long off=(long long) s*P.outRow+dataCol(P,col);
     if(col < P.C && off < P.Ltot) storeIO(dst+off,acc[i]*P.scale,P.io64 & 2);
   }
   __syncthreads();
@@ -260,8 +273,9 @@ outerRealFwdKernel(const OuterPlan<T> P)
     T re=(T) 0, im=(T) 0;
     if(col < P.C) {
       int s=2*t;
-      if(s < L) re=loadIOr(src+(long long) s*P.inRow+col,P.io64 & 1);
-      if(s+1 < L) im=loadIOr(src+(long long) (s+1)*P.inRow+col,P.io64 & 1);
+      const long long dc=dataCol(P,col);
+      if(s < L) re=loadIOr(src+(long long) s*P.inRow+dc,P.io64 & 1);
+      if(s+1 < L) im=loadIOr(src+(long long) (s+1)*P.inRow+dc,P.io64 & 1);
     }
     x[sp(i)]=mk(re,im);
   }
@@ -333,8 +347,9 @@ outerRealBwdKernel(const OuterPlan<T> P)
     if(col >= P.C) continue;
     cplx<T> v=X[sp(i)]*P.scale;
     int s=2*t;
-    if(s < L) storeIOr(dst+(long long) s*P.outRow+col,v.x,P.io64 & 2);
-    if(s+1 < L) storeIOr(dst+(long long) (s+1)*P.outRow+col,v.y,P.io64 & 2);
+    const long long dc=dataCol(P,col);
+    if(s < L) storeIOr(dst+(long long) s*P.outRow+dc,v.x,P.io64 & 2);
+    if(s+1 < L) storeIOr(dst+(long long) (s+1)*P.outRow+dc,v.y,P.io64 & 2);
   }
 }
 

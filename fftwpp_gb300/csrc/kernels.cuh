@@ -128,6 +128,8 @@ struct OuterPlan {
                            // a residue block in digit-reversed order
   int conj;                // real kernels: conjugate the complex side
                            // (the sign -1 r2c / sign +1 c2r of plain FFTs)
+  int cz;                  // data side with strides: column c lies at
+  long long cs;            // (c / cz) cs + c % cz (cz = 0: at c)
   T scale;
   FFTPlanDev fp;           // length-m (complex) or length-N/2 (real) FFT
   const typename TwT<T>::type *twN;

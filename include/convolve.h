@@ -16,16 +16,20 @@
 //    members m, p, q, n of a transform are those of the GPU plan, filled in
 //    when the Convolution that uses it is constructed; a forced
 //    Application m is honoured (convolve.h:103-111);
-//  * multipliers must be one of the built-ins (or jacobianMultiplier): a
-//    host function pointer cannot run on the device, and there is no CPU
-//    fallback, so any other multiplier throws std::invalid_argument;
-//  * arrays must be dense (S == C): strided layouts throw;
+//  * a host function pointer cannot run on the device and there is no CPU
+//    fallback, so a multiplier is one of the built-ins (or
+//    jacobianMultiplier), recognised by address, or a device functor
+//    compiled into the row kernels: Application(A, B, DeviceMultiplier{
+//    fgb::deviceLaunchers(functor)}, ...) from a .cu file that includes
+//    fftwpp_gb300_mult.cuh; any other host multiplier throws
+//    std::invalid_argument;
 //  * errors throw std::runtime_error instead of exit() (convolve.h:226-232).
 #ifndef FFTWPP_GB300_CONVOLVE_H
 #define FFTWPP_GB300_CONVOLVE_H
 
 #include <cmath>
 #include <cstddef>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -144,6 +148,13 @@ inline void jacobianMultiplier(Complex **F, size_t n, Indices *, size_t)
   for(size_t j=0; j < n; ++j) F0[j]=F0[j]*F3[j]-F1[j]*F2[j];
 }
 
+// A multiplier compiled for the device from a caller's functor: the
+// row-kernel instantiation built by fgb::deviceLaunchers (declared in
+// fftwpp_gb300_mult.cuh, which needs nvcc), kept alive by this handle.
+struct DeviceMultiplier {
+  std::shared_ptr<const void> launchers;
+};
+
 inline int multiplierCode(multiplier *m)
 {
   if(m == multNone) return FGB_MULT_NONE;
@@ -165,6 +176,7 @@ public:
   size_t m, D;
   ptrdiff_t I;
   size_t maxthreads;
+  DeviceMultiplier device;
   Application(size_t A, size_t B, multiplier *mult,
               size_t threads=fftw::maxthreadsRef(), bool verbose=false,
               size_t m=0, size_t D=0, ptrdiff_t I=-1)
@@ -174,6 +186,17 @@ public:
               size_t m=0, size_t D=0, ptrdiff_t I=-1)
     : A(A), B(B), mult(mult), threads(1), verbose(parent.verbose),
       m(m == 1 ? 0 : m), D(D), I(I), maxthreads(parent.maxthreads) {}
+  // A device functor in place of the host multiplier.
+  Application(size_t A, size_t B, DeviceMultiplier device,
+              size_t threads=fftw::maxthreadsRef(), bool verbose=false,
+              size_t m=0, size_t D=0, ptrdiff_t I=-1)
+    : A(A), B(B), mult(NULL), threads(threads), verbose(verbose),
+      m(m == 1 ? 0 : m), D(D), I(I), maxthreads(threads), device(device) {}
+  Application(size_t A, size_t B, DeviceMultiplier device,
+              Application& parent, size_t m=0, size_t D=0, ptrdiff_t I=-1)
+    : A(A), B(B), mult(NULL), threads(1), verbose(parent.verbose),
+      m(m == 1 ? 0 : m), D(D), I(I), maxthreads(parent.maxthreads),
+      device(device) {}
 };
 
 // fftBase (convolve.h:123-464): the padding specification of one axis.
@@ -258,6 +281,7 @@ protected:
   fgb_conv *plan;
   std::vector<fftBase *> ffts;
   size_t A, B;
+  std::shared_ptr<const void> launchers;     // device functor, if any
   void build(std::vector<fftBase *> axes) {
     ffts=axes;
     int dim=(int) axes.size();
@@ -272,18 +296,43 @@ protected:
       M[d]=axes[d]->M;
       m[d]=axes[d]->m;
     }
-    // Dense layouts only: the column count of each outer axis must be the
-    // stored size of the axes inside it, with unit extra stride.
-    size_t inner=1;
-    for(int d=dim-1; d >= 0; --d) {
-      if(d < dim-1 && (axes[d]->C != inner || axes[d]->S != inner))
-        throw std::invalid_argument("fftwpp_gb300: strided layouts (S != C) "
-                                    "are not supported");
-      inner *= (size_t) axes[d]->inputLength();
+    // Layouts (convolve.h:1274, 1556, 1614-1622): in 2D the x axis has C =
+    // the stored y entries and stride S = Sx >= C; in 3D the y axis has
+    // C = the stored z entries and S = Sy, the x axis S = Sx >= Ly Sy and
+    // C = Ly Sy when Sy is the z extent, else the z extent.
+    size_t S[3]={0,0,0};
+    bool dense=true;
+    if(dim == 2) {
+      size_t Hy=axes[1]->inputLength();
+      if(axes[0]->C != Hy)
+        throw std::invalid_argument("fftwpp_gb300: the x transform's count C "
+                                    "must be the stored y extent");
+      S[0]=axes[0]->S;
+      dense=S[0] == Hy;
+    } else if(dim == 3) {
+      size_t Hz=axes[2]->inputLength();
+      if(axes[1]->C != Hz)
+        throw std::invalid_argument("fftwpp_gb300: the y transform's count C "
+                                    "must be the stored z extent");
+      S[1]=axes[1]->S;
+      S[0]=axes[0]->S;
+      if(axes[0]->C != (S[1] == Hz ? L[1]*S[1] : Hz))
+        throw std::invalid_argument("fftwpp_gb300: the x transform's count C "
+                                    "must be Ly Sy (contiguous y-z planes) "
+                                    "or the stored z extent");
+      dense=S[1] == Hz && S[0] == L[1]*Hz;
     }
-    plan=fgb_create(dim,kinds,L,M,m,(int) A,(int) B,
-                    multiplierCode(app.mult),fgb_get_drop_in_precision(),1);
+    launchers=app.device.launchers;
+    int code=launchers ? FGB_MULT_USER : multiplierCode(app.mult);
+    plan=fgb_create(dim,kinds,L,M,m,(int) A,(int) B,code,
+                    fgb_get_drop_in_precision(),1);
     if(!plan) throw std::runtime_error(fgb_last_error());
+    if(!dense && fgb_set_strides(plan,S) != 0) {
+      std::string why=fgb_last_error();
+      fgb_destroy(plan);
+      plan=NULL;
+      throw std::invalid_argument(why);
+    }
     long info[32];
     fgb_info(plan,info);
     for(int d=0; d < dim; ++d) axes[d]->setPlan(info+8*d);
@@ -292,8 +341,9 @@ protected:
     void *in[8];
     for(size_t a=0; a < A; ++a) in[a]=(void *) (f[a]+offset);
     fgb_set_normalize(plan,normalize ? 1 : 0);
-    if(fgb_convolve_host(plan,in,in) != 0)
-      throw std::runtime_error(fgb_last_error());
+    int rc=launchers ? fgb_convolve_host_with(plan,launchers.get(),in,in) :
+      fgb_convolve_host(plan,in,in);
+    if(rc != 0) throw std::runtime_error(fgb_last_error());
   }
 public:
   ConvolutionBase() : plan(NULL), A(0), B(0) {}

@@ -77,6 +77,18 @@ int fgb_convolve_device(fgb_conv *c, void *const *in, void *const *out,
  * out.  This is also the path of the FFTW++-compatible convolve calls. */
 int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out);
 
+/* Strided layouts (the reference's fftPad(L, M, app, C, S) with S > C,
+ * convolve.h:515-536, and the Sx / Sy strides of Convolution2 /
+ * Convolution3, convolve.h:1274, 1556; driven by tests/hybridconv2.cc,
+ * hybridconvh2.cc, hybridconv3.cc): stride[d] for each outer axis
+ * d < dim-1 is the number of elements between consecutive entries of axis
+ * d in every input and output array (2D: entry (i, j) at i*stride[0] + j;
+ * 3D: (i, j, k) at i*stride[0] + j*stride[1] + k); the innermost axis is
+ * contiguous.  Entries in the gaps are neither read nor written.  NULL
+ * restores the dense layout.  2D and 3D plans only; -1 for strides
+ * smaller than the data they step over. */
+int fgb_set_strides(fgb_conv *c, const size_t *stride);
+
 /* Convolve with a caller's device multiplier (the reference's user
  * multiplier hook, typedef multiplier in convolve.h:78-79, with the slot
  * positions of its Indices, convolve.h:48-82).  The plan is made by

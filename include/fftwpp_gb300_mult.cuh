@@ -41,6 +41,8 @@
 #ifndef FFTWPP_GB300_MULT_CUH
 #define FFTWPP_GB300_MULT_CUH
 
+#include <memory>
+
 #include "fftwpp_gb300.h"
 #include "../fftwpp_gb300/csrc/rowkernels.cuh"
 
@@ -116,8 +118,21 @@ template<int PRECS=7, class F>
 int convolveWith(fgb_conv *plan, const F& f, void *const *in,
                  void *const *out, cudaStream_t stream=0)
 {
-  FunctorLaunchers<F,PRECS> L(f);
-  return fgb_convolve_device_with(plan,&L,in,out,(void *) stream);
+  const FunctorLaunchers<F,PRECS> L(f);
+  const RowLaunchers *base=&L;      // the library reads a RowLaunchers *
+  return fgb_convolve_device_with(plan,base,in,out,(void *) stream);
+}
+
+// The row-kernel instantiation for f as a type-erased handle, for the C++
+// drop-in API: Application(A, B, fftwpp::DeviceMultiplier{
+// fgb::deviceLaunchers(f)}, ...) (include/convolve.h).
+template<int PRECS=7, class F>
+std::shared_ptr<const void> deviceLaunchers(const F& f)
+{
+  std::shared_ptr<const RowLaunchers> p=
+    std::make_shared<const FunctorLaunchers<F,PRECS>>(f);
+  // The erased pointer is the RowLaunchers base, which the library reads.
+  return std::shared_ptr<const void>(p,static_cast<const void *>(p.get()));
 }
 
 // The same on host arrays (as fgb_convolve_host), synchronous.
@@ -125,8 +140,9 @@ template<int PRECS=7, class F>
 int convolveHostWith(fgb_conv *plan, const F& f, void *const *in,
                      void *const *out)
 {
-  FunctorLaunchers<F,PRECS> L(f);
-  return fgb_convolve_host_with(plan,&L,in,out);
+  const FunctorLaunchers<F,PRECS> L(f);
+  const RowLaunchers *base=&L;
+  return fgb_convolve_host_with(plan,base,in,out);
 }
 
 } // namespace fgb

@@ -68,3 +68,43 @@ int user_mixed_device(fgb_conv *c, void **in, void **out, void *s)
 }
 
 }
+
+// The same weighted product through the FFTW++-compatible C++ classes
+// (include/convolve.h): a 2D centred-Hermitian Convolution2 whose y
+// Application carries the functor, on host arrays with x stride Sx.
+#include "convolve.h"
+
+extern "C" int cpp_weighted_her2(const double *f, const double *g, double *h,
+                                 size_t Lx, size_t Ly, size_t Sx, long *N)
+{
+  using namespace fftwpp;
+  try {
+    size_t Hy=utils::ceilquotient(Ly,2);
+    Application appx(2,1,multNone);
+    Application appy(2,1,DeviceMultiplier{fgb::deviceLaunchers(Weighted())},
+                     appx);
+    fftPadCentered fftx(Lx,3*utils::ceilquotient(Lx,2)-2*(Lx%2),appx,Hy,Sx);
+    fftPadHermitian ffty(Ly,3*Hy-2*(Ly%2),appy);
+    Convolution2 C(&fftx,&ffty);
+    Complex **F=utils::ComplexAlign(2,Lx*Sx);
+    for(size_t i=0; i < Lx; ++i)
+      for(size_t j=0; j < Hy; ++j) {
+        F[0][i*Sx+j]=Complex(f[2*(i*Hy+j)],f[2*(i*Hy+j)+1]);
+        F[1][i*Sx+j]=Complex(g[2*(i*Hy+j)],g[2*(i*Hy+j)+1]);
+      }
+    C.convolve(F);
+    for(size_t i=0; i < Lx; ++i)
+      for(size_t j=0; j < Hy; ++j) {
+        h[2*(i*Hy+j)]=F[0][i*Sx+j].re;
+        h[2*(i*Hy+j)+1]=F[0][i*Sx+j].im;
+      }
+    N[0]=(long) fftx.paddedSize();
+    N[1]=(long) ffty.paddedSize();
+    utils::deleteAlign(F[0]);
+    delete [] F;
+  } catch(std::exception& e) {
+    fprintf(stderr,"cpp_weighted_her2: %s\n",e.what());
+    return -1;
+  }
+  return 0;
+}

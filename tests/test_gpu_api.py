@@ -73,6 +73,10 @@ API_CASES = [
     ("real2", [H.REAL, H.PAD], [16, 12], [31, 23], "binary"),
     ("pad3", [H.PAD, H.PAD, H.PAD], [6, 5, 4], [11, 9, 7], "binary"),
     ("real3", [H.REAL, H.PAD, H.PAD], [6, 5, 4], [11, 9, 7], "binary"),
+    ("pad2s", [H.PAD, H.PAD], [16, 12], [31, 23], "binary"),
+    ("her2s", [H.CENTERED, H.HERMITIAN], [31, 31], [46, 46], "realbinary"),
+    ("pad3s", [H.PAD, H.PAD, H.PAD], [6, 5, 4], [11, 9, 7], "binary"),
+    ("real3s", [H.REAL, H.PAD, H.PAD], [6, 5, 4], [11, 9, 7], "binary"),
     ("her3", [H.CENTERED, H.CENTERED, H.HERMITIAN], [7, 7, 7], [10, 10, 10],
      "realbinary"),
 ]

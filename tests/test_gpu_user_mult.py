@@ -217,3 +217,22 @@ def test_functor_plan_misuse(user_lib):
     plan = HybridConvolution(kinds, L, mult="user")
     with pytest.raises(RuntimeError):
         plan.convolve(t, t)
+
+
+def test_functor_through_cpp_classes(user_lib):
+    """The functor as the Application multiplier of the FFTW++-compatible
+    C++ classes (include/convolve.h: Convolution2 over fftPadCentered x
+    fftPadHermitian, host arrays with an x stride beyond the stored rows)."""
+    fn = user_lib.cpp_weighted_her2
+    dp = ctypes.POINTER(ctypes.c_double)
+    fn.argtypes = [dp, dp, dp, ctypes.c_size_t, ctypes.c_size_t,
+                   ctypes.c_size_t, ctypes.POINTER(ctypes.c_long)]
+    fn.restype = ctypes.c_int
+    kinds, L = [H.CENTERED, H.HERMITIAN], [31, 31]
+    fs = _inputs(kinds, L, 2, seed=19)
+    h = np.empty_like(fs[0])
+    N = (ctypes.c_long * 2)()
+    args = [np.ascontiguousarray(a).ctypes.data_as(dp) for a in (fs[0], fs[1])]
+    assert fn(args[0], args[1], h.ctypes.data_as(dp), 31, 31, 16 + 4, N) == 0
+    want = _weighted_oracle(fs, kinds, L, [N[0], N[1]])
+    assert rel_l2(h, want) <= 1e-13
