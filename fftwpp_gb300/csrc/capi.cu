@@ -952,7 +952,7 @@ size_t fgb_pad_index(const fgb_pad *h, size_t r, size_t j)
 {
   if(!h) return 0;
   const AxisPlan& a=h->t->plan();
-  return a.kind == KIND_REAL ? j : a.q*j+r;
+  return a.kind == KIND_REAL || a.kind == KIND_HERMITIAN ? j : a.q*j+r;
 }
 
 void fgb_pad_destroy(fgb_pad *h) {delete h;}

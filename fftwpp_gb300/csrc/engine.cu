@@ -1615,9 +1615,8 @@ cudaError_t Conv::runHost(const void *const *in, void *const *out,
 PadTransform::PadTransform(int kind, long L, long M, long C, long mForce,
                            int prec) : C(C), prec(prec)
 {
-  if(kind != KIND_PAD && kind != KIND_CENTERED && kind != KIND_REAL)
-    throw std::runtime_error("standalone padded transforms take fftPad, "
-                             "fftPadCentered or fftPadReal data");
+  if(kind < KIND_PAD || kind > KIND_REAL)
+    throw std::runtime_error("unknown padded-transform kind");
   if(prec != PREC_F64 && prec != PREC_F32)
     throw std::runtime_error("standalone padded transforms run in FP64 or "
                              "FP32");
@@ -1629,15 +1628,40 @@ PadTransform::PadTransform(int kind, long L, long M, long C, long mForce,
     throw std::runtime_error("transform too large");
   a.kind=kind; a.L=L; a.M=M; a.stored=L; a.tile=a.tileB=1; a.rpc=1;
   a.rows=0;
+  if(kind == KIND_HERMITIAN) {
+    // Explicit padding to an even N: the ceil(L/2) stored modes to N real
+    // values and back (fftPadHermitian with m = N, D = 1; a forced m gives
+    // the N = m q of the reference's parameters, convolve.cc:403-410).
+    long Mh=M;
+    if(mForce > 0) {
+      size_t p,n,q;
+      refParameters(L,M,mForce,true,p,n,q);
+      Mh=std::max<long>(M,mForce*(long) q);
+    }
+    a.stored=(long) ceilquotient(L,2);
+    a.N=evenSmooth(Mh);
+    a.m=a.N; a.q=1; a.p=1; a.cshift=0;
+    a.rows=a.N;
+    const long Nh=a.N/2;
+    auto sm=[&](int t) {return FGB_BY_PREC(prec,outerRealSmem,a.N,Nh,t);};
+    if(sm(1) > SMEM_MAX)
+      throw std::runtime_error("transform too long for one CTA's shared "
+                               "memory");
+    a.tile=pickTile(wide(prec) ? 8 : 16,C,1,sm,wide(prec) ? 2 : 4);
+    a.tileB=a.tile;
+    return;
+  }
   planOuter(a,mForce,prec,C,1,1,1);
 }
 
+size_t PadTransform::inElements() const {return (size_t) a.stored*C;}
 size_t PadTransform::outElements() const {return (size_t) a.rows*C;}
 
 bool PadTransform::aligned(const void *f, const void *F) const
 {
   size_t cplx=elem(prec), data=a.kind == KIND_REAL ? cplx/2 : cplx;
-  return (size_t) f % data == 0 && (size_t) F % cplx == 0;
+  size_t trans=a.kind == KIND_HERMITIAN ? cplx/2 : cplx;
+  return (size_t) f % data == 0 && (size_t) F % trans == 0;
 }
 
 template<typename T>
@@ -1659,6 +1683,18 @@ cudaError_t PadTransform::runT(const void *in, void *out, bool fwd,
   P.in[0]=(const Cx *) in;
   P.out[0]=(Cx *) out;
   const int threads=256;
+  if(a.kind == KIND_HERMITIAN) {
+    // Forward: the H stored modes (complex side) to N reals with sign +1
+    // (the complex-to-real kernel with the complex side conjugated);
+    // backward: N reals to the H modes with sign -1 (real-to-complex,
+    // conjugated).
+    P.L=(int) a.N;
+    P.fp=fftPlan(a.N/2,prec);
+    P.conj=1;
+    P.kc=(int) a.stored;
+    return fwd ? launchOuterRealBwd<T>(P,threads,s) :
+      launchOuterRealFwd<T>(P,threads,s);
+  }
   if(a.kind == KIND_REAL)
     return fwd ? launchOuterRealFwd<T>(P,threads,s) :
       launchOuterRealBwd<T>(P,threads,s);

@@ -218,6 +218,10 @@ private:
 //       f[s][c] = sum_{r,j} F[r*m+j][c] exp(-2 pi i (s - cshift)(q j + r)/N).
 //   real kind: f is L x C real; F is (N/2+1) x C complex in natural order
 //     (row k: frequency k); backward is the matching complex-to-real sum.
+//   Hermitian kind: f is ceil(L/2) x C complex (the stored modes k >= 0,
+//     f_0 real); F is N x C real, F[t][c] = sum_{|k|<H} f_k w^{k t} with
+//     f_{-k} = conj(f_k) (fftPadHermitian's explicit forward, m = N);
+//     backward is the real-to-complex sum over t with w^{-k t}.
 // backward(forward(f)) = N f.
 class PadTransform {
 public:
@@ -227,7 +231,7 @@ public:
   const AxisPlan& plan() const {return a;}
   long columns() const {return C;}
   int precision() const {return prec;}
-  size_t inElements() const {return (size_t) a.L*C;}
+  size_t inElements() const;
   size_t outElements() const;
   // Whether f (data side) and F (transform side) meet the element
   // alignment the kernels' vector accesses need.

@@ -285,6 +285,7 @@ outerRealFwdKernel(const OuterPlan<T> P)
     int k=dTile(i), cc=i-k*tile;
     int col=col0+cc;
     if(col >= P.C) continue;
+    if(P.kc > 0 && k >= P.kc) continue;
     int k0=k == Nh ? 0 : k;
     int km=k == 0 || k == Nh ? 0 : Nh-k;
     cplx<T> zk=X[sp(k0*tile+cc)];
@@ -324,8 +325,10 @@ outerRealBwdKernel(const OuterPlan<T> P)
     int col=col0+cc;
     cplx<T> v=mk((T) 0,(T) 0);
     if(col < P.C) {
-      cplx<T> gk=src[(long long) k*P.inRow+col];
-      cplx<T> gm=src[(long long) (Nh-k)*P.inRow+col];
+      const int kc=P.kc > 0 ? P.kc : Nh+1;
+      cplx<T> gk=k < kc ? src[(long long) k*P.inRow+col] : mk((T) 0,(T) 0);
+      cplx<T> gm=Nh-k < kc ? src[(long long) (Nh-k)*P.inRow+col] :
+        mk((T) 0,(T) 0);
       if(P.conj) {
         gk=conjg(gk);
         gm=conjg(gm);

@@ -130,6 +130,8 @@ struct OuterPlan {
                            // (the sign -1 r2c / sign +1 c2r of plain FFTs)
   int cz;                  // data side with strides: column c lies at
   long long cs;            // (c / cz) cs + c % cz (cz = 0: at c)
+  int kc;                  // real kernels: complex-side rows stored (the
+                           // ceil(L/2) Hermitian modes), 0 for all N/2+1
   T scale;
   FFTPlanDev fp;           // length-m (complex) or length-N/2 (real) FFT
   const typename TwT<T>::type *twN;

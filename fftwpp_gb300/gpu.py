@@ -344,14 +344,17 @@ class BatchedConvolution:
 
 class PaddedTransform:
     """Standalone forward/backward padded transform along one axis of C
-    interleaved columns (fftPad / fftPadCentered / fftPadReal,
-    convolve.h:515-536, 623-646, 855-877), for work in padded space.
+    interleaved columns (fftPad / fftPadCentered / fftPadHermitian /
+    fftPadReal, convolve.h:515-536, 623-646, 737-757, 855-877), for work in
+    padded space.
 
     Complex kinds: f has shape (L, C) (or (L,) for C = 1); forward returns
     F of shape (N, C) whose row r*m + j is the padded DFT (sign +1) at
     transformed index q*j + r (index(r, j)); backward is the unnormalised
     adjoint, so backward(forward(f)) = N f.  Real kind: f real (L, C), F
-    complex (N/2 + 1, C) in natural frequency order.
+    complex (N/2 + 1, C) in natural frequency order.  Hermitian kind: f
+    complex (ceil(L/2), C), the stored modes k >= 0; F real (N, C), the
+    physical values at grid points 0..N-1 (explicit padding, N even).
     """
 
     def __init__(self, kind: int, L: int, M: int | None = None, *, C: int = 1,
@@ -374,10 +377,15 @@ class PaddedTransform:
         self.lib.fgb_pad_info(self.handle, info)
         (self.m, self.p, self.q, self.N, _, _, self.rows,
          self.cshift) = list(info)[:8]
+        # Entries stored on the data side (ceil(L/2) Hermitian modes).
+        self.stored = (self.L + 1) // 2 if kind == HERMITIAN else self.L
 
     @property
     def cdtype(self):
+        """Element type of the transformed side F."""
         import torch
+        if self.kind == HERMITIAN:
+            return torch.float64 if self.prec == F64 else torch.float32
         return torch.complex128 if self.prec == F64 else torch.complex64
 
     @property
@@ -386,7 +394,7 @@ class PaddedTransform:
         import torch
         if self.kind == REAL:
             return torch.float64 if self.prec == F64 else torch.float32
-        return self.cdtype
+        return torch.complex128 if self.prec == F64 else torch.complex64
 
     def index(self, r: int, j: int) -> int:
         return self.lib.fgb_pad_index(self.handle, r, j)
@@ -399,7 +407,7 @@ class PaddedTransform:
 
     def forward(self, f, out=None, stream=None):
         import torch
-        self._check(f, self.L, self.idtype, "f")
+        self._check(f, self.stored, self.idtype, "f")
         if out is None:
             out = torch.empty((self.rows, self.C), dtype=self.cdtype,
                               device=f.device)
@@ -416,9 +424,9 @@ class PaddedTransform:
         import torch
         self._check(F, self.rows, self.cdtype, "F")
         if out is None:
-            out = torch.empty((self.L, self.C), dtype=self.idtype,
+            out = torch.empty((self.stored, self.C), dtype=self.idtype,
                               device=F.device)
-        self._check(out, self.L, self.idtype, "out")
+        self._check(out, self.stored, self.idtype, "out")
         s = stream if stream is not None else torch.cuda.current_stream()
         rc = self.lib.fgb_pad_backward_device(
             self.handle, ctypes.c_void_p(F.data_ptr()),

@@ -231,10 +231,13 @@ int fgb_batch_block_problem(fgb_batch *b, int i, int blocked);
  *   q*j + r, measured from the centred origin floor(L/2) for
  *   FGB_CENTERED.  Real kind: f is L x C real, F is (N/2+1) x C
  *   complex in natural frequency order (fgb_pad_index(0, k) = k).
+ *   Hermitian kind (fftPadHermitian, convolve.h:737-757; tests/hybridh.cc):
+ *   f is ceil(L/2) x C complex (the stored modes k >= 0, f_0 real), F is
+ *   N x C real, the physical values at grid points t = 0..N-1 of the
+ *   Hermitian-extended spectrum (explicit padding to an even N, as
+ *   fftPadHermitian with m = N, D = 1; fgb_pad_index(0, t) = t).
  * backward is the unnormalised adjoint (sign -1) accumulated over residues,
- * so backward(forward(f)) = N f.  Device pointers, asynchronous on stream.
- * The Hermitian kind (fftPadHermitian) is fused into the convolution's row
- * kernel and has no standalone form. */
+ * so backward(forward(f)) = N f.  Device pointers, asynchronous on stream. */
 typedef struct fgb_pad fgb_pad;
 fgb_pad *fgb_pad_create(int kind, size_t L, size_t M, size_t C, size_t m,
                         int precision);

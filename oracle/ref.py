@@ -38,6 +38,10 @@ def lib():
         _lib.ref_forward_layout.argtypes = [
             ctypes.c_int, sz, sz, sz, sz, ctypes.c_long,
             P(ctypes.c_double), P(ctypes.c_double), P(sz), sz, P(sz)]
+        _lib.ref_forward_layout_hermitian.restype = ctypes.c_long
+        _lib.ref_forward_layout_hermitian.argtypes = [
+            sz, sz, sz, sz, ctypes.c_long,
+            P(ctypes.c_double), P(ctypes.c_double), P(sz), sz, P(sz)]
         _lib.ref_parameters.argtypes = [sz, sz, sz, ctypes.c_int, P(sz), P(sz),
                                         P(sz)]
         _lib.ref_nextfftsize.restype = sz
@@ -100,6 +104,24 @@ def forward_layout(kind, L, M, m=0, D=0, I=-1, f=None):
         kind, L, M, m, D, I, f.view(np.float64).ctypes.data_as(
             ctypes.POINTER(ctypes.c_double)),
         F.view(np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+        idx.ctypes.data_as(ctypes.POINTER(ctypes.c_size_t)), cap, info)
+    if n < 0 or n > cap:
+        return None
+    return F[:n].copy(), idx[:n].astype(np.int64), tuple(int(x) for x in info)
+
+
+def forward_layout_hermitian(L, M, m=0, D=0, I=-1, f=None):
+    """Forward real blocks of a 1D fftPadHermitian and their transformed
+    indices (tests/hybridh.cc:74-99); f holds the ceil(L/2) stored modes."""
+    f = np.ascontiguousarray(f, dtype=np.complex128)
+    cap = 8 * M + 64
+    F = np.zeros(cap, dtype=np.float64)
+    idx = np.zeros(cap, dtype=np.uintp)
+    info = (ctypes.c_size_t * 8)()
+    n = lib().ref_forward_layout_hermitian(
+        L, M, m, D, I, f.view(np.float64).ctypes.data_as(
+            ctypes.POINTER(ctypes.c_double)),
+        F.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
         idx.ctypes.data_as(ctypes.POINTER(ctypes.c_size_t)), cap, info)
     if n < 0 or n > cap:
         return None

@@ -226,6 +226,51 @@ long ref_forward_layout(int kind, size_t L, size_t M, size_t m, size_t D,
   return (long) total;
 }
 
+// Forward layout of a 1D fftPadHermitian (the loop of tests/hybridh.cc:
+// 74-99, C = 1): for every residue r and copy d < D, the noutputs(r) real
+// values of block d and their transformed indices.  out_F receives `total`
+// doubles.  Returns total (or -1 on error).
+long ref_forward_layout_hermitian(size_t L, size_t M, size_t m, size_t D,
+                                  long I, const double *in, double *out_F,
+                                  size_t *out_index, size_t capacity,
+                                  size_t *info)
+{
+  Application app(1,1,multNone,1,false,m,D,I);
+  fftPadHermitian *fft=new fftPadHermitian(L,M,app,1);
+  report(fft,info);
+  size_t H=ceilquotient(L,2);
+  Complex *f=ComplexAlign(H);
+  Complex *F=ComplexAlign(fft->outputSize());
+  size_t wsize=fft->workSizeW();
+  Complex *W0=wsize ? ComplexAlign(wsize) : NULL;
+  memcpy((double *) f,in,2*H*sizeof(double));
+  fft->pad(W0);
+  size_t total=0;
+  size_t stride=fft->noutputs(0);
+  for(size_t r=0; r < fft->R; r += fft->increment(r)) {
+    fft->forward(f,F,r,W0);
+    size_t D1=r == 0 ? fft->D0 : fft->D;
+    for(size_t d=0; d < D1; ++d) {
+      double *Fr=(double *) (F+fft->b*d);
+      for(size_t k=0; k < stride; ++k) {
+        if(total >= capacity) {total=capacity+1; break;}
+        out_F[total]=Fr[k];
+        out_index[total]=fft->index(r,k+stride*d);
+        ++total;
+      }
+    }
+  }
+  if(info) {
+    info[6]=fft->R;
+    info[7]=fft->M;
+  }
+  if(W0) deleteAlign(W0);
+  deleteAlign(F);
+  deleteAlign(f);
+  delete fft;
+  return (long) total;
+}
+
 // The reference's parameter rule (convolve.cc:403-410) for direct testing.
 void ref_parameters(size_t L, size_t M, size_t m, int centered,
                     size_t *p, size_t *n, size_t *q)

@@ -50,7 +50,7 @@ int main(int argc, char **argv)
   // Strided cases: the dense input rows (of `run` doubles) are laid out
   // with `pitch` doubles between consecutive rows of the innermost axis
   // (3D: `plane` doubles between planes of axis 0).
-  bool strided=c.size() == 5 && c[4] == 's';
+  bool strided=c.size() > 4 && c.back() == 's';
   size_t run=words, pitch=words, plane=words, rows=1, planes=1, Sx=0, Sy=0;
   if(strided) {
     size_t w=c.substr(0,3) == "rea" ? 1 : 2;      // doubles per element

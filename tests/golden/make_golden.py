@@ -13,7 +13,9 @@ linked against the clean-room FFTW3 backend) on:
   every forward/backward routine family is exercised;
 * seeded uniform/normal inputs;
 * the analytic known-answer case of tests/hybridconv.cc:50-69;
-* forward residue layouts and transformed indices (tests/hybrid.cc:69-105);
+* forward residue layouts and transformed indices (tests/hybrid.cc:69-105),
+  and the real forward blocks of fftPadHermitian with theirs
+  (tests/hybridh.cc:74-99; `--only hlayouts` regenerates just these);
 * the parameter rule and nextfftsize over a grid.
 
 Usage (in a checkout where the reference and oracle/_ref exist):
@@ -295,5 +297,41 @@ def main():
           f"{len(par)} parameter rows")
 
 
+def hermitian_layouts():
+    """Forward blocks of a 1D fftPadHermitian (real values at transformed
+    indices) for explicit and hybrid plans; the inputs are the reference
+    test's (tests/hybridh.cc:58-62: f_0 = 1, f_j = (j+1) + i (j+2))."""
+    lay = {}
+    meta = []
+    k = 0
+    for (L, M) in ((15, 22), (16, 24), (31, 46), (63, 94), (20, 30),
+                   (511, 766)):
+        H = (L + 1) // 2
+        f = (np.arange(H) + 1) + 1j * (np.arange(H) + 2)
+        f[0] = 1
+        for m in (0, M, (M + 2) // 2 * 2, 8, 4, 16, 32):
+            for D in (0, 1, 2):
+                r = ref.forward_layout_hermitian(L, M, m, D, -1, f)
+                if r is None:
+                    continue
+                F, idx, info = r
+                key = f"h{k:04d}"
+                lay[key + "_F"] = F
+                lay[key + "_idx"] = idx
+                lay[key + "_info"] = np.array(info, dtype=np.int64)
+                meta.append((key, L, M, m, D))
+                k += 1
+    np.savez_compressed(os.path.join(HERE, "hlayouts.npz"), **lay)
+    with open(os.path.join(HERE, "hlayouts.txt"), "w") as fh:
+        fh.write("# key L M m D   (info: m p q n D I R N)\n")
+        for row in meta:
+            fh.write(" ".join(map(str, row)) + "\n")
+    return k
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--only", "hlayouts"]:
+        print(f"{hermitian_layouts()} Hermitian layouts")
+    else:
+        main()
+        print(f"{hermitian_layouts()} Hermitian layouts")

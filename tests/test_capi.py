@@ -141,8 +141,17 @@ def test_padded_transform_plans(native_lib):
                 assert lib.fgb_pad_index(h, 1, 5) == q * 5 + 1
         finally:
             lib.fgb_pad_destroy(h)
-    assert not lib.fgb_pad_create(2, 16, 24, 1, 0, 0)
-    assert "fftPadReal" in _native.last_error()
+    h = lib.fgb_pad_create(2, 15, 22, 3, 0, 0)     # fftPadHermitian
+    assert h, _native.last_error()
+    try:
+        assert lib.fgb_pad_info(h, info) == 0
+        mm, p, q, N, LL, CC, rows, c = list(info)[:8]
+        assert (q, N % 2, rows, mm) == (1, 0, N, N) and N >= 22
+        assert lib.fgb_pad_index(h, 0, 7) == 7
+    finally:
+        lib.fgb_pad_destroy(h)
+    assert not lib.fgb_pad_create(7, 16, 24, 1, 0, 0)
+    assert "kind" in _native.last_error()
     assert not lib.fgb_pad_create(0, 16, 8, 1, 0, 0)
     assert "greater than M" in _native.last_error()
 

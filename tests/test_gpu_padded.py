@@ -139,3 +139,61 @@ def test_rejects_bad_tensors(native_lib):
         t.forward(torch.zeros(16, 3, dtype=torch.complex128, device="cuda"))
     with pytest.raises(ValueError):
         t.forward(torch.zeros(16, 2, dtype=torch.complex64, device="cuda"))
+
+
+def _hermitian_layouts():
+    data = np.load(os.path.join(GOLD, "hlayouts.npz"))
+    for line in open(os.path.join(GOLD, "hlayouts.txt")):
+        if line.startswith("#"):
+            continue
+        key, L, M, m, D = line.split()
+        yield (key, int(L), int(M), int(m), data[key + "_F"],
+               data[key + "_idx"], data[key + "_info"])
+
+
+def test_hermitian_forward_matches_reference_layouts(native_lib):
+    """The standalone Hermitian transform against every real value the
+    reference's fftPadHermitian forward produced (tests/hybridh.cc:74-99,
+    explicit and hybrid plans), looked up by transformed index, wherever the
+    reference's padded length N is even with N/2 a product of 2, 3, 5, 7
+    (the GPU's explicit grid is then the same)."""
+    import torch
+    from fftwpp_gb300.gpu import PaddedTransform
+    checked = 0
+    for key, L, M, m, F, idx, info in _hermitian_layouts():
+        N = int(info[7])
+        if N % 2 or not _smooth(N // 2):
+            continue
+        t = PaddedTransform(H.HERMITIAN, L, N)
+        assert t.N == N, key
+        Hm = (L + 1) // 2
+        f = (np.arange(Hm) + 1) + 1j * (np.arange(Hm) + 2)
+        f[0] = 1
+        got = t.forward(torch.from_numpy(f).cuda()).cpu().numpy()[:, 0]
+        assert rel_l2(got[idx], F) <= 1e-13, key
+        assert t.index(0, int(idx[3])) == int(idx[3])
+        checked += 1
+    assert checked >= 60
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-13), ("f32", 2e-6)])
+@pytest.mark.parametrize("L,M,C,m", [(15, 22, 1, 0), (63, 94, 5, 0),
+                                     (1023, 1534, 3, 0), (31, 46, 2, 8)])
+def test_hermitian_forward_backward(native_lib, L, M, C, m, precision, tol):
+    """Forward against the explicit oracle on C interleaved columns;
+    backward(forward(f)) = N f."""
+    import torch
+    from fftwpp_gb300.gpu import PaddedTransform
+    from oracle import explicit as E
+    t = PaddedTransform(H.HERMITIAN, L, M, C=C, m=m, precision=precision)
+    assert t.N % 2 == 0 and t.N >= M
+    Hm = (L + 1) // 2
+    rng = np.random.default_rng(L + C)
+    f = rng.uniform(-1, 1, (Hm, C)) + 1j * rng.uniform(-1, 1, (Hm, C))
+    f[0] = f[0].real
+    tf = torch.from_numpy(f).to(t.idtype).cuda()
+    F = t.forward(tf)
+    want = E._forward(f.T, E.HERMITIAN, L, t.N, 1).T
+    assert rel_l2(F.cpu().numpy().astype(np.float64), want) <= tol
+    back = t.backward(F).cpu().numpy().astype(np.complex128)
+    assert rel_l2(back, t.N * f) <= tol

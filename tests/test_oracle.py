@@ -260,3 +260,32 @@ def test_explicit_oracle_matches_hybrid(case):
         got = E.convolve(fs, kinds, L, Ns, lambda v, ix: [v[0] * v[1]])[0]
         err = Dr.rel_l2(got, want)
         assert err <= 1e-13, (Ns, err)
+
+
+def hermitian_layouts():
+    data = np.load(os.path.join(GOLD, "hlayouts.npz"))
+    for line in open(os.path.join(GOLD, "hlayouts.txt")):
+        if line.startswith("#"):
+            continue
+        key, L, M, m, D = line.split()
+        yield (key, int(L), int(M), int(m), int(D), data[key + "_F"],
+               data[key + "_idx"], data[key + "_info"])
+
+
+def test_hermitian_layouts_pin_explicit_oracle():
+    """Every real value the reference's fftPadHermitian forward produced
+    (tests/hybridh.cc:74-99, explicit and hybrid plans) equals the explicit
+    oracle's complex-to-real transform at its transformed index."""
+    from oracle import explicit as E
+    n = 0
+    for key, L, M, m, D, F, idx, info in hermitian_layouts():
+        N = int(info[7])
+        H_ = (L + 1) // 2
+        f = (np.arange(H_) + 1) + 1j * (np.arange(H_) + 2)
+        f[0] = 1
+        u = E._forward(f, E.HERMITIAN, L, N, 0)
+        assert len(set(idx.tolist())) == len(idx) <= N, key
+        np.testing.assert_allclose(F, u[idx], rtol=0,
+                                   atol=1e-12 * np.abs(u).max(), err_msg=key)
+        n += 1
+    assert n >= 100
