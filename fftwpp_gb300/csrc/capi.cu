@@ -670,6 +670,8 @@ int fgb_convolve_host(fgb_conv *c, void *const *in, void *const *out)
   return 0;
 }
 
+void fgb_set_ff_range_guard(int on) {Conv::setRangeGuard(on != 0);}
+
 int fgb_set_strides(fgb_conv *c, const size_t *stride)
 {
   if(!c) {report("fgb_set_strides","bad arguments"); return -1;}

@@ -422,8 +422,8 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
 Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
            const long *mForce, int A, int B, int mult, int prec, long batch,
            bool tuneSchedule)
-  : batch(batch), user(NULL), isStrided(false), tuning(false), staging(0),
-    hostIn(NULL),
+  : batch(batch), user(NULL), isStrided(false), ffState(NULL),
+    tuning(false), staging(0), hostIn(NULL),
     hostOut(NULL), nlaunch(0),
     timing(false), normalize(true), marks(0), hostTile(0), hostThr(0),
     hostTileB(0), hostThrB(0), side(NULL), chunks(0)
@@ -540,9 +540,14 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
     // A throwing constructor runs no destructor: release what was taken.
     for(void *p : bufs) cudaFree(p);
     bufs.clear();
+    if(ffState) cudaFree(ffState);
+    ffState=NULL;
     throw;
   }
 }
+
+bool Conv::rangeGuard=true;
+void Conv::setRangeGuard(bool on) {rangeGuard=on;}
 
 bool Conv::autotune=true;
 void Conv::setAutotune(bool on) {autotune=on;}
@@ -810,6 +815,7 @@ Conv::~Conv()
   for(void *p : bufs) cudaFree(p);
   if(hostIn) cudaFree(hostIn);
   if(hostOut) cudaFree(hostOut);
+  if(ffState) cudaFree(ffState);
 }
 
 size_t Conv::elemBytes() const   // user-facing element (FP64 in ff mode)
@@ -861,6 +867,14 @@ void Conv::allocate()
 {
   size_t e=elem(I.prec);
   int A=I.A;
+  if(I.prec == PREC_FF) {
+    if(devAlloc((void **) &ffState,32*sizeof(int)) != cudaSuccess ||
+       cudaMemset(ffState,0,32*sizeof(int)) != cudaSuccess) {
+      ffState=NULL;
+      throw std::runtime_error("device allocation of the range guard's "
+                               "state failed");
+    }
+  }
   auto get=[&](size_t bytes) {
     void *p=NULL;
     if(devAlloc((void **) &p,bytes) != cudaSuccess)
@@ -930,6 +944,23 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   double scale=1.0;
   if(normalize)
     for(int d=0; d < I.dim; ++d) scale /= (double) I.axis[d].N;
+  // Float-float mode: the first launch reads the caller's FP64 arrays and
+  // the last one writes them, scaled by the range guard's exponents, which
+  // a scan of the inputs sets first (its time counts with the first
+  // launch's).
+  const int IN64=std::is_same<T,ff>::value ? 1 : 0, OUT64=2*IN64;
+  const int *guard=NULL;
+  if(IN64 && rangeGuard && ffState && I.mult != MULT_USER) {
+    FFScaleArgs G;
+    for(int a=0; a < A; ++a) G.in[a]=(const unsigned long long *) in[a];
+    G.count=A; G.B=B; G.mult=I.mult;
+    G.n=(long long) (elements()*(I.axis[0].kind == KIND_REAL ? 1 : 2));
+    G.state=ffState;
+    if(isStrided) G.n=(long long) (spanElements()*
+                                   (I.axis[0].kind == KIND_REAL ? 1 : 2));
+    if((e=launchFFScale(G,s)) != cudaSuccess) return e;
+    guard=ffState+16;
+  }
   // Slot positions for position-dependent (caller's) multipliers.
   IndexMap im;
   std::memset(&im,0,sizeof(im));
@@ -953,6 +984,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   }
   auto rowPlan=[&](RowPlan<T>& P, const AxisPlan& a) {
     P.im=im;
+    P.ioShift=guard;
     P.L=(int) a.stored; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
     P.cshift=a.cshift; P.A=A; P.B=B; P.mult=I.mult;
     P.realIO=a.kind == KIND_REAL && I.dim == 1;
@@ -964,6 +996,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   };
   auto hermPlan=[&](HermRowPlan<T>& P, const AxisPlan& a) {
     P.im=im;
+    P.ioShift=guard;
     P.H=(int) a.stored; P.N=(int) a.N; P.Nh=(int) (a.N/2);
     P.A=A; P.B=B; P.mult=I.mult;
     P.rpc=a.rpc;
@@ -972,6 +1005,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };
   auto outerPlan=[&](OuterPlan<T>& P, const AxisPlan& a) {
+    P.ioShift=guard;
     P.L=(int) a.L; P.m=(int) a.m; P.q=(int) a.q; P.N=(int) a.N;
     P.cshift=a.cshift; P.tile=a.tile;
     P.io64=0;
@@ -981,9 +1015,6 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
     P.twX=NULL; P.NX=1;
   };
-  // Float-float mode: the first launch reads the caller's FP64 arrays and
-  // the last one writes them.
-  const int IN64=std::is_same<T,ff>::value ? 1 : 0, OUT64=2*IN64;
   // The first outer-axis launch.  While a host call copies the inputs in
   // (chunks > 0): input 0 one launch per column range, each on its own
   // stream after its range has landed, and every other input one launch
@@ -1065,6 +1096,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.io64=0;
     O.inplace=0;
     O.conj=0;
+    O.ioShift=guard;
     O.count=A; O.nbatch=1; O.inBatch=O.outBatch=0;
     O.inRow=m; O.outRow=m; O.C=(int) m; O.Ltot=a.L;
     O.scale=(T) 1;
@@ -1411,7 +1443,10 @@ cudaError_t Conv::runZeroCopy(const void *const *hin, const void *const *in,
   cudaError_t e;
   // With an outer axis, the inputs are copied on a side stream and the
   // first transform of each piece starts as soon as it has arrived.
-  const bool pipeline=copyIn && I.dim > 1 && !I.longRow;
+  // (Float-float plans scan all inputs before the first transform, so
+  // their inputs arrive whole.)
+  const bool pipeline=copyIn && I.dim > 1 && !I.longRow &&
+    !(I.prec == PREC_FF && rangeGuard);
   if(pipeline) {
     std::vector<void *> dev(A);
     for(int a=0; a < A; ++a) dev[a]=(void *) src[a];

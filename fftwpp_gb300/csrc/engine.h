@@ -134,6 +134,12 @@ public:
   // Normalise by 1/prod(N) (Convolution::convolve) or not (convolveRaw).
   void setNormalize(bool on) {normalize=on;}
 
+  // Range guard of the float-float mode, process-wide (default on): each
+  // convolution first scans its FP64 inputs for their largest exponents and
+  // scales inputs and outputs by exact powers of two (launchFFScale), so
+  // FP64 data of any magnitude fit the float exponent range.
+  static void setRangeGuard(bool on);
+
   // Plan-time autotuning (the GPU counterpart of FFTW++'s optimiser,
   // convolve.cc:177-470): rows per CTA of the innermost-axis kernel and the
   // column tiles of the outer-axis kernels are chosen by timing every
@@ -148,6 +154,8 @@ private:
   const RowLaunchers *user;        // row launches of a MULT_USER plan
   bool isStrided;
   long strideS[3];                 // outer-axis strides (setStrides)
+  int *ffState;                    // float-float range guard (32 ints)
+  static bool rangeGuard;
   cudaError_t runHostStrided(const void *const *in, void *const *out,
                              cudaStream_t s);
   bool tuning;                     // inside tune(): MULT_USER runs without

@@ -65,7 +65,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
         int s=posmod(t+c,m);
         long long off=(long long) s*P.inRow+dataCol(P,col);
         if(s < L && col < P.C && off < P.Ltot) {
-          if(P.io64 & 1) convertStaged(x,sp(i));
+          if(P.io64 & 1) convertStaged(x,sp(i),ioShift<T>(P.ioShift,a));
           if(r != 0) x[sp(i)]=twmul<1>(x[sp(i)],tw[twExp(s,c,r,N)]);
         }
       }
@@ -89,7 +89,8 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
         int s=dTile(i), cc=i-s*tile;
         int col=col0+cc;
         long long off=(long long) s*P.inRow+dataCol(P,col);
-        if(col < P.C && off < P.Ltot) convertStaged(y,i);
+        if(col < P.C && off < P.Ltot)
+          convertStaged(y,i,ioShift<T>(P.ioShift,a));
       }
     }
     __syncthreads();
@@ -214,7 +215,8 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
         int col=col0+cc;
         long long off=(long long) s*P.outRow+dataCol(P,col);
         if(col < P.C && off < P.Ltot)
-          storeIO(dst+off,X[sp(posmod(s-c,m)*tile+cc)]*P.scale,P.io64 & 2);
+          storeIO(dst+off,X[sp(posmod(s-c,m)*tile+cc)]*P.scale,P.io64 & 2,
+                  ioShift<T>(P.ioShift,8+b));
       }
       __syncthreads();
       return;
@@ -232,7 +234,8 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
     int s=dTile(i), cc=i-s*tile;
     int col=col0+cc;
     long long off=(long long) s*P.outRow+dataCol(P,col);
-    if(col < P.C && off < P.Ltot) storeIO(dst+off,acc[i]*P.scale,P.io64 & 2);
+    if(col < P.C && off < P.Ltot)
+      storeIO(dst+off,acc[i]*P.scale,P.io64 & 2,ioShift<T>(P.ioShift,8+b));
   }
   __syncthreads();
 }
@@ -274,8 +277,9 @@ outerRealFwdKernel(const OuterPlan<T> P)
     if(col < P.C) {
       int s=2*t;
       const long long dc=dataCol(P,col);
-      if(s < L) re=loadIOr(src+(long long) s*P.inRow+dc,P.io64 & 1);
-      if(s+1 < L) im=loadIOr(src+(long long) (s+1)*P.inRow+dc,P.io64 & 1);
+      const int sh=ioShift<T>(P.ioShift,a);
+      if(s < L) re=loadIOr(src+(long long) s*P.inRow+dc,P.io64 & 1,sh);
+      if(s+1 < L) im=loadIOr(src+(long long) (s+1)*P.inRow+dc,P.io64 & 1,sh);
     }
     x[sp(i)]=mk(re,im);
   }
@@ -351,8 +355,9 @@ outerRealBwdKernel(const OuterPlan<T> P)
     cplx<T> v=X[sp(i)]*P.scale;
     int s=2*t;
     const long long dc=dataCol(P,col);
-    if(s < L) storeIOr(dst+(long long) s*P.outRow+dc,v.x,P.io64 & 2);
-    if(s+1 < L) storeIOr(dst+(long long) (s+1)*P.outRow+dc,v.y,P.io64 & 2);
+    const int sh=ioShift<T>(P.ioShift,8+b);
+    if(s < L) storeIOr(dst+(long long) s*P.outRow+dc,v.x,P.io64 & 2,sh);
+    if(s+1 < L) storeIOr(dst+(long long) (s+1)*P.outRow+dc,v.y,P.io64 & 2,sh);
   }
 }
 
@@ -663,6 +668,93 @@ __global__ void __launch_bounds__(256) bulkCopyKernel(CopyArgs P)
     }
     for(; i < n; i += stride) dst[i]=src[i];
   }
+}
+
+// Float-float range guard (kernels.cuh, FFScaleArgs).  Every block takes
+// the largest biased exponent of its share of each array (integer work on
+// the bit patterns, no FP64 pipe; infinities and NaNs ignored) into
+// state[a]; the last block to finish (a wrapping counter in state[8])
+// turns them into the scales and zeroes the accumulators.  Multipliers
+// whose every output is one product of two inputs (or one input) take a
+// scale per input, and the output scale is the sum (binary, correlation,
+// the Jacobian adjoint).  Those whose outputs add products take one scale
+// per factor group so that every term scales alike: the Jacobian
+// u0 u3 - u1 u2 shares a scale between u0 and u1 and one between u2 and u3
+// (the derivatives of psi and of omega), a dot product sum_k u_k u_{K+k}
+// one per half.  A caller's functor gets no scaling.
+__global__ void __launch_bounds__(256) ffScaleKernel(const FFScaleArgs P)
+{
+  __shared__ bool last;
+  const long long stride=(long long) gridDim.x*blockDim.x;
+  for(int a=0; a < P.count; ++a) {
+    unsigned m=0;
+    for(long long i=blockIdx.x*(long long) blockDim.x+threadIdx.x; i < P.n;
+        i += stride) {
+      const unsigned e=(unsigned) ((__ldg(P.in[a]+i) >> 52) & 0x7ff);
+      if(e != 0x7ff && e > m) m=e;
+    }
+    m=__reduce_max_sync(0xffffffffu,m);
+    if((threadIdx.x & 31) == 0 && m) atomicMax((unsigned *) P.state+a,m);
+  }
+  __threadfence();
+  __syncthreads();
+  if(threadIdx.x == 0)
+    last=atomicInc((unsigned *) P.state+8,gridDim.x-1) == gridDim.x-1;
+  __syncthreads();
+  if(!last || threadIdx.x != 0) return;
+  __threadfence();
+  int sh[FGB_MAXA];
+  for(int a=0; a < P.count; ++a) {
+    const unsigned m=atomicExch((unsigned *) P.state+a,0u);
+    sh[a]=m ? (int) m-1023 : 0;
+  }
+  int in[FGB_MAXA], out[FGB_MAXA];
+  const bool user=P.mult == MULT_USER;
+  for(int a=0; a < P.count; ++a) in[a]=user ? 0 : sh[a];
+  if(P.mult == MULT_REALJACOBIAN || P.mult == MULT_JACOBIAN) {
+    in[0]=in[1]=max(sh[0],sh[1]);
+    in[2]=in[3]=max(sh[2],sh[3]);
+  } else if(P.mult == MULT_DOT || P.mult == MULT_REALDOT) {
+    const int K=P.count/2;
+    int t1=sh[0], t2=sh[K];
+    for(int k=1; k < K; ++k) {
+      t1=max(t1,sh[k]);
+      t2=max(t2,sh[K+k]);
+    }
+    for(int k=0; k < K; ++k) {
+      in[k]=t1;
+      in[K+k]=t2;
+    }
+  }
+  for(int b=0; b < P.B; ++b) out[b]=in[b];
+  switch(P.mult) {
+    case MULT_BINARY: case MULT_REALBINARY: case MULT_CORRELATION:
+    case MULT_REALJACOBIAN: case MULT_JACOBIAN:
+      out[0]=in[0]+in[P.mult == MULT_REALJACOBIAN ||
+                     P.mult == MULT_JACOBIAN ? 3 : 1];
+      break;
+    case MULT_DOT: case MULT_REALDOT:
+      out[0]=in[0]+in[P.count/2];
+      break;
+    case MULT_REALJACADJ:
+      for(int b=0; b < 4; ++b) out[b]=in[4]+in[3-b];
+      break;
+    default:
+      break;
+  }
+  for(int a=0; a < FGB_MAXA; ++a) {
+    P.state[16+a]=a < P.count ? in[a] : 0;
+    P.state[24+a]=a < P.B ? out[a] : 0;
+  }
+}
+
+cudaError_t launchFFScale(const FFScaleArgs& P, cudaStream_t s)
+{
+  if(P.count < 1 || P.count > FGB_MAXA || P.n < 1) return cudaErrorInvalidValue;
+  long long blocks=(P.n+255)/256;
+  const int grid=(int) std::min<long long>(blocks,152*4);
+  ffScaleKernel<<<grid,256,0,s>>>(P);
+  return cudaGetLastError();
 }
 
 cudaError_t launchBulkCopy(const CopyArgs& P, cudaStream_t s)

@@ -86,6 +86,8 @@ struct RowPlan {
                            // load straight into the transform buffer and
                            // store straight from it (no staging, no
                            // accumulator)
+  const int *ioShift;      // float-float range guard: device exponents,
+                           // [a] input a, [8+b] output b (NULL: none)
   T scale;
   FFTPlanDev fp;           // length-m complex FFT
   const typename TwT<T>::type *twN;   // W_N^t, t < N
@@ -103,6 +105,7 @@ struct HermRowPlan {
   int A, B, mult;
   int rpc;                 // rows per CTA
   int io64;                // as RowPlan::io64
+  const int *ioShift;      // as RowPlan::ioShift
   T scale;
   FFTPlanDev fp;           // length-Nh complex FFT
   const typename TwT<T>::type *twN;   // W_N^t, t < N
@@ -123,6 +126,7 @@ struct OuterPlan {
   int L, m, q, N, cshift;
   int tile;
   int io64;                // as RowPlan::io64
+  const int *ioShift;      // as RowPlan::ioShift
   int inplace;             // FP32-pipe modes with L <= m and no twX: fold
                            // from memory and transform in place, rows of
                            // a residue block in digit-reversed order
@@ -203,6 +207,20 @@ template<typename T> cudaError_t launchOuterRealFwd(const OuterPlan<T>& P,
 template<typename T> cudaError_t launchOuterRealBwd(const OuterPlan<T>& P,
                                                     int threads,
                                                     cudaStream_t s);
+
+// Range guard of the float-float mode: the largest exponent of each of the
+// `count` FP64 input arrays (n doubles each) gives the power-of-two scale
+// of its values on the way in and, by the multiplier's algebra, of every
+// output on the way out; written to state[16+a] and state[24+b] (state:
+// 32 ints, zero before the first launch; the launch leaves its
+// accumulators zeroed again).
+struct FFScaleArgs {
+  const unsigned long long *in[FGB_MAXA];
+  int count, B, mult;
+  long long n;
+  int *state;
+};
+cudaError_t launchFFScale(const FFScaleArgs& P, cudaStream_t s);
 
 // Copy `count` arrays of `bytes` bytes each (16-byte aligned, a multiple of
 // 16) with the SMs.

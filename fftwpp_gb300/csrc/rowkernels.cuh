@@ -285,14 +285,24 @@ __device__ __forceinline__ void mulHermSlot(const Mul& mul,
 // leading 24 significand bits of x, lo the float nearest to the remaining
 // 29, so hi + lo = x to 2^-48 relative; values outside [2^-70, 2^101)
 // (zero, subnormals, huge values) take the FP64 conversion.
+//
+// Range guard: FP64 data span exponents far beyond a float's, so every
+// input array a is scaled by an exact power of two 2^-sh[a] on the way in
+// (its largest magnitude then lies in [1, 2)) and every output b by
+// 2^sh[8+b] on the way out (ffScaleKernel in kernels.cu chooses them from
+// the data and the multiplier).  Scaling by a power of two only moves the
+// exponent, so it costs no accuracy.
 
-__device__ __forceinline__ ff toFF(double x)
+__device__ __forceinline__ ff toFF(double x, int sh=0)
 {
   unsigned long long b=(unsigned long long) __double_as_longlong(x);
-  int e=(int) ((b >> 52) & 0x7ff)-1023;
-  if(e < -70 || e > 100) {          // keep 2^(e-52) a normal float
-    float h=__double2float_rn(x);
-    return ff(h,__double2float_rn(x-(double) h));
+  const int ef=(int) ((b >> 52) & 0x7ff);
+  const int e=ef-1023-sh;
+  if(ef == 0 || ef == 0x7ff || e < -70 || e > 100) {
+    // keep 2^(e-52) a normal float: the FP64 conversion
+    const double xs=sh ? scalbn(x,-sh) : x;
+    float h=__double2float_rn(xs);
+    return ff(h,__double2float_rn(xs-(double) h));
   }
   unsigned sign=(unsigned) (b >> 32) & 0x80000000u;
   float hi=__uint_as_float(sign | ((unsigned) (e+127) << 23) |
@@ -309,51 +319,64 @@ __device__ __forceinline__ ff toFF(double x)
   return ffFast(hi,lo);
 }
 
-// A float widened to double exactly by moving its fields (the FP64 pipe
-// only for subnormals, infinities and NaNs).
-__device__ __forceinline__ double widen(float f)
+// f 2^sh widened to double exactly by moving its fields (the FP64 pipe only
+// for subnormals, infinities, NaNs and results outside the double range).
+__device__ __forceinline__ double widen(float f, int sh=0)
 {
   unsigned u=__float_as_uint(f);
   unsigned ef=(u >> 23) & 0xffu;
   unsigned long long sign=(unsigned long long) (u & 0x80000000u) << 32;
   if((u & 0x7fffffffu) == 0) return __longlong_as_double((long long) sign);
-  if(ef == 0 || ef == 255) return (double) f;
+  const int E=(int) ef+896+sh;
+  if(ef == 0 || ef == 255 || E <= 0 || E >= 2047)
+    return sh ? scalbn((double) f,sh) : (double) f;
   return __longlong_as_double((long long) (sign |
-    ((unsigned long long) (ef+896) << 52) |
+    ((unsigned long long) E << 52) |
     ((unsigned long long) (u & 0x7fffffu) << 29)));
 }
 
-__device__ __forceinline__ double fromFF(ff v)
+__device__ __forceinline__ double fromFF(ff v, int sh=0)
 {
-  return widen(v.hi)+widen(v.lo);
+  return widen(v.hi,sh)+widen(v.lo,sh);
+}
+
+// The range-guard exponent of input a (io < 8) or output io-8 of the
+// float-float mode; 0 for the other modes or without a guard.
+template<typename T>
+__device__ __forceinline__ int ioShift(const int *sh, int io)
+{
+  if constexpr(std::is_same<T,ff>::value) return sh ? __ldg(sh+io) : 0;
+  else return 0;
 }
 
 template<typename T>
-__device__ __forceinline__ cplx<T> loadIO(const cplx<T> *p, bool f64)
+__device__ __forceinline__ cplx<T> loadIO(const cplx<T> *p, bool f64,
+                                          int sh=0)
 {
   if constexpr(std::is_same<T,ff>::value) {
     if(f64) {
       double2 d=*(const double2 *) p;
-      return mk(toFF(d.x),toFF(d.y));
+      return mk(toFF(d.x,sh),toFF(d.y,sh));
     }
   }
   return *p;
 }
 
 template<typename T>
-__device__ __forceinline__ T loadIOr(const T *p, bool f64)
+__device__ __forceinline__ T loadIOr(const T *p, bool f64, int sh=0)
 {
   if constexpr(std::is_same<T,ff>::value)
-    if(f64) return toFF(*(const double *) p);
+    if(f64) return toFF(*(const double *) p,sh);
   return *p;
 }
 
 template<typename T>
-__device__ __forceinline__ void storeIO(cplx<T> *p, cplx<T> v, bool f64)
+__device__ __forceinline__ void storeIO(cplx<T> *p, cplx<T> v, bool f64,
+                                        int sh=0)
 {
   if constexpr(std::is_same<T,ff>::value) {
     if(f64) {
-      *(double2 *) p=make_double2(fromFF(v.x),fromFF(v.y));
+      *(double2 *) p=make_double2(fromFF(v.x,sh),fromFF(v.y,sh));
       return;
     }
   }
@@ -361,11 +384,11 @@ __device__ __forceinline__ void storeIO(cplx<T> *p, cplx<T> v, bool f64)
 }
 
 template<typename T>
-__device__ __forceinline__ void storeIOr(T *p, T v, bool f64)
+__device__ __forceinline__ void storeIOr(T *p, T v, bool f64, int sh=0)
 {
   if constexpr(std::is_same<T,ff>::value) {
     if(f64) {
-      *(double *) p=fromFF(v);
+      *(double *) p=fromFF(v,sh);
       return;
     }
   }
@@ -375,11 +398,11 @@ __device__ __forceinline__ void storeIOr(T *p, T v, bool f64)
 // Convert n elements staged in shared memory as FP64 (by cp.async) to
 // float-float in place; each thread converts the elements it copied.
 template<typename T>
-__device__ __forceinline__ void convertStaged(cplx<T> *y, int i)
+__device__ __forceinline__ void convertStaged(cplx<T> *y, int i, int sh=0)
 {
   if constexpr(std::is_same<T,ff>::value) {
     double2 d=*(double2 *) (y+i);
-    y[i]=mk(toFF(d.x),toFF(d.y));
+    y[i]=mk(toFF(d.x,sh),toFF(d.y,sh));
   }
 }
 
@@ -513,8 +536,11 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
         long long row=row0+col-a*R;
         if(s < L && row < P.nrows) {
           long long off=row*P.rowStride+s;
-          if(P.realIO) v[u]=mk(loadIOr((const T *) P.in[a]+off,P.io64 & 1),(T) 0);
-          else if(P.io64 & 1) v[u]=loadIO(P.in[a]+off,true);
+          if(P.realIO)
+            v[u]=mk(loadIOr((const T *) P.in[a]+off,P.io64 & 1,
+                            ioShift<T>(P.ioShift,a)),(T) 0);
+          else if(P.io64 & 1)
+            v[u]=loadIO(P.in[a]+off,true,ioShift<T>(P.ioShift,a));
           else v[u]=ldx<CG>(P.in[a]+off);
         }
       }
@@ -554,8 +580,9 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
       if(row >= P.nrows) continue;
       cplx<T> v=Z[sp(posmod(s-c,m)*ld+col)];
       long long off=row*P.rowStride+s;
-      if(P.realIO) storeIOr((T *) P.out[b]+off,v.x*P.scale,P.io64 & 2);
-      else storeIO(P.out[b]+off,v*P.scale,P.io64 & 2);
+      const int sh=ioShift<T>(P.ioShift,8+b);
+      if(P.realIO) storeIOr((T *) P.out[b]+off,v.x*P.scale,P.io64 & 2,sh);
+      else storeIO(P.out[b]+off,v*P.scale,P.io64 & 2,sh);
     }
     __syncthreads();
   } else {
@@ -572,8 +599,11 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
         long long row=row0+col-a*R;
         if(row < P.nrows) {
           long long off=row*P.rowStride+s;
-          if(P.realIO) v[u]=mk(loadIOr((const T *) P.in[a]+off,P.io64 & 1),(T) 0);
-          else if(P.io64 & 1) v[u]=loadIO(P.in[a]+off,true);
+          if(P.realIO)
+            v[u]=mk(loadIOr((const T *) P.in[a]+off,P.io64 & 1,
+                            ioShift<T>(P.ioShift,a)),(T) 0);
+          else if(P.io64 & 1)
+            v[u]=loadIO(P.in[a]+off,true,ioShift<T>(P.ioShift,a));
           else v[u]=ldx<CG>(P.in[a]+off);
         }
       }
@@ -633,8 +663,10 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
       long long row=row0+col-b*R;
       if(row >= P.nrows) continue;
       long long off=row*P.rowStride+s;
-      if(P.realIO) storeIOr((T *) P.out[b]+off,acc[i].x*P.scale,P.io64 & 2);
-      else storeIO(P.out[b]+off,acc[i]*P.scale,P.io64 & 2);
+      const int sh=ioShift<T>(P.ioShift,8+b);
+      if(P.realIO)
+        storeIOr((T *) P.out[b]+off,acc[i].x*P.scale,P.io64 & 2,sh);
+      else storeIO(P.out[b]+off,acc[i]*P.scale,P.io64 & 2,sh);
     }
     __syncthreads();
   }
@@ -692,8 +724,9 @@ hermRowKernel(const HermRowPlan<T> P, const Mul mul)
         const cplx<T> *zr=P.in[a]+row*P.rowStride;
         const bool live=i < Nh*ld && row < P.nrows;
         const int kk=Nh-k;
-        zk[u]=live && k < H ? loadIO(zr+k,P.io64 & 1) : mk((T) 0,(T) 0);
-        zc[u]=live && kk < H ? loadIO(zr+kk,P.io64 & 1) : mk((T) 0,(T) 0);
+        const int sh=ioShift<T>(P.ioShift,a);
+        zk[u]=live && k < H ? loadIO(zr+k,P.io64 & 1,sh) : mk((T) 0,(T) 0);
+        zc[u]=live && kk < H ? loadIO(zr+kk,P.io64 & 1,sh) : mk((T) 0,(T) 0);
       }
 #pragma unroll
       for(int u=0; u < FGB_LOADS; ++u) {
@@ -742,7 +775,8 @@ hermRowKernel(const HermRowPlan<T> P, const Mul mul)
       cplx<T> dd=zk-zm;
       cplx<T> o=mk(dd.y*half,-dd.x*half);
       cplx<T> v=e+twmul<-1>(o,tw[k]);
-      storeIO(P.out[b]+row*P.rowStride+k,v*P.scale,P.io64 & 2);
+      storeIO(P.out[b]+row*P.rowStride+k,v*P.scale,P.io64 & 2,
+              ioShift<T>(P.ioShift,8+b));
     }
     __syncthreads();
   }

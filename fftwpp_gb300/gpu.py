@@ -22,7 +22,8 @@ from ._native import (CENTERED, F32, F64, FF, HERMITIAN, MULT, PAD,
 
 __all__ = ["HybridConvolution", "BatchedConvolution", "PaddedTransform",
            "PAD", "CENTERED", "HERMITIAN", "REAL", "default_M",
-           "set_autotune", "set_residue_search", "set_host_path"]
+           "set_autotune", "set_residue_search", "set_host_path",
+           "set_ff_range_guard"]
 
 
 def set_autotune(on: bool = True) -> None:
@@ -34,6 +35,12 @@ def set_residue_search(on: bool = True) -> None:
     """Timed choice of the residue block length m per axis, process-wide
     (fgb_set_residue_search; the counterpart of FFTW++'s OptBase search)."""
     _native.load().fgb_set_residue_search(int(bool(on)))
+
+
+def set_ff_range_guard(on: bool = True) -> None:
+    """Exponent scaling of FP64 data in the float-float mode, process-wide
+    (fgb_set_ff_range_guard, default on)."""
+    _native.load().fgb_set_ff_range_guard(int(bool(on)))
 
 
 def set_host_path(inputs: int = -1, outputs: int = -1) -> None:

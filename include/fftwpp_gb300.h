@@ -112,6 +112,21 @@ int fgb_convolve_host_with(fgb_conv *c, const void *launchers,
 int fgb_set_drop_in_precision(int precision);
 int fgb_get_drop_in_precision(void);
 
+/* Range guard of the float-float mode, process-wide (default on).  Floats
+ * span exponents of about +-126 against a double's +-1022, so before each
+ * float-float convolution a scan of the FP64 inputs finds each array's
+ * largest exponent, the first kernel scales the inputs by exact powers of
+ * two and the last kernel scales the outputs back: inputs of any FP64
+ * magnitude (1e-300 to 1e300) keep FP64-grade accuracy.  Multipliers whose
+ * outputs are single products (binary, correlation, the Jacobian adjoint)
+ * scale each input separately; sums of products share a scale per factor
+ * group (the Jacobian u0 u3 - u1 u2: one for u0 and u1, one for u2 and u3;
+ * dot products: one per half); a caller's functor (FGB_MULT_USER) is not
+ * scaled.  Values below about 2^-120 of
+ * their array's largest magnitude lose relative accuracy (their share of
+ * the L2 norm is below 1e-36).  0 turns the scan off. */
+void fgb_set_ff_range_guard(int on);
+
 /* Failure injection for tests, on the host: the n-th following device
  * allocation of the library (0: the next one) fails as cudaMalloc would, so
  * error paths (NULL plans, released partial allocations) can be exercised;

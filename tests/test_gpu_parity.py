@@ -174,10 +174,13 @@ def test_host_pointer_entry(native_lib, precision):
 
 
 @pytest.mark.parametrize("scales", [(1e-25, 1e30), (1e20, 1e-18), (1.0, 0.0),
-                                    (2.0 ** -69, 2.0 ** 69)])
+                                    (2.0 ** -69, 2.0 ** 69), (1e150, 1e-150),
+                                    (1e300, 1e-5), (1e-300, 1e5),
+                                    (1e150, 1e150), (1e-160, 1e-160)])
 def test_float_float_scales(native_lib, scales):
-    """FP64 inputs far from 1 (both sides of the fast split's range, and
-    zero) in the float-float mode."""
+    """FP64 inputs far from 1 (both sides of the fast split's range, far
+    beyond a float's exponent range, and zero) in the float-float mode: the
+    range guard scales them into range and back."""
     kinds, L, M = [H.CENTERED, H.HERMITIAN], [31, 31], [46, 46]
     fs = _inputs(kinds, L, 2, seed=13)
     fs = [fs[0] * scales[0], fs[1] * scales[1]]
@@ -389,3 +392,31 @@ def test_residue_search(native_lib, precision):
     assert rel_l2(searched[0], want) <= TOL[precision]
     a0, a1 = c0.axes[0], c1.axes[0]
     assert a0["m"] * a0["q"] >= 2047 and a1["m"] * a1["q"] >= 2047
+
+
+@pytest.mark.parametrize("case", [
+    ([H.CENTERED, H.HERMITIAN], [15, 15], [22, 22], "realjacobian", 4,
+     (1e150, 1e150, 1e-140, 1e-140)),
+    ([H.REAL, H.PAD, H.PAD], [8, 6, 5], [15, 11, 9], "binary", 2,
+     (1e-200, 1e250)),
+    ([H.PAD], [300], [599], "binary", 2, (1e280, 1e-250)),
+    ([H.PAD], [20000], [39999], "binary", 2, (1e-280, 1e250))])
+def test_float_float_range_guard(native_lib, case):
+    """Every first/last kernel family of the float-float mode (outer complex
+    and real, complex and Hermitian rows, the long 1D path) with inputs far
+    outside a float's range, against the oracle; without the guard the
+    same inputs overflow or underflow the float exponent."""
+    from fftwpp_gb300.gpu import set_ff_range_guard
+    kinds, L, M, mult, A, sc = case
+    fs = _inputs(kinds, L, A, seed=sum(L) + A)
+    fs = [f * s for f, s in zip(fs, sc)]
+    want = H.convolve(fs, kinds, L, M, mult=mult)[0]
+    got, _ = run_gpu(kinds, L, M, fs, mult, "ff")
+    assert rel_l2(got[0], want) <= 1e-13
+    try:
+        set_ff_range_guard(False)
+        raw, _ = run_gpu(kinds, L, M, fs, mult, "ff")
+    finally:
+        set_ff_range_guard(True)
+    assert not (rel_l2(raw[0], want) <= 1e-13)
+
