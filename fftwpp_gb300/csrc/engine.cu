@@ -422,7 +422,7 @@ static void planOuter(AxisPlan& a, long mForce, int prec, long C, long nbatch,
 Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
            const long *mForce, int A, int B, int mult, int prec, long batch,
            bool tuneSchedule)
-  : batch(batch), user(NULL), isStrided(false), ffState(NULL),
+  : batch(batch), user(NULL), isStrided(false), ffState(NULL), longBuf(0),
     tuning(false), staging(0), hostIn(NULL),
     hostOut(NULL), nlaunch(0),
     timing(false), normalize(true), marks(0), hostTile(0), hostThr(0),
@@ -497,11 +497,13 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
   else ok=planRowComplex(in,mf,A,B,prec);
   if(in.kind == KIND_REAL && dim == 1) in.rows=0;
   if(!ok) {
-    if(dim != 1 || in.kind != KIND_PAD)
-      throw std::runtime_error("row too long for one CTA (only 1D complex "
-                               "fftPad data takes the long path)");
-    // Long 1D: N = rowM * rowQ; columns of length rowQ (outer, explicit,
-    // with the W_N^{t r} twiddle), rows of length rowM (unpadded).
+    // Long rows (beyond one CTA's shared memory), any kind: the row is a
+    // cyclic convolution of length N = rowM * rowQ >= M (explicit padding,
+    // which is dealiased for every kind once N >= M), computed as columns
+    // of length rowQ (outer, with the W_N^{t r} twiddle), rows of length
+    // rowM and the inverse columns.  Centred data sit cyclically shifted
+    // by floor(L/2), Hermitian data as their mirrored full spectrum, real
+    // data with zero imaginary parts (FlatMode).
     long N=nextfftsize(in.M);
     long best=0;
     for(long m=1; m <= N; ++m)
@@ -511,19 +513,26 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
     I.longRow=true;
     I.rowM=best;
     I.rowQ=N/best;
-    in.N=N; in.m=best; in.q=N/best; in.p=ceilquotient(in.L,best);
-    in.cshift=0;
-    auto sm=[&](int t) {return outerNeed(prec,in.p,I.rowQ,t);};
-    in.tile=pickTile(wide(prec) ? 8 : 16,I.rowM,A,sm);
-    in.tileB=pickTile(wide(prec) ? 8 : 16,I.rowM,B,sm);
-    if(mForce && mForce[0] > 0)
+    in.N=N; in.m=best; in.q=N/best; in.p=ceilquotient(in.stored,best);
+    in.cshift=in.kind == KIND_CENTERED ? (int) (in.L/2) : 0;
+    // The column kernels of the other kinds cover all rowQ rows.
+    const long colRows=in.kind == KIND_PAD || in.kind == KIND_REAL ? in.p :
+      I.rowQ;
+    long outerRows=batch;
+    for(int d=0; d < dim-1; ++d) outerRows *= I.axis[d].rows;
+    auto sm=[&](int t) {return outerNeed(prec,colRows,I.rowQ,t);};
+    in.tile=pickTile(wide(prec) ? 8 : 16,I.rowM,A*outerRows,sm);
+    in.tileB=pickTile(wide(prec) ? 8 : 16,I.rowM,B*outerRows,sm);
+    if(mForce && mForce[dim-1] > 0)
       throw std::runtime_error("forced m not supported on the long path");
+    if(outerRows*A > 65535 || outerRows*B > 65535)
+      throw std::runtime_error("too many long rows for one launch");
   }
   // Rows per CTA of the row kernel.
   long nrows=batch;
   for(int d=0; d < dim-1; ++d) nrows *= I.axis[d].rows;
   if(I.longRow) {
-    in.rpc=pickRpc(I.rowM,A,I.rowQ,[&](int r) {
+    in.rpc=pickRpc(I.rowM,A,I.rowQ*nrows,[&](int r) {
       return rowNeed(prec,I.rowM,I.rowM,A,B,r,1);});
   } else if(in.kind == KIND_HERMITIAN) {
     in.rpc=pickRpc(in.N/2,A,nrows,[&](int r) {
@@ -682,8 +691,8 @@ void Conv::tune()
     Tunable t;
     t.param=&in.rpc;
     t.thr=&in.thr;
-    t.launch=I.longRow ? 1 : dim-1;
-    long avail=I.longRow ? I.rowQ : nrows;
+    t.launch=I.longRow ? dim : dim-1;
+    long avail=I.longRow ? I.rowQ*nrows : nrows;
     for(int r : {1,2,3,4,6,8}) {
       if(r > avail) break;
       size_t need=I.longRow ? rowNeed(prec,I.rowM,I.rowM,A,B,r,1) :
@@ -884,8 +893,7 @@ void Conv::allocate()
     staging += bytes;
   };
   if(I.dim == 1) {
-    if(I.longRow) for(int a=0; a < A; ++a) get(e*(size_t) I.axis[0].N);
-    nlaunch=I.longRow ? 3 : 1;
+    nlaunch=1;
   } else if(I.dim == 2) {
     size_t rows=I.axis[0].rows;
     size_t C=I.axis[1].stored;
@@ -897,6 +905,15 @@ void Conv::allocate()
     for(int a=0; a < A; ++a) get(e*rx*Ly*nz);
     for(int a=0; a < A; ++a) get(e*rx*ry*nz);
     nlaunch=5;
+  }
+  if(I.longRow) {
+    // Long rows: A column-transformed copies of every inner row, N each;
+    // two more launches (the column kernels around the row kernel).
+    size_t rows=batch;
+    for(int d=0; d < I.dim-1; ++d) rows *= I.axis[d].rows;
+    longBuf=bufs.size();
+    for(int a=0; a < A; ++a) get(e*rows*(size_t) I.axis[I.dim-1].N);
+    nlaunch += 2;
   }
 }
 
@@ -980,7 +997,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
         for(int k=0; k < f.nst; ++k) im.radix[d][k]=(unsigned char) f.radix[k];
       }
     }
-    if(I.longRow) im.q[0]=(int) I.rowQ;     // long 1D rows: k = row + q k2
+    if(I.longRow) im.longQ=(int) I.rowQ;    // long rows: k = k1 + q k2
   }
   auto rowPlan=[&](RowPlan<T>& P, const AxisPlan& a) {
     P.im=im;
@@ -1083,48 +1100,9 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     return e;
   }
 
-  if(I.dim == 1) {  // long 1D complex
-    const AxisPlan& a=I.axis[0];
-    long m=I.rowM, q=I.rowQ;
-    OuterPlan<T> O{};
-    O.L=(int) a.p; O.m=(int) q; O.q=1; O.N=(int) q; O.cshift=0;
-    O.tile=a.tile;
-    O.fp=fftPlan(q,I.prec);
-    O.twN=(const typename TwT<T>::type *) twiddles(q,I.prec);
-    O.twX=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
-    O.NX=a.N;
-    O.io64=0;
-    O.inplace=0;
-    O.conj=0;
-    O.ioShift=guard;
-    O.count=A; O.nbatch=1; O.inBatch=O.outBatch=0;
-    O.inRow=m; O.outRow=m; O.C=(int) m; O.Ltot=a.L;
-    O.scale=(T) 1;
-    O.io64=IN64;
-    for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) bufs[i];}
-    e=launchOuterFwd<T>(O,threads,s);
-    tick(s);
-    if(e != cudaSuccess) return e;
-    AxisPlan ra=a;
-    ra.stored=m; ra.L=m; ra.m=m; ra.q=1; ra.N=m; ra.cshift=0;
-    RowPlan<T> P{};
-    rowPlan(P,ra);
-    for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
-    for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
-    P.rowStride=m; P.nrows=q; P.scale=(T) 1;
-    e=rowLaunch<T>(P,a.thr,q,s);
-    tick(s);
-    if(e != cudaSuccess) return e;
-    O.count=B;
-    O.tile=a.tileB;
-    O.Ltot=a.L;
-    O.scale=(T) scale;
-    O.io64=OUT64;
-    for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) bufs[i]; O.out[i]=(Cx *) out[i];}
-    e=launchOuterBwd<T>(O,threads,s);
-    tick(s);
-    return e;
-  }
+  if(I.dim == 1)             // long 1D rows
+    return runLong<T>(in,out,batch,I.axis[0].stored,IN64 | OUT64,guard,&im,
+                      scale,s);
 
   if(I.dim == 2) {
     const AxisPlan& ax=I.axis[0];
@@ -1144,13 +1122,17 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     e=firstOuter(O,ax);
     tick(s);
     if(e != cudaSuccess) return e;
-    if(ay.kind == KIND_HERMITIAN) {
+    if(I.longRow) {
+      e=runLong<T>((const void *const *) bufs.data(),bufs.data(),ax.rows,C,0,
+                   NULL,&im,1.0,s);
+    } else if(ay.kind == KIND_HERMITIAN) {
       HermRowPlan<T> P{};
       hermPlan(P,ay);
       for(int i=0; i < A; ++i) P.in[i]=(const Cx *) bufs[i];
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
       P.rowStride=C; P.nrows=ax.rows; P.scale=(T) 1;
       e=hermLaunch<T>(P,ay.thr,ax.rows,s);
+      tick(s);
     } else {
       RowPlan<T> P{};
       rowPlan(P,ay);
@@ -1158,8 +1140,8 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
       for(int i=0; i < B; ++i) P.out[i]=(Cx *) bufs[i];
       P.rowStride=C; P.nrows=ax.rows; P.scale=(T) 1;
       e=rowLaunch<T>(P,ay.thr,ax.rows,s);
+      tick(s);
     }
-    tick(s);
     if(e != cudaSuccess) return e;
     O.count=B;
     O.tile=ax.tileB;
@@ -1211,13 +1193,16 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   if(e != cudaSuccess) return e;
 
   long nrows=ax.rows*ay.rows;
-  if(az.kind == KIND_HERMITIAN) {
+  if(I.longRow) {
+    e=runLong<T>((const void *const *) by,by,nrows,nz,0,NULL,&im,1.0,s);
+  } else if(az.kind == KIND_HERMITIAN) {
     HermRowPlan<T> P{};
     hermPlan(P,az);
     for(int i=0; i < A; ++i) P.in[i]=(const Cx *) by[i];
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) by[i];
     P.rowStride=nz; P.nrows=nrows; P.scale=(T) 1;
     e=hermLaunch<T>(P,az.thr,nrows,s);
+    tick(s);
   } else {
     RowPlan<T> P{};
     rowPlan(P,az);
@@ -1225,8 +1210,8 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     for(int i=0; i < B; ++i) P.out[i]=(Cx *) by[i];
     P.rowStride=nz; P.nrows=nrows; P.scale=(T) 1;
     e=rowLaunch<T>(P,az.thr,nrows,s);
+    tick(s);
   }
-  tick(s);
   if(e != cudaSuccess) return e;
 
   Y.count=B;
@@ -1246,6 +1231,68 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   for(int i=0; i < B; ++i) {X.in[i]=(const Cx *) bx[i]; X.out[i]=(Cx *) out[i];}
   e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(X,ax.thrB,s) :
     launchOuterBwd<T>(X,ax.thrB,s);
+  tick(s);
+  return e;
+}
+
+template<typename T>
+cudaError_t Conv::runLong(const void *const *in, void *const *out,
+                          long long nrows, long long rowStride, int io64,
+                          const int *guard, const IndexMap *im, double scale,
+                          cudaStream_t s)
+{
+  typedef cplx<T> Cx;
+  const AxisPlan& a=I.axis[I.dim-1];
+  const int A=I.A, B=I.B;
+  const long m=I.rowM, q=I.rowQ, N=a.N;
+  void *const *lb=bufs.data()+longBuf;
+  const int flat=a.kind == KIND_CENTERED ? FLAT_CENTERED :
+    a.kind == KIND_HERMITIAN ? FLAT_HERMITIAN :
+    a.kind == KIND_REAL ? FLAT_REAL : FLAT_PAD;
+  const int threads=256;
+  cudaError_t e;
+  // Columns of length q over the q x m view of every row, with the
+  // W_N^{col k} twiddle (explicit padding of the row to N).
+  OuterPlan<T> O{};
+  O.L=(int) (flat == FLAT_PAD || flat == FLAT_REAL ? a.p : q);
+  O.m=(int) q; O.q=1; O.N=(int) q; O.cshift=0;
+  O.tile=a.tile;
+  O.fp=fftPlan(q,I.prec);
+  O.twN=(const typename TwT<T>::type *) twiddles(q,I.prec);
+  O.twX=(const typename TwT<T>::type *) twiddles(N,I.prec);
+  O.NX=N;
+  O.io64=io64 & 1; O.ioShift=guard;
+  O.inplace=0; O.conj=0;
+  O.flat=flat; O.flatC=a.cshift;
+  O.count=A; O.nbatch=(int) nrows; O.inBatch=rowStride; O.outBatch=N;
+  O.inRow=m; O.outRow=m; O.C=(int) m; O.Ltot=a.stored;
+  O.scale=(T) 1;
+  for(int i=0; i < A; ++i) {O.in[i]=(const Cx *) in[i]; O.out[i]=(Cx *) lb[i];}
+  e=launchOuterFwd<T>(O,threads,s);
+  tick(s);
+  if(e != cudaSuccess) return e;
+  // Rows of length m: one residue, one fold (the direct row variant).
+  RowPlan<T> P{};
+  P.im=*im;
+  P.L=(int) m; P.m=(int) m; P.q=1; P.N=(int) m; P.cshift=0;
+  P.A=A; P.B=B; P.mult=I.mult; P.realIO=0;
+  P.rpc=a.rpc; P.io64=0; P.direct=1; P.ioShift=NULL;
+  P.fp=fftPlan(m,I.prec,true);
+  P.twN=(const typename TwT<T>::type *) twiddles(m,I.prec);
+  for(int i=0; i < A; ++i) P.in[i]=(const Cx *) lb[i];
+  for(int i=0; i < B; ++i) P.out[i]=(Cx *) lb[i];
+  P.rowStride=m; P.nrows=nrows*q; P.scale=(T) 1;
+  e=rowLaunch<T>(P,a.thr,nrows*q,s);
+  tick(s);
+  if(e != cudaSuccess) return e;
+  // Inverse columns, back into the rows' stored entries.
+  O.count=B;
+  O.tile=a.tileB;
+  O.io64=io64 & 2;
+  O.scale=(T) scale;
+  O.inBatch=N; O.outBatch=rowStride;
+  for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) lb[i]; O.out[i]=(Cx *) out[i];}
+  e=launchOuterBwd<T>(O,threads,s);
   tick(s);
   return e;
 }

@@ -17,6 +17,7 @@ namespace fgb {
 struct RowLaunchers;       // kernels.cuh
 template<typename T> struct RowPlan;
 template<typename T> struct HermRowPlan;
+struct IndexMap;
 
 enum AxisKind {KIND_PAD=0, KIND_CENTERED=1, KIND_HERMITIAN=2, KIND_REAL=3};
 // PREC_FF: FP64 data at the interface, float-float arithmetic inside.
@@ -167,6 +168,8 @@ private:
                                               cudaStream_t s);
   cudaError_t checkUser(const RowLaunchers *L);
   std::vector<void *> bufs;        // device staging buffers
+  size_t longBuf;                  // index in bufs of the long rows' A
+                                   // column-transformed copies
   size_t staging;
   void *hostIn, *hostOut;          // device copies for runHost
   int nlaunch;
@@ -181,6 +184,15 @@ private:
   void tick(cudaStream_t s);
   template<typename T> cudaError_t runT(const void *const *in,
                                         void *const *out, cudaStream_t s);
+  // The innermost axis on the long path: nrows rows of rowStride stored
+  // entries in in[] (FP64 values in float-float mode when io64 bit 0 is
+  // set) convolved into out[] (bit 1); three launches.
+  template<typename T> cudaError_t runLong(const void *const *in,
+                                           void *const *out, long long nrows,
+                                           long long rowStride, int io64,
+                                           const int *guard,
+                                           const IndexMap *im,
+                                           double scale, cudaStream_t s);
   // Axis-0 schedule for runs that read or write page-locked host arrays
   // in place: the fastest column tiles (and threads) whose rows span at
   // least 64 bytes, 0 where no candidate does; and the ways (HostWay) the

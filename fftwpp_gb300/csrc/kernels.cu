@@ -45,7 +45,35 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
   const typename TwT<T>::type *tw=P.twN;
   const UDiv dTile(tile);
 
-  if(L <= m) {
+  if(P.flat != FLAT_PAD) {
+    // Long rows of the other kinds: every position n = t*C + col of the
+    // flattened row holds the data index of its kind (FlatMode); loaded
+    // and converted directly (conjugated mirror, real values).
+    const T *srcR=(const T *) P.in[a]+batch*P.inBatch;
+    const int sh=ioShift<T>(P.ioShift,a);
+    for(int i=tid; i < m*tile; i += nthr) {
+      int t=dTile(i), cc=i-t*tile;
+      int col=col0+cc;
+      cplx<T> v=mk((T) 0,(T) 0);
+      if(col < P.C) {
+        const long long n=(long long) t*P.inRow+col;
+        if(P.flat == FLAT_CENTERED) {
+          long long sx=n+P.flatC;
+          if(sx >= P.NX) sx -= P.NX;
+          if(sx < P.Ltot) v=loadIO(src+sx,P.io64 & 1,sh);
+        } else if(P.flat == FLAT_HERMITIAN) {
+          if(n < P.Ltot) {
+            v=loadIO(src+n,P.io64 & 1,sh);
+            if(n == 0) v.y=(T) 0;
+          } else if(P.NX-n < P.Ltot) v=conjg(loadIO(src+(P.NX-n),P.io64 & 1,sh));
+        } else if(n < P.Ltot) {
+          v=mk(loadIOr(srcR+n,P.io64 & 1,sh),(T) 0);
+        }
+      }
+      x[sp(i)]=v;
+    }
+    __syncthreads();
+  } else if(L <= m) {
     // One term per output: asynchronous copies straight to each value's
     // transform slot, then the conversion and residue twiddle in place by
     // the same thread.
@@ -208,6 +236,29 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
       X=x;
     } else {
       X=fftSmem<T,-1>(x,y,P.fp,tile,tile,tid,nthr);
+    }
+    if(direct && P.flat != FLAT_PAD) {
+      // Long rows of the other kinds: the output of data index sx is the
+      // flattened position n of its kind (FlatMode).
+      T *dstR=(T *) P.out[b]+batch*P.outBatch;
+      const int sh=ioShift<T>(P.ioShift,8+b);
+      for(int i=tid; i < m*tile; i += nthr) {
+        int t=dTile(i), cc=i-t*tile;
+        int col=col0+cc;
+        if(col >= P.C) continue;
+        const long long n=(long long) t*P.outRow+col;
+        const cplx<T> v=X[sp(i)]*P.scale;
+        if(P.flat == FLAT_CENTERED) {
+          long long sx=n+P.flatC;
+          if(sx >= P.NX) sx -= P.NX;
+          if(sx < P.Ltot) storeIO(dst+sx,v,P.io64 & 2,sh);
+        } else if(n < P.Ltot) {
+          if(P.flat == FLAT_REAL) storeIOr(dstR+n,v.x,P.io64 & 2,sh);
+          else storeIO(dst+n,v,P.io64 & 2,sh);
+        }
+      }
+      __syncthreads();
+      return;
     }
     if(direct) {
       for(int i=tid; i < L*tile; i += nthr) {

@@ -66,6 +66,9 @@ struct IndexMap {
   int nst[2];              // ... over these radices (fftDIF order)
   unsigned char radix[2][FGB_MAXSTAGES];
   long long rowsY;         // 3D: staging rows of axis 1 per row of axis 0
+  int longQ;               // innermost axis on the long path: its column
+                           // DFT length q (row = outer row * q + k1, inner
+                           // index k1 + q k2); 0 otherwise
 };
 
 template<typename T>
@@ -112,6 +115,8 @@ struct HermRowPlan {
   IndexMap im;             // slot positions (position-dependent multipliers)
 };
 
+enum FlatMode {FLAT_PAD=0, FLAT_CENTERED=1, FLAT_HERMITIAN=2, FLAT_REAL=3};
+
 template<typename T>
 struct OuterPlan {
   const cplx<T> *in[FGB_MAXA];
@@ -136,6 +141,13 @@ struct OuterPlan {
   long long cs;            // (c / cz) cs + c % cz (cz = 0: at c)
   int kc;                  // real kernels: complex-side rows stored (the
                            // ceil(L/2) Hermitian modes), 0 for all N/2+1
+  int flat;                // long rows (twX set, q = 1): position n of the
+                           // flattened q x C view holds data index
+                           // FLAT_PAD n, FLAT_CENTERED (n + flatC) mod NX,
+                           // FLAT_HERMITIAN the Hermitian-mirrored modes
+                           // (n < Ltot, conj of NX - n), FLAT_REAL n of a
+                           // real array
+  long long flatC;
   T scale;
   FFTPlanDev fp;           // length-m (complex) or length-N/2 (real) FFT
   const typename TwT<T>::type *twN;

@@ -250,11 +250,14 @@ __device__ __forceinline__ void mulRowSlot(const Mul& mul, const RowPlan<T>& P,
                                            long long row, int j, int r)
 {
   if constexpr(Mul::positional) {
-    Indices ix=outerIndices(P.im,row);
     const int jn=REV ? digitRev(j,P.fp.n,P.fp.nst,P.fp.radix) : j;
     int k=P.q*jn+r;
-    if(P.im.dim == 1 && P.im.q[0] > 0)     // long 1D rows: column k1 = row
-      k=(int) row+P.im.q[0]*jn;
+    long long orow=row;
+    if(P.im.longQ > 0) {               // long rows: column k1 of outer row
+      orow=row/P.im.longQ;
+      k=(int) (row-orow*P.im.longQ)+P.im.longQ*jn;
+    }
+    Indices ix=outerIndices(P.im,orow);
     ix.index[P.im.dim-1]=k;
     mul.at(X,base,stride,ix);
   } else {

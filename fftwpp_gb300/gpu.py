@@ -226,13 +226,15 @@ class HybridConvolution:
         k = self.kinds
         inner = "herm_row" if k[-1] == HERMITIAN else "row_conv"
         x = "real" if k[0] == REAL else ""
+        # Long inner rows: column kernels around the row kernel.
+        rows = (["outer_fwd_cols", "row_conv", "outer_bwd_cols"]
+                if self.long_path else [inner])
         if self.dim == 1:
-            names = (["outer_fwd_cols", "row_conv", "outer_bwd_cols"]
-                     if self.long_path else [inner])
+            names = rows
         elif self.dim == 2:
-            names = [f"outer{x}_fwd_x", inner, f"outer{x}_bwd_x"]
+            names = [f"outer{x}_fwd_x", *rows, f"outer{x}_bwd_x"]
         else:
-            names = [f"outer{x}_fwd_x", "outer_fwd_y", inner, "outer_bwd_y",
+            names = [f"outer{x}_fwd_x", "outer_fwd_y", *rows, "outer_bwd_y",
                      f"outer{x}_bwd_x"]
         return names
 

@@ -131,6 +131,7 @@ CASES = [
     ([H.REAL, H.PAD], [16, 15], [31, 29], None),
     ([H.REAL, H.PAD, H.PAD], [12, 10, 9], [23, 19, 17], None),
     ([H.CENTERED, H.CENTERED, H.HERMITIAN], [9, 7, 9], [13, 10, 13], None),
+    ([H.CENTERED, H.HERMITIAN], [7, 8191], [10, 12286], None),  # long rows
 ]
 
 
