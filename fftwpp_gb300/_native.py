@@ -53,6 +53,9 @@ def load():
     lib.fgb_convolve_device_with.argtypes = [vp, vp, P(vp), P(vp), vp]
     lib.fgb_convolve_host_with.restype = ctypes.c_int
     lib.fgb_convolve_host_with.argtypes = [vp, vp, P(vp), P(vp)]
+    lib.fgb_fft_origin_shift_device.restype = ctypes.c_int
+    lib.fgb_fft_origin_shift_device.argtypes = [vp, sz, sz, sz, ctypes.c_int,
+                                                vp]
     lib.fgb_set_ff_range_guard.restype = None
     lib.fgb_set_ff_range_guard.argtypes = [ctypes.c_int]
     lib.fgb_set_strides.restype = ctypes.c_int

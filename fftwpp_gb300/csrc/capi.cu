@@ -1004,6 +1004,34 @@ int fgb_fft_execute_device(fgb_fft *h, const void *in, void *out,
 
 void fgb_fft_destroy(fgb_fft *h) {delete h;}
 
+int fgb_fft_origin_shift_device(void *f, size_t nx, size_t ny, size_t nz,
+                                int precision, void *stream)
+{
+  const char *where="fgb_fft_origin_shift_device";
+  if(!f || nx < 1 || ny < 1 || nz < 1) {report(where,"bad arguments"); return -1;}
+  if(precision != PREC_F64 && precision != PREC_F32) {
+    report(where,"precision must be FGB_F64 or FGB_F32");
+    return -1;
+  }
+  if(nx % 2 || (nz > 1 && ny % 2)) {
+    report(where,"shifting the Fourier origin needs an even nx (and an "
+           "even ny in 3D)");
+    return -1;
+  }
+  if((size_t) f % (precision == PREC_F64 ? 8 : 4)) {
+    report(where,"array must be aligned to its element size");
+    return -1;
+  }
+  cudaError_t e=launchOriginShift(f,(long long) nx,(long long) ny,
+                                  (long long) nz,precision == PREC_F64,
+                                  (cudaStream_t) stream);
+  if(e != cudaSuccess) {
+    report(where,cudaGetErrorString(e));
+    return -2;
+  }
+  return 0;
+}
+
 const char *fgb_last_error(void)
 {
   static thread_local std::string s;

@@ -1801,7 +1801,8 @@ cudaError_t PadTransform::backward(const void *F, void *f, cudaStream_t s)
 PlainFFT::PlainFFT(int kind, long n, int sign, long C, long B, long istride,
                    long ibatch, long ostride, long obatch, int prec)
   : kind(kind), sign(sign), prec(prec), n(n), C(C), B(B), istride(istride),
-    ibatch(ibatch), ostride(ostride), obatch(obatch), tile(1)
+    ibatch(ibatch), ostride(ostride), obatch(obatch), tile(1), n1(0), n2(0),
+    tile1(1), tile2(1), scratch(NULL)
 {
   if(kind != FFT_C2C && kind != FFT_R2C && kind != FFT_C2R)
     throw std::runtime_error("unknown transform kind");
@@ -1827,10 +1828,109 @@ PlainFFT::PlainFFT(int kind, long n, int sign, long C, long B, long istride,
                       FGB_BY_PREC(prec,outerBwdSmem,n,n,t,1,0));
     return FGB_BY_PREC(prec,outerRealSmem,n,n/2,t);
   };
-  if(sm(1) > SMEM_MAX)
-    throw std::runtime_error("length "+std::to_string(n)+
-                             " is too long for one CTA's shared memory");
+  if(sm(1) > SMEM_MAX) {
+    if(kind != FFT_C2C || C != 1 || istride != 1 || ostride != 1)
+      throw std::runtime_error("length "+std::to_string(n)+" is too long for "
+                               "one CTA's shared memory (longer transforms "
+                               "take complex contiguous sequences)");
+    if(B > 1 && (ibatch < n || obatch < n))
+      throw std::runtime_error("long sequences must not overlap");
+    // n = n1 n2 with both passes in one CTA, n1 as close to sqrt(n) as
+    // the factors allow.
+    auto fits=[&](long k, int t) {
+      return std::max(FGB_BY_PREC(prec,outerFwdSmem,k,k,t,0),
+                      FGB_BY_PREC(prec,outerBwdSmem,k,k,t,1,0)) <= SMEM_MAX;
+    };
+    long best=0;
+    for(long a=2; a*a <= n*4 && a < n; ++a)
+      if(n % a == 0 && smooth(a) && fits(a,1) && fits(n/a,1) &&
+         (!best || std::labs(a*a-n) < std::labs(best*best-n))) best=a;
+    if(!best)
+      throw std::runtime_error("no two-pass plan for length "+
+                               std::to_string(n));
+    n1=best;
+    n2=n/best;
+    // Coalesced side: the pass that reads (or writes) with unit column
+    // stride takes whole tiles; the strided one single columns.
+    auto smw=[&](long k) {
+      return [&,k](int t) {
+        return std::max(FGB_BY_PREC(prec,outerFwdSmem,k,k,t,0),
+                        FGB_BY_PREC(prec,outerBwdSmem,k,k,t,1,0));
+      };
+    };
+    tile1=pickTile(maxTile,sign > 0 ? n2 : n1,B,smw(sign > 0 ? n1 : n2));
+    tile2=pickTile(maxTile,sign > 0 ? n1 : n2,B,smw(sign > 0 ? n2 : n1));
+    if(devAlloc(&scratch,elem(prec)*(size_t) n*(size_t) B) != cudaSuccess) {
+      scratch=NULL;
+      throw std::runtime_error("device allocation of the scratch array "
+                               "failed");
+    }
+    return;
+  }
   tile=C > 1 ? pickTile(maxTile,C,B,sm) : 1;
+}
+
+PlainFFT::~PlainFFT()
+{
+  if(scratch) cudaFree(scratch);
+}
+
+// Two passes over the n1 x n2 view of each sequence (see engine.h).
+//   sign +1: s = i n2 + t.  Columns of length n1 over i (n2 of them,
+//     adjacent), the W_n^{t k1} twiddle after: Z[k1][t]; then the rows of Z
+//     read as single columns of stride 1 (column k1 at k1 n2), transformed
+//     over t into X[k1 + n1 k2].
+//   sign -1: s = i + n1 t.  Columns of length n2 over t (n1 of them,
+//     adjacent) written transposed as Y[i][k2] (column i at i n2); then
+//     columns of length n1 over i (n2 of them, adjacent) with the
+//     W_n^{-i k2} twiddle before: X[k2 + n2 k1].
+template<typename T>
+cudaError_t PlainFFT::runTwoPass(const void *in, void *out, cudaStream_t s)
+{
+  typedef cplx<T> Cx;
+  const int threads=256;
+  cudaError_t e;
+  auto base=[&](OuterPlan<T>& P, long len) {
+    P.L=(int) len; P.m=(int) len; P.q=1; P.N=(int) len; P.cshift=0;
+    P.fp=fftPlan(len,prec);
+    P.twN=(const typename TwT<T>::type *) twiddles(len,prec);
+    P.twX=NULL; P.NX=1;
+    P.io64=0; P.inplace=0; P.conj=0;
+    P.count=1; P.nbatch=(int) B;
+    P.Ltot=LLONG_MAX;
+    P.scale=(T) 1;
+  };
+  OuterPlan<T> P{};
+  if(sign > 0) {
+    base(P,n1);
+    P.twX=(const typename TwT<T>::type *) twiddles(n,prec); P.NX=n;
+    P.tile=tile1;
+    P.C=(int) n2; P.inRow=n2; P.outRow=n2;
+    P.inBatch=ibatch; P.outBatch=n;
+    P.in[0]=(const Cx *) in; P.out[0]=(Cx *) scratch;
+    if((e=launchOuterFwd<T>(P,threads,s)) != cudaSuccess) return e;
+    OuterPlan<T> Q{};
+    base(Q,n2);
+    Q.tile=tile2;
+    Q.C=(int) n1; Q.inRow=1; Q.cz=1; Q.cs=n2; Q.outRow=n1;
+    Q.inBatch=n; Q.outBatch=obatch;
+    Q.in[0]=(const Cx *) scratch; Q.out[0]=(Cx *) out;
+    return launchOuterFwd<T>(Q,threads,s);
+  }
+  base(P,n2);
+  P.tile=tile1;
+  P.C=(int) n1; P.inRow=n1; P.outRow=1; P.cz=1; P.cs=n2;
+  P.inBatch=ibatch; P.outBatch=n;
+  P.in[0]=(const Cx *) in; P.out[0]=(Cx *) scratch;
+  if((e=launchOuterBwd<T>(P,threads,s)) != cudaSuccess) return e;
+  OuterPlan<T> Q{};
+  base(Q,n1);
+  Q.twX=(const typename TwT<T>::type *) twiddles(n,prec); Q.NX=n;
+  Q.tile=tile2;
+  Q.C=(int) n2; Q.inRow=n2; Q.outRow=n2;
+  Q.inBatch=n; Q.outBatch=obatch;
+  Q.in[0]=(const Cx *) scratch; Q.out[0]=(Cx *) out;
+  return launchOuterBwd<T>(Q,threads,s);
 }
 
 template<typename T>
@@ -1873,6 +1973,9 @@ bool PlainFFT::aligned(const void *in, const void *out) const
 
 cudaError_t PlainFFT::execute(const void *in, void *out, cudaStream_t s)
 {
+  if(n1 > 0)
+    return prec == PREC_F64 ? runTwoPass<double>(in,out,s) :
+      runTwoPass<float>(in,out,s);
   return prec == PREC_F64 ? runT<double>(in,out,s) : runT<float>(in,out,s);
 }
 

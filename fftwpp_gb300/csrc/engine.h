@@ -271,23 +271,35 @@ private:
 // batches: element s of sequence c in batch b is at b*batch + s*stride + c,
 // counted in the element type of each side (real values on the real side
 // of r2c/c2r).  Signs follow FFTW: c2c either, r2c -1, c2r +1.  n is a
-// product of 2, 3, 5 and 7 (even for real transforms) that fits one CTA's
-// shared memory.
+// product of 2, 3, 5 and 7 (even for real transforms).  Lengths beyond one
+// CTA's shared memory (complex, contiguous sequences: C = 1, unit strides)
+// take two passes through a device scratch array: n = n1 n2, columns of
+// length n1 with the W_n twiddle, then rows of length n2 (the four-step
+// FFT; sign +1 in decimation-in-frequency order, sign -1 in
+// decimation-in-time order, so the twiddle always sits on the side of the
+// kernel that applies it).
 enum FFTKind {FFT_C2C=0, FFT_R2C=1, FFT_C2R=2};
 
 class PlainFFT {
 public:
   PlainFFT(int kind, long n, int sign, long C, long B, long istride,
            long ibatch, long ostride, long obatch, int prec);
+  ~PlainFFT();
   cudaError_t execute(const void *in, void *out, cudaStream_t s);
   int columnsPerCTA() const {return tile;}
   bool aligned(const void *in, const void *out) const;
+  bool twoPass() const {return n1 > 0;}
 private:
   int kind, sign, prec;
   long n, C, B, istride, ibatch, ostride, obatch;
   int tile;
+  long n1, n2;                 // two-pass factors (0: one pass)
+  int tile1, tile2;
+  void *scratch;               // n x B complex (two-pass only)
   template<typename T> cudaError_t runT(const void *in, void *out,
                                         cudaStream_t s);
+  template<typename T> cudaError_t runTwoPass(const void *in, void *out,
+                                              cudaStream_t s);
 };
 
 const void *twiddles(long n, int prec);

@@ -808,6 +808,37 @@ cudaError_t launchFFScale(const FFScaleArgs& P, cudaStream_t s)
   return cudaGetLastError();
 }
 
+// The origin shift of the fft0 transforms (fftw++.h:144-228, fftw::Shift):
+// the real values of an nx x ny (x nz) array with (i + j) odd (2D: i odd)
+// change sign, which moves the Fourier origin to (nx/2, 0) or
+// (nx/2, ny/2, 0).
+template<typename R>
+__global__ void __launch_bounds__(256) originShiftKernel(R *f, long long nx,
+                                                         long long ny,
+                                                         long long nz)
+{
+  const long long n=nx*ny*nz;
+  const long long stride=(long long) gridDim.x*blockDim.x;
+  for(long long e=blockIdx.x*(long long) blockDim.x+threadIdx.x; e < n;
+      e += stride) {
+    const long long row=e/nz;        // i*ny + j
+    const long long i=row/ny, j=row-i*ny;
+    const long long parity=nz > 1 ? i+j : i;
+    if(parity & 1) f[e]=-f[e];
+  }
+}
+
+cudaError_t launchOriginShift(void *f, long long nx, long long ny,
+                              long long nz, bool f64, cudaStream_t s)
+{
+  const long long n=nx*ny*nz;
+  if(n <= 0) return cudaSuccess;
+  const int grid=(int) std::min<long long>((n+255)/256,152*8);
+  if(f64) originShiftKernel<double><<<grid,256,0,s>>>((double *) f,nx,ny,nz);
+  else originShiftKernel<float><<<grid,256,0,s>>>((float *) f,nx,ny,nz);
+  return cudaGetLastError();
+}
+
 cudaError_t launchBulkCopy(const CopyArgs& P, cudaStream_t s)
 {
   if(P.bytes % 16) return cudaErrorInvalidValue;

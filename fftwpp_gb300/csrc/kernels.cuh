@@ -244,6 +244,11 @@ struct CopyArgs {
 };
 cudaError_t launchBulkCopy(const CopyArgs& P, cudaStream_t s);
 
+// fft0 origin shift: negate the real entries (i, j, k) of an nx x ny x nz
+// array with i + j odd (nz = 1: with i odd).
+cudaError_t launchOriginShift(void *f, long long nx, long long ny,
+                              long long nz, bool f64, cudaStream_t s);
+
 // The innermost-axis launches of a convolution whose multiplier is a
 // caller's device functor: the functor's header (fftwpp_gb300_mult.cuh)
 // implements this interface by instantiating the row kernels with it, and

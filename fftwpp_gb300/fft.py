@@ -9,11 +9,19 @@ take +1 or -1, real-to-complex use -1 and complex-to-real +1.  Every pass
 runs in the hand-written shared-memory kernels of lib_fftwpp.so through
 fgb_fft_* (include/fftwpp_gb300.h); there is no library or CPU fallback.
 
+fft0 / fft0Normalized are the origin-shifted transforms of rcfft2d,
+crfft2d, rcfft3d and crfft3d (Fourier origin at (nx/2, 0) or
+(nx/2, ny/2, 0)): the forward ones negate the entries with i (+ j) odd of
+their real input first, as fftw++ does to its input, the backward ones of
+their real output afterwards; the other classes ignore the shift, as in
+fftw++.h.
+
 Differences from fftw++.h: arrays are torch CUDA tensors (complex128 /
 float64, or complex64 / float32 with precision="f32"); lengths must be
-products of 2, 3, 5 and 7 (even for real transforms) within one CTA's
-shared memory; complex-to-real transforms leave their input intact; the
-fft0 origin-shifted variants are not provided.
+products of 2, 3, 5 and 7 (even for real transforms); real transforms and
+interleaved sequences stay within one CTA's shared memory, while complex
+sequences of any such length (fft1d, mfft1d with stride 1) take two passes;
+complex-to-real transforms leave their input intact.
 """
 from __future__ import annotations
 
@@ -111,6 +119,37 @@ class _Plain:
     def fftNormalized(self, x, out=None, stream=None):
         return self.Normalize(self.fft(x, out, stream))
 
+    # Origin shift (fftw::Shift) of the real side: None for classes that
+    # ignore it, else ("in" | "out", shape of the real array).
+    shift = None
+
+    def _shift(self, t, stream):
+        import torch
+        s = (stream if stream is not None else
+             torch.cuda.current_stream()).cuda_stream
+        dims = list(t.shape) + [1] * (3 - t.dim())
+        rc = self.lib.fgb_fft_origin_shift_device(
+            ctypes.c_void_p(t.data_ptr()), dims[0], dims[1], dims[2],
+            self.prec, ctypes.c_void_p(s))
+        if rc != 0:
+            raise ValueError(_native.last_error())
+
+    def fft0(self, x, out=None, stream=None):
+        """The transform with the Fourier origin shifted to (nx/2, 0) (2D) or
+        (nx/2, ny/2, 0) (3D); the forward real-to-complex classes negate
+        their input's entries with i (+ j) odd in place first, as fftw++
+        does."""
+        if self.shift == "in":
+            self._check(x, self.in_shape, self.in_dtype, "input")
+            self._shift(x, stream)
+        out = self.fft(x, out, stream)
+        if self.shift == "out":
+            self._shift(out, stream)
+        return out
+
+    def fft0Normalized(self, x, out=None, stream=None):
+        return self.Normalize(self.fft0(x, out, stream))
+
 
 def _mgeom(n, M, stride, dist):
     """(C, B, stride, batch) of M sequences at t*dist + s*stride."""
@@ -183,6 +222,8 @@ class fft2d(_Plain):
 class rcfft2d(_Plain):
     """nx x ny reals -> nx x (ny/2+1) complex (the ky >= 0 half plane)."""
 
+    shift = "in"
+
     def __init__(self, nx, ny, precision="f64"):
         h = ny // 2 + 1
         super().__init__((nx, ny), "r", (nx, h), "c",
@@ -192,6 +233,8 @@ class rcfft2d(_Plain):
 
 
 class crfft2d(_Plain):
+    shift = "out"
+
     def __init__(self, nx, ny, precision="f64"):
         h = ny // 2 + 1
         super().__init__((nx, h), "c", (nx, ny), "r",
@@ -210,6 +253,8 @@ class fft3d(_Plain):
 
 
 class rcfft3d(_Plain):
+    shift = "in"
+
     def __init__(self, nx, ny, nz, precision="f64"):
         h = nz // 2 + 1
         super().__init__((nx, ny, nz), "r", (nx, ny, h), "c",
@@ -220,6 +265,8 @@ class rcfft3d(_Plain):
 
 
 class crfft3d(_Plain):
+    shift = "out"
+
     def __init__(self, nx, ny, nz, precision="f64"):
         h = nz // 2 + 1
         super().__init__((nx, ny, h), "c", (nx, ny, nz), "r",

@@ -272,9 +272,12 @@ void fgb_pad_destroy(fgb_pad *t);
  * C interleaved sequences in each of B batches: element s of sequence c in
  * batch b at b*batch + s*stride + c, counted in the element type of each
  * side (stride >= C when C > 1).  n: a product of 2, 3, 5, 7 (even for
- * real transforms) within one CTA's shared memory.  Complex transforms may
- * run in place, real ones only with C == 1.  Device pointers, asynchronous
- * on stream.  No normalisation (fftNormalized divides by n). */
+ * real transforms).  Lengths beyond one CTA's shared memory are taken by
+ * complex transforms of contiguous sequences (C == 1, unit strides) in two
+ * passes through a scratch array the plan allocates (n = n1 n2, the
+ * four-step FFT).  Complex transforms may run in place, real ones only
+ * with C == 1.  Device pointers, asynchronous on stream.  No normalisation
+ * (fftNormalized divides by n). */
 #define FGB_FFT_C2C 0
 #define FGB_FFT_R2C 1
 #define FGB_FFT_C2R 2
@@ -285,6 +288,14 @@ fgb_fft *fgb_fft_create(int kind, size_t n, int sign, size_t C, size_t B,
 int fgb_fft_execute_device(fgb_fft *t, const void *in, void *out,
                            void *stream);
 void fgb_fft_destroy(fgb_fft *t);
+
+/* The origin shift of the fft0 transforms (fftw++.h:144-228, Shift; used by
+ * rcfft2d/crfft2d/rcfft3d/crfft3d::fft0): negate the real values (i, j, k)
+ * of a device array of nx x ny x nz reals with i + j odd (nz == 1: i
+ * odd), which moves the Fourier origin to (nx/2, 0) or (nx/2, ny/2, 0).
+ * nx (and ny in 3D) must be even. */
+int fgb_fft_origin_shift_device(void *f, size_t nx, size_t ny, size_t nz,
+                                int precision, void *stream);
 
 /* Text of the last error on this thread. */
 const char *fgb_last_error(void);

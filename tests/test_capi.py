@@ -169,7 +169,9 @@ def test_plain_fft_plans(native_lib):
                       ((0, 16, 2, 1, 1, 1, 16, 1, 16, 0), "sign"),
                       ((0, 16, 1, 8, 1, 4, 0, 8, 0, 0), "stride >= C"),
                       ((0, 16, 1, 1, 1, 1, 16, 1, 16, 2), "FP64 or FP32"),
-                      ((0, 1 << 16, 1, 1, 1, 1, 1, 1, 1, 0), "too long")]:
+                      ((1, 1 << 16, -1, 1, 1, 1, 1 << 16, 1, 1, 0),
+                       "too long"),
+                      ((0, 1 << 16, 1, 2, 1, 2, 0, 2, 0, 0), "too long")]:
         h = lib.fgb_fft_create(*args)
         if msg is None:
             assert h

@@ -111,3 +111,69 @@ def test_in_place_complex(native_lib):
     t = _dev(x, "f64")
     fft2d(48, 40, -1).fft(t, out=t)
     assert rel_l2(t.cpu().numpy(), np.fft.fft2(x)) <= 1e-14
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("n", [1 << 16, 3 * 5 * 7 * 1024, 1 << 20])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_fft1d_two_pass(native_lib, precision, n, sign):
+    """Lengths beyond one CTA (two passes through the plan's scratch
+    array, the four-step FFT), both signs, in place too."""
+    from fftwpp_gb300.fft import fft1d
+    x = _c(n, n % 97)
+    t = fft1d(n, sign, precision=precision)
+    assert t.passes[0].handle
+    got = t.fft(_dev(x, precision))
+    want = np.fft.fft(x) if sign < 0 else np.fft.ifft(x) * n
+    tol = 1e-13 if precision == "f64" else 4e-6
+    assert rel_l2(got.cpu().numpy(), want) <= tol
+    d = _dev(x, precision)
+    t.fft(d, out=d)
+    assert rel_l2(d.cpu().numpy(), want) <= tol
+
+
+def test_mfft1d_two_pass(native_lib):
+    """Several long contiguous sequences (dist beyond n)."""
+    from fftwpp_gb300.fft import mfft1d
+    n, M, dist = 1 << 15, 3, (1 << 15) + 64
+    t = mfft1d(n, 1, M, 1, dist)
+    x = _c(t.in_shape[0], 4)
+    got = t.fft(_dev(x, "f64")).cpu().numpy()
+    for m in range(M):
+        idx = m * dist + np.arange(n)
+        assert rel_l2(got[idx], np.fft.ifft(x[idx]) * n) <= 1e-13
+
+
+def _shift(r):
+    """fftw::Shift of the real side: (-1)^(i (+ j))."""
+    i = np.arange(r.shape[0])[:, None]
+    if r.ndim == 2:
+        return r * (-1.0) ** i
+    j = np.arange(r.shape[1])[None, :]
+    return r * ((-1.0) ** (i + j))[:, :, None]
+
+
+@pytest.mark.parametrize("shape", [(8, 12), (64, 30), (8, 6, 10)])
+def test_fft0_origin_shift(native_lib, shape):
+    """fft0 of rcfft2d/rcfft3d: the Fourier origin at (nx/2, 0) or
+    (nx/2, ny/2, 0), i.e. the transform of the shifted input; crfft fft0
+    undoes it; the classes without a shift ignore it."""
+    from fftwpp_gb300 import fft as F
+    r = np.random.default_rng(2).normal(size=shape)
+    if len(shape) == 2:
+        fwd, bwd = F.rcfft2d(*shape), F.crfft2d(*shape)
+        want = np.fft.rfft2(_shift(r))
+    else:
+        fwd, bwd = F.rcfft3d(*shape), F.crfft3d(*shape)
+        want = np.fft.rfftn(_shift(r))
+    d = _dev(r, "f64", True)
+    got = fwd.fft0(d)
+    assert rel_l2(got.cpu().numpy(), want) <= 1e-14
+    assert rel_l2(d.cpu().numpy(), _shift(r)) == 0     # shifted in place
+    back = bwd.fft0Normalized(got).cpu().numpy()
+    assert rel_l2(back, r) <= 1e-14
+    c = F.fft2d(8, 12, -1)
+    x = _c((8, 12), 3)
+    assert rel_l2(c.fft0(_dev(x, "f64")).cpu().numpy(), np.fft.fft2(x)) <= 1e-14
+    with pytest.raises(ValueError):
+        F.rcfft2d(7, 12).fft0(_dev(np.zeros((7, 12)), "f64", True))
