@@ -104,7 +104,11 @@ __device__ __forceinline__ ff ffDot2(ff a, ff b, ff c, ff d)
 }
 
 template<typename T> struct cplx { T x, y; };
-// Float-float complex values move as one 16-byte vector.
+// Complex values move as one vector (8 bytes for FP32, 16 for FP64 and
+// float-float): aligned to their size, so every shared and global access of
+// an element is a single 64- or 128-bit load or store.
+template<> struct __align__(8) cplx<float> { float x, y; };
+template<> struct __align__(16) cplx<double> { double x, y; };
 template<> struct __align__(16) cplx<ff> { ff x, y; };
 
 template<typename T> struct TwT;
