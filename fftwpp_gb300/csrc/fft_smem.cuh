@@ -21,6 +21,8 @@
 
 #include "complex.cuh"
 
+#include <type_traits>
+
 namespace fgb {
 
 #define FGB_MAXSTAGES 20
@@ -126,6 +128,11 @@ template<int S, typename T> struct Codelet<8,S,T> {
   }
 };
 
+// FP64 radix 8 and 3 without twiddles: the constant rotations fused into
+// the combining additions (see the fused butterflies below).
+template<int S> struct Codelet<8,S,double>;
+template<int S> struct Codelet<3,S,double>;
+
 template<int S, typename T> struct Codelet<3,S,T> {
   static __device__ __forceinline__ void run(cplx<T> *a) {
     const T c=(T) -0.5;
@@ -186,6 +193,170 @@ template<int S, typename T> struct Codelet<7,S,T> {
   }
 };
 
+// ---------------------------------------------------------------------------
+// FP64 butterflies with the twiddles of their inputs fused in (the FP64
+// kernels are bound by GB300's FP64 pipe, so every DADD/DMUL/DFMA saved is
+// time saved).  Two rules do it: a + w b is four DFMAs (fmaTw) instead of a
+// multiply and an add, and the difference a - w b of a pair is taken from
+// its sum s as 2a - s (one DFMA per component).  Radix 2, 3, 4 and 8 take
+// 6, 18, 24 and 72 FP64 instructions with their twiddles, against 8, 22,
+// 28 and 84 for a twiddle multiply per input followed by the plain
+// butterfly; radix 8 and 3 without twiddles take 52 and 12 (56 and 14):
+// the rotations by W_8 and the sqrt(3)/2 terms go into the combining
+// additions as DFMAs.
+
+// acc + a w^S (w a stored twiddle exp(+i theta)): four DFMAs.
+template<int S>
+__device__ __forceinline__ cplx<double> fmaTw(cplx<double> acc, cplx<double> a,
+                                              double2 w)
+{
+  const double wy=S > 0 ? w.y : -w.y;
+  return mk(fma(a.x,w.x,fma(-a.y,wy,acc.x)),fma(a.y,w.x,fma(a.x,wy,acc.y)));
+}
+
+// 2a - s: the difference a - b of a pair from its sum s = a + b.
+__device__ __forceinline__ cplx<double> twoMinus(cplx<double> a,
+                                                 cplx<double> s)
+{
+  return mk(fma(2.0,a.x,-s.x),fma(2.0,a.y,-s.y));
+}
+
+// Radix 4 on (a0, a1 w1, a2 w2, a3 w3), a0 untwiddled.
+template<int S>
+__device__ __forceinline__ void tw4(cplx<double> *o, cplx<double> a0,
+                                    cplx<double> a1, double2 w1,
+                                    cplx<double> a2, double2 w2,
+                                    cplx<double> a3, double2 w3)
+{
+  const cplx<double> s02=fmaTw<S>(a0,a2,w2);
+  const cplx<double> d02=twoMinus(a0,s02);
+  const cplx<double> b1=twmul<S>(a1,w1);
+  const cplx<double> s13=fmaTw<S>(b1,a3,w3);
+  const cplx<double> d13=mulI<S>(twoMinus(b1,s13));
+  o[0]=s02+s13;
+  o[2]=s02-s13;
+  o[1]=d02+d13;
+  o[3]=d02-d13;
+}
+
+// The last layer of radix 8 from the radix-4 transforms e (even inputs)
+// and o (odd inputs): a[k] = e[k] + W_8^{S k} o[k], a[k+4] = e[k] - ...
+template<int S>
+__device__ __forceinline__ void combine8(cplx<double> *a, const cplx<double> *e,
+                                         const cplx<double> *o)
+{
+  const double h=FGB_SQRT1_2;
+  a[0]=e[0]+o[0];
+  a[4]=e[0]-o[0];
+  const cplx<double> o2=mulI<S>(o[2]);
+  a[2]=e[2]+o2;
+  a[6]=e[2]-o2;
+  // W_8^{S} o1 = h (p + i q); W_8^{3S} o3 = h (-u + i v) (S > 0) or
+  // h (u' - i v') (S < 0).
+  const double p=S > 0 ? o[1].x-o[1].y : o[1].x+o[1].y;
+  const double q=S > 0 ? o[1].y+o[1].x : o[1].y-o[1].x;
+  a[1]=mk(fma(h,p,e[1].x),fma(h,q,e[1].y));
+  a[5]=mk(fma(-h,p,e[1].x),fma(-h,q,e[1].y));
+  if(S > 0) {
+    const double u=o[3].x+o[3].y, v=o[3].x-o[3].y;
+    a[3]=mk(fma(-h,u,e[3].x),fma(h,v,e[3].y));
+    a[7]=mk(fma(h,u,e[3].x),fma(-h,v,e[3].y));
+  } else {
+    const double u=o[3].y-o[3].x, v=o[3].x+o[3].y;
+    a[3]=mk(fma(h,u,e[3].x),fma(-h,v,e[3].y));
+    a[7]=mk(fma(-h,u,e[3].x),fma(h,v,e[3].y));
+  }
+}
+
+template<int S>
+__device__ __forceinline__ void radix3(cplx<double> *a, cplx<double> t,
+                                       cplx<double> d)
+{
+  const double s=S*FGB_SQRT3_2;
+  const cplx<double> b=mk(fma(-0.5,t.x,a[0].x),fma(-0.5,t.y,a[0].y));
+  a[0]=a[0]+t;
+  a[1]=mk(fma(-s,d.y,b.x),fma(s,d.x,b.y));
+  a[2]=mk(fma(s,d.y,b.x),fma(-s,d.x,b.y));
+}
+
+template<int R, int S> struct TwButterfly;   // a[r] *= w[r] (r >= 1), DFT
+
+template<int S> struct TwButterfly<2,S> {
+  static __device__ __forceinline__ void run(cplx<double> *a, const double2 *w) {
+    const cplx<double> b=fmaTw<S>(a[0],a[1],w[1]);
+    a[1]=twoMinus(a[0],b);
+    a[0]=b;
+  }
+};
+
+template<int S> struct TwButterfly<4,S> {
+  static __device__ __forceinline__ void run(cplx<double> *a, const double2 *w) {
+    cplx<double> o[4];
+    tw4<S>(o,a[0],a[1],w[1],a[2],w[2],a[3],w[3]);
+    a[0]=o[0]; a[1]=o[1]; a[2]=o[2]; a[3]=o[3];
+  }
+};
+
+template<int S> struct TwButterfly<8,S> {
+  static __device__ __forceinline__ void run(cplx<double> *a, const double2 *w) {
+    cplx<double> e[4], o[4];
+    tw4<S>(e,a[0],a[2],w[2],a[4],w[4],a[6],w[6]);
+    tw4<S>(o,twmul<S>(a[1],w[1]),a[3],w[3],a[5],w[5],a[7],w[7]);
+    combine8<S>(a,e,o);
+  }
+};
+
+template<int S> struct TwButterfly<3,S> {
+  static __device__ __forceinline__ void run(cplx<double> *a, const double2 *w) {
+    const cplx<double> b1=twmul<S>(a[1],w[1]);
+    const cplx<double> t=fmaTw<S>(b1,a[2],w[2]);
+    radix3<S>(a,t,twoMinus(b1,t));
+  }
+};
+
+// Whether a fused butterfly serves (T, R).
+template<typename T, int R> __host__ __device__ constexpr bool fusedTw()
+{
+  return std::is_same<T,double>::value && (R == 2 || R == 3 || R == 4 ||
+                                           R == 8);
+}
+
+// Inputs r >= 1 multiplied by tw[r*step] (S: its conjugate for S < 0),
+// then the radix-R DFT.
+template<int S> struct Codelet<8,S,double> {
+  static __device__ __forceinline__ void run(cplx<double> *a) {
+    cplx<double> e[4]={a[0],a[2],a[4],a[6]};
+    cplx<double> o[4]={a[1],a[3],a[5],a[7]};
+    Codelet<4,S,double>::run(e);
+    Codelet<4,S,double>::run(o);
+    combine8<S>(a,e,o);
+  }
+};
+
+template<int S> struct Codelet<3,S,double> {
+  static __device__ __forceinline__ void run(cplx<double> *a) {
+    const cplx<double> t=a[1]+a[2];
+    radix3<S>(a,t,a[1]-a[2]);
+  }
+};
+
+template<typename T, int R, int S>
+__device__ __forceinline__ void twiddledDFT(cplx<T> *a,
+                                            const typename TwT<T>::type *tw,
+                                            int step)
+{
+  if constexpr(fusedTw<T,R>()) {
+    double2 w[R];
+#pragma unroll
+    for(int r=1; r < R; ++r) w[r]=tw[r*step];
+    TwButterfly<R,S>::run(a,w);
+  } else {
+#pragma unroll
+    for(int r=1; r < R; ++r) a[r]=twmul<S>(a[r],tw[r*step]);
+    Codelet<R,S,T>::run(a);
+  }
+}
+
 template<typename T, int R, int S>
 __device__ __forceinline__ void fftStage(const cplx<T> *__restrict__ x,
                                          cplx<T> *__restrict__ y,
@@ -211,11 +382,8 @@ __device__ __forceinline__ void fftStage(const cplx<T> *__restrict__ x,
     for(int r=0; r < R; ++r) a[r]=nrm(x[sp((j+r*nR)*ld+c)]);
     // Uniform per stage: the first stage has no twiddles; later stages apply
     // them to every element (W^0 = 1 exactly, so k = 0 needs no branch).
-    if(Ns > 1) {
-#pragma unroll
-      for(int r=1; r < R; ++r) a[r]=twmul<S>(a[r],tw[r*k*tstride]);
-    }
-    Codelet<R,S,T>::run(a);
+    if(Ns > 1) twiddledDFT<T,R,S>(a,tw,k*tstride);
+    else Codelet<R,S,T>::run(a);
     int base=(j-k)*R+k;
 #pragma unroll
     for(int r=0; r < R; ++r) y[sp((base+r*Ns)*ld+c)]=a[r];
@@ -283,11 +451,8 @@ __device__ __forceinline__ void ipStage(cplx<T> *__restrict__ x, int n, int Ls,
     cplx<T> a[R];
 #pragma unroll
     for(int r=0; r < R; ++r) a[r]=nrm(x[sp((base+r*m)*ld+c)]);
-    if(!DIF && m > 1) {
-#pragma unroll
-      for(int r=1; r < R; ++r) a[r]=twmul<S>(a[r],tw[r*j*tstride]);
-    }
-    Codelet<R,S,T>::run(a);
+    if(!DIF && m > 1) twiddledDFT<T,R,S>(a,tw,j*tstride);
+    else Codelet<R,S,T>::run(a);
     if(DIF && m > 1) {
 #pragma unroll
       for(int r=1; r < R; ++r) a[r]=twmul<S>(a[r],tw[r*j*tstride]);

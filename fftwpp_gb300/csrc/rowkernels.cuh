@@ -711,12 +711,14 @@ hermRowKernel(const HermRowPlan<T> P, const Mul mul)
   // Rows g*R .. g*R+R-1 are transformed together; column col = a*R + rho.
   for(long long g=blockIdx.x; g < groups; g += gridDim.x) {
     const long long row0=g*R;
-    // Y[k] = (Z[k] + conj Z[Nh-k]) + i W_N^k (Z[k] - conj Z[Nh-k]), with
-    // Z read from the row itself (the two reads of an element are L1/L2
-    // hits; every read of the group precedes its writes, so in = out is
-    // safe).
+    // Y[k] = S + i W_N^k D with S = Z[k] + conj Z[Nh-k], D = Z[k] -
+    // conj Z[Nh-k], Z read from the row itself.  One thread forms the pair
+    // k, Nh-k from the same two loads: Y[Nh-k] = conj(S) + i conj(W_N^k D)
+    // (since W_N^{Nh} = -1), so the pair costs one twiddle multiply.
+    // Every read of the group precedes its writes, so in = out is safe.
     // The loads of FGB_LOADS iterations are issued before any is used.
-    for(int i0=tid; i0 < Nh*ld; i0 += FGB_LOADS*nthr) {
+    const int np=Nh/2+1;                 // k = 0 .. floor(Nh/2)
+    for(int i0=tid; i0 < np*ld; i0 += FGB_LOADS*nthr) {
       cplx<T> zk[FGB_LOADS], zc[FGB_LOADS];
 #pragma unroll
       for(int u=0; u < FGB_LOADS; ++u) {
@@ -725,7 +727,7 @@ hermRowKernel(const HermRowPlan<T> P, const Mul mul)
         int a=dR(col);
         long long row=row0+col-a*R;
         const cplx<T> *zr=P.in[a]+row*P.rowStride;
-        const bool live=i < Nh*ld && row < P.nrows;
+        const bool live=i < np*ld && row < P.nrows;
         const int kk=Nh-k;
         const int sh=ioShift<T>(P.ioShift,a);
         zk[u]=live && k < H ? loadIO(zr+k,P.io64 & 1,sh) : mk((T) 0,(T) 0);
@@ -734,14 +736,16 @@ hermRowKernel(const HermRowPlan<T> P, const Mul mul)
 #pragma unroll
       for(int u=0; u < FGB_LOADS; ++u) {
         const int i=i0+u*nthr;
-        if(i >= Nh*ld) break;
-        const int k=dLd(i);
+        if(i >= np*ld) break;
+        const int k=dLd(i), col=i-k*ld;
         cplx<T> a=zk[u];
         if(k == 0) a.y=(T) 0;
-        cplx<T> b=conjg(zc[u]);
-        cplx<T> s=a+b;
-        cplx<T> d=twmul<1>(a-b,tw[k]);
-        x[sp(i)]=mk(s.x-d.y,s.y+d.x);
+        const cplx<T> b=conjg(zc[u]);
+        const cplx<T> S=a+b;
+        const cplx<T> Pw=twmul<1>(a-b,tw[k]);
+        x[sp(i)]=mk(S.x-Pw.y,S.y+Pw.x);
+        if(k != 0 && 2*k != Nh)
+          x[sp((Nh-k)*ld+col)]=mk(S.x+Pw.y,Pw.x-S.y);
       }
     }
     __syncthreads();
@@ -765,21 +769,26 @@ hermRowKernel(const HermRowPlan<T> P, const Mul mul)
       __syncthreads();
       Z=fftSmem<T,-1>(X,Y,P.fp,lb,ld,tid,nthr);
     }
-    // V[k] = E[k] + W_N^{-k} O[k],  E=(Zk+conj Zm)/2, O=(Zk-conj Zm)/(2i)
+    // V[k] = (s + Q)/2 with s = Z[k] + conj Z[m], Q = W_N^{-k} (-i)(Z[k] -
+    // conj Z[m]), m = Nh-k (m = 0 for k = 0).  When both k and Nh-k are
+    // stored modes the lower one also writes V[Nh-k] = conj(s - Q)/2, and
+    // the upper one skips.
+    const T hs=half*P.scale;
     for(int i=tid; i < lb*H; i += nthr) {
       int col=dH(i), k=i-col*H;
       int b=dR(col);
       long long row=row0+col-b*R;
-      if(row >= P.nrows) continue;
-      cplx<T> zk=Z[sp(k*ld+col)];
-      int km=k == 0 ? 0 : Nh-k;
-      cplx<T> zm=conjg(Z[sp(km*ld+col)]);
-      cplx<T> e=(zk+zm)*half;
-      cplx<T> dd=zk-zm;
-      cplx<T> o=mk(dd.y*half,-dd.x*half);
-      cplx<T> v=e+twmul<-1>(o,tw[k]);
-      storeIO(P.out[b]+row*P.rowStride+k,v*P.scale,P.io64 & 2,
-              ioShift<T>(P.ioShift,8+b));
+      const int km=k == 0 ? 0 : Nh-k;
+      const bool pair=k != 0 && km < H && km != k;
+      if(row >= P.nrows || (pair && km < k)) continue;
+      const cplx<T> zk=Z[sp(k*ld+col)];
+      const cplx<T> zm=conjg(Z[sp(km*ld+col)]);
+      const cplx<T> sum=zk+zm, dd=zk-zm;
+      const cplx<T> Q=twmul<-1>(mk(dd.y,-dd.x),tw[k]);
+      cplx<T> *o=P.out[b]+row*P.rowStride;
+      const int sh=ioShift<T>(P.ioShift,8+b);
+      storeIO(o+k,(sum+Q)*hs,P.io64 & 2,sh);
+      if(pair) storeIO(o+km,conjg(sum-Q)*hs,P.io64 & 2,sh);
     }
     __syncthreads();
   }
