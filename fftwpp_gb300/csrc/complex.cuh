@@ -126,6 +126,23 @@ __device__ __forceinline__ cplx<T> operator-(cplx<T> a, cplx<T> b) { return mk(a
 template<typename T>
 __device__ __forceinline__ cplx<T> operator*(cplx<T> a, T s) { return mk(a.x*s,a.y*s); }
 
+// FP32 complex values as float2 pairs for the packed FP32 instructions of
+// sm_100-class GPUs (one FADD2 / FMUL2 / FFMA2 does both components).
+__device__ __forceinline__ float2 f2(cplx<float> a) {return make_float2(a.x,a.y);}
+__device__ __forceinline__ cplx<float> c2(float2 v) {return mk(v.x,v.y);}
+__device__ __forceinline__ cplx<float> operator+(cplx<float> a, cplx<float> b)
+{
+  return c2(__fadd2_rn(f2(a),f2(b)));
+}
+__device__ __forceinline__ cplx<float> operator-(cplx<float> a, cplx<float> b)
+{
+  return c2(__fadd2_rn(f2(a),make_float2(-b.x,-b.y)));
+}
+__device__ __forceinline__ cplx<float> operator*(cplx<float> a, float s)
+{
+  return c2(__fmul2_rn(f2(a),make_float2(s,s)));
+}
+
 template<typename T>
 __device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b)
 {
@@ -189,14 +206,18 @@ __device__ __forceinline__ cplx<double> twmul(cplx<double> a, double2 w)
 template<int S>
 __device__ __forceinline__ cplx<float> twmul(cplx<float> a, float4 w)
 {
-  // (hi + lo) applied as a*lo first, then the dominant a*hi term fused in.
-  float wy=S > 0 ? w.y : -w.y;
-  float ly=S > 0 ? w.w : -w.w;
-  float rx=fmaf(a.x,w.z,-a.y*ly);
-  float ry=fmaf(a.x,ly,a.y*w.z);
-  rx=fmaf(a.x,w.x,fmaf(-a.y,wy,rx));
-  ry=fmaf(a.x,wy,fmaf(a.y,w.x,ry));
-  return mk(rx,ry);
+  // (hi + lo) applied as a*lo first, then the dominant a*hi term fused in;
+  // both components at once with the packed FP32 instructions, in the
+  // rounding order of the scalar form rx = ax wx + (-ay wy + (ax lx +
+  // (-ay ly))), ry likewise.
+  const float wy=S > 0 ? w.y : -w.y;
+  const float ly=S > 0 ? w.w : -w.w;
+  const float2 ax=make_float2(a.x,a.x), ay=make_float2(a.y,a.y);
+  float2 r=__fmul2_rn(ay,make_float2(-ly,w.z));
+  r=__ffma2_rn(ax,make_float2(w.z,ly),r);
+  r=__ffma2_rn(ay,make_float2(-wy,w.x),r);
+  r=__ffma2_rn(ax,make_float2(w.x,wy),r);
+  return c2(r);
 }
 
 template<int S>

@@ -737,13 +737,33 @@ __global__ void __launch_bounds__(256) ffScaleKernel(const FFScaleArgs P)
 {
   __shared__ bool last;
   const long long stride=(long long) gridDim.x*blockDim.x;
+  const long long first=blockIdx.x*(long long) blockDim.x+threadIdx.x;
   for(int a=0; a < P.count; ++a) {
     unsigned m=0;
-    for(long long i=blockIdx.x*(long long) blockDim.x+threadIdx.x; i < P.n;
-        i += stride) {
-      const unsigned e=(unsigned) ((__ldg(P.in[a]+i) >> 52) & 0x7ff);
+    auto take=[&](unsigned long long b) {
+      const unsigned e=(unsigned) ((b >> 52) & 0x7ff);
       if(e != 0x7ff && e > m) m=e;
+    };
+    const unsigned long long *in=P.in[a];
+    long long i0=0;
+    if(((size_t) in & 15) == 0) {
+      // Two doubles per 16-byte load, four loads in flight per thread.
+      const ulonglong2 *v=(const ulonglong2 *) in;
+      const long long n2=P.n/2;
+      long long i=first;
+      for(; i+3*stride < n2; i += 4*stride) {
+        const ulonglong2 b0=__ldg(v+i), b1=__ldg(v+i+stride),
+          b2=__ldg(v+i+2*stride), b3=__ldg(v+i+3*stride);
+        take(b0.x); take(b0.y); take(b1.x); take(b1.y);
+        take(b2.x); take(b2.y); take(b3.x); take(b3.y);
+      }
+      for(; i < n2; i += stride) {
+        const ulonglong2 b=__ldg(v+i);
+        take(b.x); take(b.y);
+      }
+      i0=2*n2;
     }
+    for(long long i=i0+first; i < P.n; i += stride) take(__ldg(in+i));
     m=__reduce_max_sync(0xffffffffu,m);
     if((threadIdx.x & 31) == 0 && m) atomicMax((unsigned *) P.state+a,m);
   }
@@ -802,8 +822,8 @@ __global__ void __launch_bounds__(256) ffScaleKernel(const FFScaleArgs P)
 cudaError_t launchFFScale(const FFScaleArgs& P, cudaStream_t s)
 {
   if(P.count < 1 || P.count > FGB_MAXA || P.n < 1) return cudaErrorInvalidValue;
-  long long blocks=(P.n+255)/256;
-  const int grid=(int) std::min<long long>(blocks,152*4);
+  long long blocks=(P.n/8+255)/256;
+  const int grid=(int) std::max<long long>(1,std::min<long long>(blocks,152*8));
   ffScaleKernel<<<grid,256,0,s>>>(P);
   return cudaGetLastError();
 }
