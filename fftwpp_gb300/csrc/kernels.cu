@@ -736,6 +736,7 @@ __global__ void __launch_bounds__(256) bulkCopyKernel(CopyArgs P)
 __global__ void __launch_bounds__(256) ffScaleKernel(const FFScaleArgs P)
 {
   __shared__ bool last;
+  __shared__ unsigned wmax[8];
   const long long stride=(long long) gridDim.x*blockDim.x;
   const long long first=blockIdx.x*(long long) blockDim.x+threadIdx.x;
   for(int a=0; a < P.count; ++a) {
@@ -764,8 +765,17 @@ __global__ void __launch_bounds__(256) ffScaleKernel(const FFScaleArgs P)
       i0=2*n2;
     }
     for(long long i=i0+first; i < P.n; i += stride) take(__ldg(in+i));
+    // Block maximum first (warp reduction, then across the warps), so that
+    // one atomic per block and array reaches the shared accumulator.
     m=__reduce_max_sync(0xffffffffu,m);
-    if((threadIdx.x & 31) == 0 && m) atomicMax((unsigned *) P.state+a,m);
+    if((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5]=m;
+    __syncthreads();
+    if(threadIdx.x < 32) {
+      unsigned v=threadIdx.x < (blockDim.x+31)/32 ? wmax[threadIdx.x] : 0u;
+      v=__reduce_max_sync(0xffffffffu,v);
+      if(threadIdx.x == 0 && v) atomicMax((unsigned *) P.state+a,v);
+    }
+    __syncthreads();
   }
   __threadfence();
   __syncthreads();
