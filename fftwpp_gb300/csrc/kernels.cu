@@ -721,11 +721,13 @@ __global__ void __launch_bounds__(256) bulkCopyKernel(CopyArgs P)
   }
 }
 
-// Float-float range guard (kernels.cuh, FFScaleArgs).  Every block takes
-// the largest biased exponent of its share of each array (integer work on
-// the bit patterns, no FP64 pipe; infinities and NaNs ignored) into
-// state[a]; the last block to finish (a wrapping counter in state[8])
-// turns them into the scales and zeroes the accumulators.  Multipliers
+// Float-float range guard (kernels.cuh, FFScaleArgs).  Block b takes the
+// largest biased exponent of chunk b % chunks of array b / chunks (integer
+// work on the bit patterns, no FP64 pipe; infinities and NaNs ignored)
+// into state[a]; the last block to finish (a wrapping counter in state[8])
+// turns them into the scales and zeroes the accumulators.  A chunk is
+// FGB_SCAN_CHUNK doubles, all of a thread's loads issued before any is
+// used, so the whole scan is one round trip to HBM per wave.  Multipliers
 // whose every output is one product of two inputs (or one input) take a
 // scale per input, and the output scale is the sum (binary, correlation,
 // the Jacobian adjoint).  Those whose outputs add products take one scale
@@ -733,49 +735,54 @@ __global__ void __launch_bounds__(256) bulkCopyKernel(CopyArgs P)
 // u0 u3 - u1 u2 shares a scale between u0 and u1 and one between u2 and u3
 // (the derivatives of psi and of omega), a dot product sum_k u_k u_{K+k}
 // one per half.  A caller's functor gets no scaling.
+#define FGB_SCAN_CHUNK 2048
 __global__ void __launch_bounds__(256) ffScaleKernel(const FFScaleArgs P)
 {
   __shared__ bool last;
   __shared__ unsigned wmax[8];
-  const long long stride=(long long) gridDim.x*blockDim.x;
-  const long long first=blockIdx.x*(long long) blockDim.x+threadIdx.x;
-  for(int a=0; a < P.count; ++a) {
-    unsigned m=0;
-    auto take=[&](unsigned long long b) {
-      const unsigned e=(unsigned) ((b >> 52) & 0x7ff);
-      if(e != 0x7ff && e > m) m=e;
-    };
-    const unsigned long long *in=P.in[a];
-    long long i0=0;
-    if(((size_t) in & 15) == 0) {
-      // Two doubles per 16-byte load, four loads in flight per thread.
-      const ulonglong2 *v=(const ulonglong2 *) in;
-      const long long n2=P.n/2;
-      long long i=first;
-      for(; i+3*stride < n2; i += 4*stride) {
-        const ulonglong2 b0=__ldg(v+i), b1=__ldg(v+i+stride),
-          b2=__ldg(v+i+2*stride), b3=__ldg(v+i+3*stride);
-        take(b0.x); take(b0.y); take(b1.x); take(b1.y);
-        take(b2.x); take(b2.y); take(b3.x); take(b3.y);
-      }
-      for(; i < n2; i += stride) {
-        const ulonglong2 b=__ldg(v+i);
-        take(b.x); take(b.y);
-      }
-      i0=2*n2;
+  const long long chunks=(P.n+FGB_SCAN_CHUNK-1)/FGB_SCAN_CHUNK;
+  const int a=(int) (blockIdx.x/chunks);
+  const long long c0=(blockIdx.x-a*chunks)*FGB_SCAN_CHUNK;
+  const long long c1=min(c0+FGB_SCAN_CHUNK,P.n);
+  const unsigned long long *src=P.in[a];
+  unsigned m=0;
+  auto take=[&](unsigned long long b) {
+    const unsigned e=(unsigned) ((b >> 52) & 0x7ff);
+    if(e != 0x7ff && e > m) m=e;
+  };
+  if(((size_t) src & 15) == 0) {
+    // Pairs of doubles by 16-byte loads (four per thread); an odd last
+    // double is read alone.
+    const ulonglong2 *v=(const ulonglong2 *) src;
+    const long long p0=c0/2, p1=c1/2;
+    ulonglong2 b[FGB_SCAN_CHUNK/512];
+#pragma unroll
+    for(int u=0; u < FGB_SCAN_CHUNK/512; ++u) {
+      const long long i=p0+threadIdx.x+u*256;
+      b[u]=i < p1 ? __ldg(v+i) : make_ulonglong2(0,0);
     }
-    for(long long i=i0+first; i < P.n; i += stride) take(__ldg(in+i));
-    // Block maximum first (warp reduction, then across the warps), so that
-    // one atomic per block and array reaches the shared accumulator.
-    m=__reduce_max_sync(0xffffffffu,m);
-    if((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5]=m;
-    __syncthreads();
-    if(threadIdx.x < 32) {
-      unsigned v=threadIdx.x < (blockDim.x+31)/32 ? wmax[threadIdx.x] : 0u;
-      v=__reduce_max_sync(0xffffffffu,v);
-      if(threadIdx.x == 0 && v) atomicMax((unsigned *) P.state+a,v);
+#pragma unroll
+    for(int u=0; u < FGB_SCAN_CHUNK/512; ++u) {take(b[u].x); take(b[u].y);}
+    if((c1 & 1) && threadIdx.x == 0) take(__ldg(src+c1-1));
+  } else {
+    unsigned long long b[FGB_SCAN_CHUNK/256];
+#pragma unroll
+    for(int u=0; u < FGB_SCAN_CHUNK/256; ++u) {
+      const long long i=c0+threadIdx.x+u*256;
+      b[u]=i < c1 ? __ldg(src+i) : 0ull;
     }
-    __syncthreads();
+#pragma unroll
+    for(int u=0; u < FGB_SCAN_CHUNK/256; ++u) take(b[u]);
+  }
+  // Block maximum (warp reduction, then across the warps): one atomic per
+  // block reaches the shared accumulator of its array.
+  m=__reduce_max_sync(0xffffffffu,m);
+  if((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5]=m;
+  __syncthreads();
+  if(threadIdx.x < 32) {
+    unsigned v=threadIdx.x < (blockDim.x+31)/32 ? wmax[threadIdx.x] : 0u;
+    v=__reduce_max_sync(0xffffffffu,v);
+    if(threadIdx.x == 0 && v) atomicMax((unsigned *) P.state+a,v);
   }
   __threadfence();
   __syncthreads();
@@ -832,9 +839,9 @@ __global__ void __launch_bounds__(256) ffScaleKernel(const FFScaleArgs P)
 cudaError_t launchFFScale(const FFScaleArgs& P, cudaStream_t s)
 {
   if(P.count < 1 || P.count > FGB_MAXA || P.n < 1) return cudaErrorInvalidValue;
-  long long blocks=(P.n/8+255)/256;
-  const int grid=(int) std::max<long long>(1,std::min<long long>(blocks,152*8));
-  ffScaleKernel<<<grid,256,0,s>>>(P);
+  const long long blocks=(P.n+FGB_SCAN_CHUNK-1)/FGB_SCAN_CHUNK*P.count;
+  if(blocks > INT_MAX) return cudaErrorInvalidValue;
+  ffScaleKernel<<<(unsigned) blocks,256,0,s>>>(P);
   return cudaGetLastError();
 }
 
