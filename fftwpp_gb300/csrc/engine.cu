@@ -169,7 +169,8 @@ const void *twiddles(long n, int prec)
 // earlier radices to be powers of two (odd radices last); the in-place
 // decimation forms want the spans n/(R0...Rs) to be powers of two (odd
 // radices first).  Either way the stage divisions become shifts.
-static FFTPlanDev fftPlan(long n, int prec, bool oddFirst=false)
+static FFTPlanDev fftPlan(long n, int prec, bool oddFirst=false,
+                          bool allow16=false)
 {
   if(!smooth(n))
     throw std::runtime_error("transform length "+std::to_string(n)+
@@ -178,7 +179,15 @@ static FFTPlanDev fftPlan(long n, int prec, bool oddFirst=false)
   p.n=(int) n;
   p.nst=0;
   long r=n;
-  // Largest radices first: 8, then 4 or 2, then odd primes.
+  // Largest radices first: 8, then 4 or 2, then odd primes.  FP32 in-place
+  // row transforms (allow16) also take radix 16 (4 x 4 in registers) where
+  // that saves a stage: a power-of-two factor 2^k takes ceil(k/3) stages of
+  // radix <= 8 but s = ceil(k/4) of radix <= 16, as k - 3s radix-16 stages
+  // and the rest radix 8.
+  int k2=0;
+  for(long t=n; t % 2 == 0; t /= 2) ++k2;
+  if(allow16 && prec == PREC_F32 && oddFirst && (k2+3)/4 < (k2+2)/3)
+    for(int i=0; i < k2-3*((k2+3)/4); ++i) {p.radix[p.nst++]=16; r /= 16;}
   while(r % 8 == 0) {p.radix[p.nst++]=8; r /= 8;}
   if(r % 4 == 0) {p.radix[p.nst++]=4; r /= 4;}
   if(r % 2 == 0) {p.radix[p.nst++]=2; r /= 2;}
@@ -1008,7 +1017,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.rpc=I.axis[I.dim-1].rpc;
     P.io64=0;
     P.direct=a.q == 1 && a.stored <= a.m;
-    P.fp=fftPlan(a.m,I.prec,inplaceFFT<T>() || P.direct);
+    P.fp=fftPlan(a.m,I.prec,inplaceFFT<T>() || P.direct,true);
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };
   auto hermPlan=[&](HermRowPlan<T>& P, const AxisPlan& a) {
@@ -1018,7 +1027,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.A=A; P.B=B; P.mult=I.mult;
     P.rpc=a.rpc;
     P.io64=0;
-    P.fp=fftPlan(a.N/2,I.prec,inplaceFFT<T>());
+    P.fp=fftPlan(a.N/2,I.prec,inplaceFFT<T>(),true);
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
   };
   auto outerPlan=[&](OuterPlan<T>& P, const AxisPlan& a) {
@@ -1277,7 +1286,7 @@ cudaError_t Conv::runLong(const void *const *in, void *const *out,
   P.L=(int) m; P.m=(int) m; P.q=1; P.N=(int) m; P.cshift=0;
   P.A=A; P.B=B; P.mult=I.mult; P.realIO=0;
   P.rpc=a.rpc; P.io64=0; P.direct=1; P.ioShift=NULL;
-  P.fp=fftPlan(m,I.prec,true);
+  P.fp=fftPlan(m,I.prec,true,true);
   P.twN=(const typename TwT<T>::type *) twiddles(m,I.prec);
   for(int i=0; i < A; ++i) P.in[i]=(const Cx *) lb[i];
   for(int i=0; i < B; ++i) P.out[i]=(Cx *) lb[i];

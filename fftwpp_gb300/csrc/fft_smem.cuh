@@ -68,6 +68,14 @@ struct FFTPlanDev {
   const void *tw;         // TwT<T>::type[n]
 };
 
+// Whether a plan holds a radix-16 stage (its kernels need the R16 form).
+inline bool hasRadix16(const FFTPlanDev& p)
+{
+  for(int s=0; s < p.nst; ++s)
+    if(p.radix[s] == 16) return true;
+  return false;
+}
+
 // Radix constants (exact decimal expansions of the algebraic values).
 #define FGB_SQRT1_2 0.707106781186547524400844362105
 #define FGB_SQRT3_2 0.866025403784438646763723170753
@@ -124,6 +132,47 @@ template<int S, typename T> struct Codelet<8,S,T> {
     for(int k=0; k < 4; ++k) {
       a[k]=e[k]+o[k];
       a[k+4]=e[k]-o[k];
+    }
+  }
+};
+
+// Radix 16 as 4 x 4 (FP32 in-place transforms of row kernels compiled
+// with it): radix-4 over the inputs k + 4r, the products with W_16^{ks},
+// radix-4 over k; outputs in natural order.
+#define FGB_C161 0.923879532511286756128183189397
+#define FGB_S161 0.382683432365089771728459984030
+template<int S, typename T> struct Codelet<16,S,T> {
+  static __device__ __forceinline__ cplx<T> rot(cplx<T> a, T c, T s) {
+    // a (c + i S s)
+    const T ss=(T) S*s;
+    return mk(fma(a.x,c,-a.y*ss),fma(a.x,ss,a.y*c));
+  }
+  static __device__ __forceinline__ void run(cplx<T> *a) {
+    const T h=(T) FGB_SQRT1_2, c1=(T) FGB_C161, s1=(T) FGB_S161;
+    cplx<T> b[4][4];
+#pragma unroll
+    for(int k=0; k < 4; ++k) {
+      cplx<T> t[4]={a[k],a[k+4],a[k+8],a[k+12]};
+      Codelet<4,S,T>::run(t);
+#pragma unroll
+      for(int s=0; s < 4; ++s) b[s][k]=t[s];
+    }
+    // W_16^{ks}: (k,s) = (1,1) W, (1,2) W^2, (1,3) W^3, (2,1) W^2,
+    // (2,2) W^4 = S i, (2,3) W^6, (3,1) W^3, (3,2) W^6, (3,3) W^9.
+    b[1][1]=rot(b[1][1],c1,s1);
+    b[2][1]=rot(b[2][1],h,h);
+    b[3][1]=rot(b[3][1],s1,c1);
+    b[1][2]=rot(b[1][2],h,h);
+    b[2][2]=mulI<S>(b[2][2]);
+    b[3][2]=rot(b[3][2],-h,h);
+    b[1][3]=rot(b[1][3],s1,c1);
+    b[2][3]=rot(b[2][3],-h,h);
+    b[3][3]=rot(b[3][3],-c1,-s1);
+#pragma unroll
+    for(int s=0; s < 4; ++s) {
+      Codelet<4,S,T>::run(b[s]);
+#pragma unroll
+      for(int t=0; t < 4; ++t) a[s+4*t]=b[s][t];
     }
   }
 };
@@ -462,13 +511,18 @@ __device__ __forceinline__ void ipStage(cplx<T> *__restrict__ x, int n, int Ls,
   }
 }
 
-template<typename T, int S, bool DIF>
+// R16: the caller is compiled with the radix-16 stage (FP32 plans made with
+// allow16 hold radix 16; no other plan does).
+template<typename T, int S, bool DIF, bool R16>
 __device__ __forceinline__ void ipDispatch(int R, cplx<T> *x, int n, int Ls,
                                            int ncol, int ld,
                                            const typename TwT<T>::type *tw,
                                            int tid, int nthr)
 {
   switch(R) {
+    case 16:
+      if constexpr(R16) ipStage<T,16,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr);
+      break;
     case 8: ipStage<T,8,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;
     case 4: ipStage<T,4,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;
     case 2: ipStage<T,2,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;
@@ -482,7 +536,7 @@ __device__ __forceinline__ void ipDispatch(int R, cplx<T> *x, int n, int Ls,
 // Natural order in, digit-reversed spectrum out (in place).  Every thread
 // of the block calls it after the block has synchronised; it returns
 // synchronised.
-template<typename T, int S>
+template<typename T, int S, bool R16=false>
 __device__ void fftDIF(cplx<T> *x, const FFTPlanDev& p, int ncol, int ld,
                        int tid, int nthr)
 {
@@ -490,14 +544,14 @@ __device__ void fftDIF(cplx<T> *x, const FFTPlanDev& p, int ncol, int ld,
   int Ls=p.n;
   for(int s=0; s < p.nst; ++s) {
     int R=p.radix[s];
-    ipDispatch<T,S,true>(R,x,p.n,Ls,ncol,ld,tw,tid,nthr);
+    ipDispatch<T,S,true,R16>(R,x,p.n,Ls,ncol,ld,tw,tid,nthr);
     __syncthreads();
     Ls /= R;
   }
 }
 
 // Digit-reversed spectrum (as fftDIF leaves it) in, natural order out.
-template<typename T, int S>
+template<typename T, int S, bool R16=false>
 __device__ void fftDIT(cplx<T> *x, const FFTPlanDev& p, int ncol, int ld,
                        int tid, int nthr)
 {
@@ -506,7 +560,7 @@ __device__ void fftDIT(cplx<T> *x, const FFTPlanDev& p, int ncol, int ld,
   for(int s=p.nst-1; s >= 0; --s) {
     int R=p.radix[s];
     Ls *= R;
-    ipDispatch<T,S,false>(R,x,p.n,Ls,ncol,ld,tw,tid,nthr);
+    ipDispatch<T,S,false,R16>(R,x,p.n,Ls,ncol,ld,tw,tid,nthr);
     __syncthreads();
   }
 }

@@ -501,7 +501,7 @@ __device__ __forceinline__ void cpAsyncWait()
 // together as interleaved columns col = a*rpc + rho, so the B x rpc output
 // columns are a contiguous prefix for the inverse transforms.  Every thread
 // of the block calls it.
-template<typename T, bool CG, class Mul, bool D=false>
+template<typename T, bool CG, class Mul, bool D=false, bool R16=false>
 __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
                                            long long group,
                                            unsigned char *smemRaw,
@@ -558,13 +558,13 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
     __syncthreads();
     const cplx<T> *Z;
     if constexpr(inplaceFFT<T>() || D) {
-      fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
+      fftDIF<T,1,R16>(x,P.fp,ld,ld,tid,nthr);
       for(int i=tid; i < m*R; i += nthr) {
         int j=dR(i), rho=i-j*R;
         mulRowSlot<Mul,true>(mul,P,x,j*ld+rho,R,row0+rho,j,0);
       }
       __syncthreads();
-      fftDIT<T,-1>(x,P.fp,lb,ld,tid,nthr);
+      fftDIT<T,-1,R16>(x,P.fp,lb,ld,tid,nthr);
       Z=x;
     } else {
       cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
@@ -633,13 +633,13 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
       __syncthreads();
       const cplx<T> *Z;
       if constexpr(inplaceFFT<T>()) {
-        fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
+        fftDIF<T,1,R16>(x,P.fp,ld,ld,tid,nthr);
         for(int i=tid; i < m*R; i += nthr) {
           int j=dR(i), rho=i-j*R;
           mulRowSlot<Mul,true>(mul,P,x,j*ld+rho,R,row0+rho,j,r);
         }
         __syncthreads();
-        fftDIT<T,-1>(x,P.fp,lb,ld,tid,nthr);
+        fftDIT<T,-1,R16>(x,P.fp,lb,ld,tid,nthr);
         Z=x;
       } else {
         cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
@@ -685,6 +685,19 @@ rowConvKernel(const RowPlan<T> P, const Mul mul)
     rowConvRow<T,false,Mul,D>(P,g,smemRaw,mul);
 }
 
+// The same for FP32 plans with a radix-16 stage: the radix-16 code needs
+// more registers, so only those plans launch it, capped at 85 registers a
+// thread (three CTAs of 256 threads per SM).
+template<typename T, class Mul, bool D>
+__global__ void __launch_bounds__(256,3)
+rowConvKernel16(const RowPlan<T> P, const Mul mul)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  const long long groups=(P.nrows+P.rpc-1)/P.rpc;
+  for(long long g=blockIdx.x; g < groups; g += gridDim.x)
+    rowConvRow<T,false,Mul,D,true>(P,g,smemRaw,mul);
+}
+
 // ---------------------------------------------------------------------------
 // Row kernel, Hermitian data (fftPadHermitian along the contiguous axis,
 // explicit padding to an even real length N): the H stored modes are packed
@@ -692,11 +705,11 @@ rowConvKernel(const RowPlan<T> P, const Mul mul)
 // physical values as (u[2t], u[2t+1]) pairs; the multiplier acts on those
 // doubles; the sign -1 FFT of the packed product is unpacked into the H
 // output modes (real-to-complex).
-template<typename T, class Mul>
-__global__ void __launch_bounds__(256)
-hermRowKernel(const HermRowPlan<T> P, const Mul mul)
+template<typename T, class Mul, bool R16>
+__device__ __forceinline__ void hermRows(const HermRowPlan<T>& P,
+                                         const Mul& mul,
+                                         unsigned char *smemRaw)
 {
-  extern __shared__ __align__(16) unsigned char smemRaw[];
   const int A=P.A, B=P.B, H=P.H, Nh=P.Nh, R=P.rpc;
   const int ld=A*R, lb=B*R;
   cplx<T> *x=(cplx<T> *) smemRaw;
@@ -751,13 +764,13 @@ hermRowKernel(const HermRowPlan<T> P, const Mul mul)
     __syncthreads();
     const cplx<T> *Z;
     if constexpr(inplaceFFT<T>()) {
-      fftDIF<T,1>(x,P.fp,ld,ld,tid,nthr);
+      fftDIF<T,1,R16>(x,P.fp,ld,ld,tid,nthr);
       for(int i=tid; i < Nh*R; i += nthr) {
         int t=dR(i), rho=i-t*R;
         mulHermSlot<Mul,true>(mul,P,x,t*ld+rho,R,row0+rho,t);
       }
       __syncthreads();
-      fftDIT<T,-1>(x,P.fp,lb,ld,tid,nthr);
+      fftDIT<T,-1,R16>(x,P.fp,lb,ld,tid,nthr);
       Z=x;
     } else {
       cplx<T> *X=fftSmem<T,1>(x,y,P.fp,ld,ld,tid,nthr);
@@ -794,6 +807,23 @@ hermRowKernel(const HermRowPlan<T> P, const Mul mul)
   }
 }
 
+template<typename T, class Mul>
+__global__ void __launch_bounds__(256)
+hermRowKernel(const HermRowPlan<T> P, const Mul mul)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  hermRows<T,Mul,false>(P,mul,smemRaw);
+}
+
+// FP32 plans with a radix-16 stage (as rowConvKernel16).
+template<typename T, class Mul>
+__global__ void __launch_bounds__(256,3)
+hermRowKernel16(const HermRowPlan<T> P, const Mul mul)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  hermRows<T,Mul,true>(P,mul,smemRaw);
+}
+
 // ---------------------------------------------------------------------------
 // Launchers of the row kernels for any multiplier type.
 
@@ -821,6 +851,11 @@ cudaError_t launchRowWith(const RowPlan<T>& P, const Mul& mul, int threads,
     kernel<<<(unsigned) grid,threads,sm,s>>>(P,mul);
     return cudaGetLastError();
   };
+  if constexpr(std::is_same<T,float>::value)
+    if(hasRadix16(P.fp)) {
+      if(P.direct) return go(rowConvKernel16<T,Mul,true>);
+      return go(rowConvKernel16<T,Mul,false>);
+    }
   if(P.direct) return go(rowConvKernel<T,Mul,true>);
   return go(rowConvKernel<T,Mul,false>);
 }
@@ -833,10 +868,15 @@ cudaError_t launchHermRowWith(const HermRowPlan<T>& P, const Mul& mul,
   const long long groups=(P.nrows+P.rpc-1)/P.rpc;
   grid=std::min(std::min(grid,groups),(long long) INT_MAX);
   if(grid < 1) return cudaSuccess;
-  cudaError_t e=setRowSmem(hermRowKernel<T,Mul>,sm);
-  if(e != cudaSuccess) return e;
-  hermRowKernel<T,Mul><<<(unsigned) grid,threads,sm,s>>>(P,mul);
-  return cudaGetLastError();
+  auto go=[&](auto kernel) {
+    cudaError_t e=setRowSmem(kernel,sm);
+    if(e != cudaSuccess) return e;
+    kernel<<<(unsigned) grid,threads,sm,s>>>(P,mul);
+    return cudaGetLastError();
+  };
+  if constexpr(std::is_same<T,float>::value)
+    if(hasRadix16(P.fp)) return go(hermRowKernel16<T,Mul>);
+  return go(hermRowKernel<T,Mul>);
 }
 
 } // namespace fgb
