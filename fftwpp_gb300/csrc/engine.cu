@@ -1534,7 +1534,8 @@ cudaError_t Conv::runZeroCopy(const void *const *hin, const void *const *in,
 // Times every combination of input and output ways on page-locked scratch
 // arrays of this plan's size (the best of three runs each, after one
 // untimed) and keeps the fastest; whole-array copies both ways if timing
-// fails.
+// fails.  The host writes the inputs before every timed run, as a caller
+// producing new data does, so the link reads lines the CPU holds dirty.
 void Conv::measureHostPath(cudaStream_t s)
 {
   hostWay[0]=hostWay[1]=HOST_COPY;
@@ -1568,6 +1569,7 @@ void Conv::measureHostPath(cudaStream_t s)
   double best=1e300;
   for(int rep=0; rep < 3 && ok; ++rep)
     for(const auto& w : ways) {
+      std::memset(h,0,stride*n);
       ok=cudaEventRecord(e0,s) == cudaSuccess &&
         runZeroCopy(hin.data(),in.data(),out.data(),w.first,w.second,s) ==
         cudaSuccess &&
