@@ -435,10 +435,12 @@ Conv::Conv(int dim, const int *kinds, const long *L, const long *M,
     tuning(false), staging(0), hostIn(NULL),
     hostOut(NULL), nlaunch(0),
     timing(false), normalize(true), marks(0), hostTile(0), hostThr(0),
-    hostTileB(0), hostThrB(0), side(NULL), chunks(0)
+    hostTileB(0), hostThrB(0), side(NULL), chunks(0), outChunks(0),
+    outCopied(NULL)
 {
   for(int k=0; k < CHUNKS; ++k) {
     lanes[k]=NULL;
+    outDone[k]=NULL;
     chunkReady[k]=chunkDone[k]=NULL;
   }
   hostWay[0]=hostWay[1]=-1;
@@ -824,7 +826,9 @@ Conv::~Conv()
 {
   for(cudaEvent_t ev : events) cudaEventDestroy(ev);
   for(cudaEvent_t ev : ready) cudaEventDestroy(ev);
+  if(outCopied) cudaEventDestroy(outCopied);
   for(int k=0; k < CHUNKS; ++k) {
+    if(outDone[k]) cudaEventDestroy(outDone[k]);
     if(chunkReady[k]) cudaEventDestroy(chunkReady[k]);
     if(chunkDone[k]) cudaEventDestroy(chunkDone[k]);
     if(k > 0 && lanes[k]) cudaStreamDestroy(lanes[k]);
@@ -1085,6 +1089,28 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     return cudaSuccess;
   };
 
+  // The last outer-axis launch.  While a host call copies the outputs out
+  // (outChunks > 0, complex outer axis): one launch per column range, each
+  // followed by the event its copy waits for.
+  auto lastOuter=[&](OuterPlan<T>& O, const AxisPlan& a) {
+    if(a.kind == KIND_REAL) return launchOuterRealBwd<T>(O,a.thrB,s);
+    if(!outChunks || timing) return launchOuterBwd<T>(O,a.thrB,s);
+    OuterPlan<T> Q=O;
+    const size_t eb=elemBytes();       // the caller's element on the output side
+    cudaError_t e;
+    for(int k=0; k < outChunks; ++k) {
+      const long c0=outCol[k];
+      Q.C=(int) (outCol[k+1]-c0);
+      for(int i=0; i < O.count; ++i) {
+        Q.in[i]=O.in[i]+c0;
+        Q.out[i]=(Cx *) ((char *) O.out[i]+c0*eb);
+      }
+      if((e=launchOuterBwd<T>(Q,a.thrB,s)) != cudaSuccess ||
+         (e=cudaEventRecord(outDone[k],s)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  };
+
   if(I.dim == 1 && !I.longRow) {
     const AxisPlan& a=I.axis[0];
     if(a.kind == KIND_HERMITIAN) {
@@ -1159,8 +1185,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     O.inRow=C;                                  // staging side
     O.outRow=isStrided ? strideS[0] : C;        // data side
     for(int i=0; i < B; ++i) {O.in[i]=(const Cx *) bufs[i]; O.out[i]=(Cx *) out[i];}
-    e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(O,ax.thrB,s) :
-      launchOuterBwd<T>(O,ax.thrB,s);
+    e=lastOuter(O,ax);
     tick(s);
     return e;
   }
@@ -1238,8 +1263,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
   X.inRow=Cx_;                                  // staging side
   X.outRow=isStrided ? strideS[0] : Cx_;        // data side
   for(int i=0; i < B; ++i) {X.in[i]=(const Cx *) bx[i]; X.out[i]=(Cx *) out[i];}
-  e=ax.kind == KIND_REAL ? launchOuterRealBwd<T>(X,ax.thrB,s) :
-    launchOuterBwd<T>(X,ax.thrB,s);
+  e=lastOuter(X,ax);
   tick(s);
   return e;
 }
@@ -1479,7 +1503,7 @@ cudaError_t Conv::pipeInputs(const void *const *in, void *const *dev,
 // or HOST_INPLACE64 (the same with the fastest tiles whose rows span at
 // least 64 bytes, whole lines of the link).
 cudaError_t Conv::runZeroCopy(const void *const *hin, const void *const *in,
-                              void *const *out,
+                              void *const *hout, void *const *out,
                               int wayIn, int wayOut, cudaStream_t s)
 {
   const size_t bytes=elements()*elemBytes();
@@ -1521,14 +1545,68 @@ cudaError_t Conv::runZeroCopy(const void *const *hin, const void *const *in,
   if(wayOut == HOST_INPLACE64 && hostTileB) {
     a0.tileB=hostTileB; a0.thrB=hostThrB;
   }
+  // With a complex outer axis the outputs leave in column ranges (2D
+  // copies on the side stream, copy engines), each as soon as the last
+  // transform has written it.
+  const bool pipeOut=copyOut && I.dim > 1 && !I.longRow &&
+    I.axis[0].kind != KIND_REAL;
+  if(pipeOut && (e=planOutputs(s)) != cudaSuccess) return e;
   e=run(src.data(),dst.data(),s);
   chunks=0;
+  const int nOut=outChunks;
+  outChunks=0;
   a0.tile=keep[0]; a0.thr=keep[1];
   a0.tileB=keep[2]; a0.thrB=keep[3];
   if(e != cudaSuccess || !copyOut) return e;
+  if(pipeOut && !timing) {
+    const size_t eb=elemBytes();
+    const long rows=I.axis[0].L, Cn=(long) elements()/rows;
+    for(int k=0; k < nOut; ++k) {
+      const size_t off=outCol[k]*eb;
+      if((e=cudaStreamWaitEvent(side,outDone[k],0)) != cudaSuccess) return e;
+      for(int b=0; b < B; ++b)
+        if((e=cudaMemcpy2DAsync((char *) hout[b]+off,Cn*eb,
+                                (const char *) dst[b]+off,Cn*eb,
+                                (outCol[k+1]-outCol[k])*eb,rows,
+                                cudaMemcpyDefault,side)) != cudaSuccess)
+          return e;
+    }
+    if((e=cudaEventRecord(outCopied,side)) != cudaSuccess) return e;
+    return cudaStreamWaitEvent(s,outCopied,0);
+  }
   C.count=B;
   for(int b=0; b < B; ++b) {C.src[b]=dst[b]; C.dst[b]=out[b];}
   return launchBulkCopy(C,s);
+}
+
+// Column ranges of the last outer transform for a host call's output
+// copies (whole backward tiles each), their events and the side stream.
+cudaError_t Conv::planOutputs(cudaStream_t s)
+{
+  cudaError_t e;
+  auto event=[](cudaEvent_t& ev) {
+    return ev ? cudaSuccess :
+      cudaEventCreateWithFlags(&ev,cudaEventDisableTiming);
+  };
+  if(!side && (e=cudaStreamCreateWithFlags(&side,cudaStreamNonBlocking)) !=
+     cudaSuccess) {
+    side=NULL;
+    return e;
+  }
+  if((e=event(outCopied)) != cudaSuccess) return e;
+  const long rows=I.axis[0].L, C=(long) elements()/rows;
+  const long unit=std::max(1,I.axis[0].tileB);
+  const long units=(C+unit-1)/unit;
+  const long per=(units+OUT_CHUNKS-1)/OUT_CHUNKS;
+  int n=0;
+  outCol[0]=0;
+  while(outCol[n] < C) {
+    outCol[n+1]=std::min(C,outCol[n]+per*unit);
+    if((e=event(outDone[n])) != cudaSuccess) return e;
+    ++n;
+  }
+  outChunks=n;
+  return cudaSuccess;
 }
 
 // Times every combination of input and output ways on page-locked scratch
@@ -1550,12 +1628,15 @@ void Conv::measureHostPath(cudaStream_t s)
   std::memset(h,0,stride*n);
   void *d=mappedAddress(h);
   std::vector<const void *> hin(I.A), in(I.A);
-  std::vector<void *> out(I.B);
+  std::vector<void *> hout(I.B), out(I.B);
   for(int a=0; a < I.A; ++a) {
     hin[a]=(char *) h+a*stride;
     in[a]=(char *) d+a*stride;
   }
-  for(int b=0; b < I.B; ++b) out[b]=(char *) d+b*stride;
+  for(int b=0; b < I.B; ++b) {
+    hout[b]=(char *) h+b*stride;
+    out[b]=(char *) d+b*stride;
+  }
   std::vector<std::pair<int,int>> ways;
   for(int wi=HOST_COPY; wi <= HOST_INPLACE64; ++wi)
     for(int wo=HOST_COPY; wo <= HOST_INPLACE64; ++wo)
@@ -1564,14 +1645,16 @@ void Conv::measureHostPath(cudaStream_t s)
   cudaEvent_t e0=NULL, e1=NULL;
   bool ok=d && cudaEventCreate(&e0) == cudaSuccess &&
     cudaEventCreate(&e1) == cudaSuccess;
-  ok=ok && runZeroCopy(hin.data(),in.data(),out.data(),HOST_COPY,HOST_COPY,s) ==
+  ok=ok && runZeroCopy(hin.data(),in.data(),hout.data(),out.data(),HOST_COPY,
+                       HOST_COPY,s) ==
     cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
   double best=1e300;
   for(int rep=0; rep < 3 && ok; ++rep)
     for(const auto& w : ways) {
       std::memset(h,0,stride*n);
       ok=cudaEventRecord(e0,s) == cudaSuccess &&
-        runZeroCopy(hin.data(),in.data(),out.data(),w.first,w.second,s) ==
+        runZeroCopy(hin.data(),in.data(),hout.data(),out.data(),w.first,
+                    w.second,s) ==
         cudaSuccess &&
         cudaEventRecord(e1,s) == cudaSuccess &&
         cudaStreamSynchronize(s) == cudaSuccess;
@@ -1679,7 +1762,7 @@ cudaError_t Conv::runHost(const void *const *in, void *const *out,
         if(wi == HOST_COPY) wi=HOST_INPLACE;
         if(wo == HOST_COPY) wo=HOST_INPLACE;
       }
-      cudaError_t e=runZeroCopy(in,min.data(),mout.data(),wi,wo,s);
+      cudaError_t e=runZeroCopy(in,min.data(),out,mout.data(),wi,wo,s);
       return e != cudaSuccess ? e : cudaStreamSynchronize(s);
     }
   }

@@ -214,12 +214,21 @@ private:
   long chunkCol[CHUNKS+1];
   cudaError_t pipeInputs(const void *const *in, void *const *dev,
                          cudaStream_t s);
+  // Outputs copied out to the host on the side stream while the last outer
+  // transform still runs: a host call sets outChunks, and that transform
+  // is launched in column ranges [outCol[k], outCol[k+1]), outDone[k]
+  // recorded after range k; the copy of range k waits for it.
+  static const int OUT_CHUNKS=2;
+  int outChunks;
+  long outCol[CHUNKS+1];
+  cudaEvent_t outDone[CHUNKS], outCopied;
+  cudaError_t planOutputs(cudaStream_t s);
   void allocate();
   void tune();
   bool directSegments() const;
   cudaError_t runZeroCopy(const void *const *hin, const void *const *in,
-                          void *const *out, int wayIn, int wayOut,
-                          cudaStream_t s);
+                          void *const *hout, void *const *out, int wayIn,
+                          int wayOut, cudaStream_t s);
   void measureHostPath(cudaStream_t s);
 };
 
