@@ -755,10 +755,19 @@ __device__ __forceinline__ void hermRows(const HermRowPlan<T>& P,
         if(k == 0) a.y=(T) 0;
         const cplx<T> b=conjg(zc[u]);
         const cplx<T> S=a+b;
-        const cplx<T> Pw=twmul<1>(a-b,tw[k]);
-        x[sp(i)]=mk(S.x-Pw.y,S.y+Pw.x);
-        if(k != 0 && 2*k != Nh)
-          x[sp((Nh-k)*ld+col)]=mk(S.x+Pw.y,Pw.x-S.y);
+        cplx<T> Y, Yc;
+        if constexpr(std::is_same<T,double>::value) {
+          // FP64: S + (i D) W as four DFMAs, the partner as conj(2S - Y).
+          const cplx<T> D=a-b;
+          Y=fmaTw<1>(S,mk(-D.y,D.x),tw[k]);
+          Yc=mk(fma((T) 2,S.x,-Y.x),fma((T) -2,S.y,Y.y));
+        } else {
+          const cplx<T> Pw=twmul<1>(a-b,tw[k]);
+          Y=mk(S.x-Pw.y,S.y+Pw.x);
+          Yc=mk(S.x+Pw.y,Pw.x-S.y);
+        }
+        x[sp(i)]=Y;
+        if(k != 0 && 2*k != Nh) x[sp((Nh-k)*ld+col)]=Yc;
       }
     }
     __syncthreads();
@@ -796,12 +805,25 @@ __device__ __forceinline__ void hermRows(const HermRowPlan<T>& P,
       if(row >= P.nrows || (pair && km < k)) continue;
       const cplx<T> zk=Z[sp(k*ld+col)];
       const cplx<T> zm=conjg(Z[sp(km*ld+col)]);
-      const cplx<T> sum=zk+zm, dd=zk-zm;
-      const cplx<T> Q=twmul<-1>(mk(dd.y,-dd.x),tw[k]);
+      cplx<T> V, Vc;
+      if constexpr(std::is_same<T,double>::value) {
+        // FP64: hs sum, hs dd = 2 hs zk - hs sum, V = hs sum + hs Q as
+        // four DFMAs, the partner as conj(2 hs sum - V).
+        const cplx<T> hsum=(zk+zm)*hs;
+        const T h2=hs+hs;
+        const cplx<T> hdd=mk(fma(h2,zk.x,-hsum.x),fma(h2,zk.y,-hsum.y));
+        V=fmaTw<-1>(hsum,mk(hdd.y,-hdd.x),tw[k]);
+        Vc=mk(fma((T) 2,hsum.x,-V.x),fma((T) -2,hsum.y,V.y));
+      } else {
+        const cplx<T> sum=zk+zm, dd=zk-zm;
+        const cplx<T> Q=twmul<-1>(mk(dd.y,-dd.x),tw[k]);
+        V=(sum+Q)*hs;
+        Vc=conjg(sum-Q)*hs;
+      }
       cplx<T> *o=P.out[b]+row*P.rowStride;
       const int sh=ioShift<T>(P.ioShift,8+b);
-      storeIO(o+k,(sum+Q)*hs,P.io64 & 2,sh);
-      if(pair) storeIO(o+km,conjg(sum-Q)*hs,P.io64 & 2,sh);
+      storeIO(o+k,V,P.io64 & 2,sh);
+      if(pair) storeIO(o+km,Vc,P.io64 & 2,sh);
     }
     __syncthreads();
   }
