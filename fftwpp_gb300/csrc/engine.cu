@@ -180,13 +180,18 @@ static FFTPlanDev fftPlan(long n, int prec, bool oddFirst=false,
   p.nst=0;
   long r=n;
   // Largest radices first: 8, then 4 or 2, then odd primes.  FP32 in-place
-  // row transforms (allow16) also take radix 16 (4 x 4 in registers) where
-  // that saves a stage: a power-of-two factor 2^k takes ceil(k/3) stages of
+  // transforms (allow16) also take radix 16 (4 x 4 in registers) where that
+  // saves a stage: a power-of-two factor 2^k takes ceil(k/3) stages of
   // radix <= 8 but s = ceil(k/4) of radix <= 16, as k - 3s radix-16 stages
-  // and the rest radix 8.
+  // and the rest radix 8.  A factor 3 with k >= 1 may take one factor 2
+  // into a radix-6 stage when that saves one more (1536 = 6 16 16).
   int k2=0;
   for(long t=n; t % 2 == 0; t /= 2) ++k2;
-  if(allow16 && prec == PREC_F32 && oddFirst && (k2+3)/4 < (k2+2)/3)
+  const bool wide=allow16 && prec == PREC_F32 && oddFirst;
+  const bool six=wide && n % 3 == 0 && k2 >= 1 &&
+    1+(k2+2)/4 < 1+(k2+3)/4;
+  if(six) {k2 -= 1; r /= 2;}           // the factor 2 of the radix-6 stage
+  if(wide && (k2+3)/4 < (k2+2)/3)
     for(int i=0; i < k2-3*((k2+3)/4); ++i) {p.radix[p.nst++]=16; r /= 16;}
   while(r % 8 == 0) {p.radix[p.nst++]=8; r /= 8;}
   if(r % 4 == 0) {p.radix[p.nst++]=4; r /= 4;}
@@ -196,12 +201,20 @@ static FFTPlanDev fftPlan(long n, int prec, bool oddFirst=false,
   while(r % 3 == 0) {p.radix[p.nst++]=3; r /= 3;}
   if(p.nst > FGB_MAXSTAGES)
     throw std::runtime_error("too many FFT stages");
+  if(six) {                              // one radix 3 becomes the radix 6
+    for(int s=p.nst-1; s >= 0; --s)
+      if(p.radix[s] == 3) {p.radix[s]=6; break;}
+  }
   if(oddFirst) {
+    // Odd radices first (the radix 6 with them, last), then the powers of
+    // two, each group in order: every span after them is a power of two.
     int k=0, tmp[FGB_MAXSTAGES];
-    for(int s=0; s < p.nst; ++s)          // odd radices, then even, in order
+    for(int s=0; s < p.nst; ++s)
       if(p.radix[s] % 2) tmp[k++]=p.radix[s];
     for(int s=0; s < p.nst; ++s)
-      if(p.radix[s] % 2 == 0) tmp[k++]=p.radix[s];
+      if(p.radix[s] == 6) tmp[k++]=p.radix[s];
+    for(int s=0; s < p.nst; ++s)
+      if(p.radix[s] % 2 == 0 && p.radix[s] != 6) tmp[k++]=p.radix[s];
     for(int s=0; s < p.nst; ++s) p.radix[s]=tmp[s];
   }
   p.tw=twiddles(n,prec);
@@ -1005,7 +1018,7 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
       im.q[d]=(int) a.q;
       im.rev[d]=inplaceFFT<T>() && a.kind != KIND_REAL && a.p == 1;
       if(im.rev[d]) {
-        FFTPlanDev f=fftPlan(a.m,I.prec,true);
+        FFTPlanDev f=fftPlan(a.m,I.prec,true,true);   // as outerPlan
         im.nst[d]=f.nst;
         for(int k=0; k < f.nst; ++k) im.radix[d][k]=(unsigned char) f.radix[k];
       }
@@ -1041,7 +1054,8 @@ cudaError_t Conv::runT(const void *const *in, void *const *out, cudaStream_t s)
     P.io64=0;
     P.inplace=inplaceFFT<T>() && a.kind != KIND_REAL && a.p == 1;
     P.conj=0;
-    P.fp=fftPlan(a.kind == KIND_REAL ? a.N/2 : a.m,I.prec,P.inplace != 0);
+    P.fp=fftPlan(a.kind == KIND_REAL ? a.N/2 : a.m,I.prec,P.inplace != 0,
+                 true);
     P.twN=(const typename TwT<T>::type *) twiddles(a.N,I.prec);
     P.twX=NULL; P.NX=1;
   };

@@ -68,11 +68,12 @@ struct FFTPlanDev {
   const void *tw;         // TwT<T>::type[n]
 };
 
-// Whether a plan holds a radix-16 stage (its kernels need the R16 form).
+// Whether a plan holds a radix-16 or radix-6 stage (its kernels need the
+// R16 form).
 inline bool hasRadix16(const FFTPlanDev& p)
 {
   for(int s=0; s < p.nst; ++s)
-    if(p.radix[s] == 16) return true;
+    if(p.radix[s] == 16 || p.radix[s] == 6) return true;
   return false;
 }
 
@@ -173,6 +174,27 @@ template<int S, typename T> struct Codelet<16,S,T> {
       Codelet<4,S,T>::run(b[s]);
 #pragma unroll
       for(int t=0; t < 4; ++t) a[s+4*t]=b[s][t];
+    }
+  }
+};
+
+// Radix 6 as 3 x 2 (with radix 16, for FP32 in-place transforms of
+// lengths 3 * 2^k where it saves a stage): radix-3 over the inputs k + 2r,
+// the products with W_6^{ks}, radix-2 over k; outputs in natural order.
+template<int S, typename T> struct Codelet<6,S,T> {
+  static __device__ __forceinline__ void run(cplx<T> *a) {
+    const T h=(T) 0.5, s3=(T) (S*FGB_SQRT3_2);
+    cplx<T> e[3]={a[0],a[2],a[4]}, o[3]={a[1],a[3],a[5]};
+    Codelet<3,S,T>::run(e);
+    Codelet<3,S,T>::run(o);
+    // W_6^S = (1/2, S sqrt3/2), W_6^{2S} = (-1/2, S sqrt3/2)
+    const cplx<T> o1=o[1], o2=o[2];
+    o[1]=mk(fma(o1.x,h,-o1.y*s3),fma(o1.x,s3,o1.y*h));
+    o[2]=mk(fma(o2.x,-h,-o2.y*s3),fma(o2.x,s3,-o2.y*h));
+#pragma unroll
+    for(int s=0; s < 3; ++s) {
+      a[s]=e[s]+o[s];
+      a[s+3]=e[s]-o[s];
     }
   }
 };
@@ -511,8 +533,8 @@ __device__ __forceinline__ void ipStage(cplx<T> *__restrict__ x, int n, int Ls,
   }
 }
 
-// R16: the caller is compiled with the radix-16 stage (FP32 plans made with
-// allow16 hold radix 16; no other plan does).
+// R16: the caller is compiled with the radix-16 and radix-6 stages (FP32
+// plans made with allow16 may hold them; no other plan does).
 template<typename T, int S, bool DIF, bool R16>
 __device__ __forceinline__ void ipDispatch(int R, cplx<T> *x, int n, int Ls,
                                            int ncol, int ld,
@@ -522,6 +544,9 @@ __device__ __forceinline__ void ipDispatch(int R, cplx<T> *x, int n, int Ls,
   switch(R) {
     case 16:
       if constexpr(R16) ipStage<T,16,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr);
+      break;
+    case 6:
+      if constexpr(R16) ipStage<T,6,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr);
       break;
     case 8: ipStage<T,8,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;
     case 4: ipStage<T,4,S,DIF>(x,n,Ls,ncol,ld,tw,tid,nthr); break;

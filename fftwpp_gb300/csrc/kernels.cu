@@ -28,7 +28,7 @@ __device__ __forceinline__ long long dataCol(const OuterPlan<T>& P, int col)
 // ---------------------------------------------------------------------------
 // Outer forward, complex data: residue block r of the padded transform along
 // a strided axis for `tile` adjacent columns.
-template<typename T, bool CG>
+template<typename T, bool CG, bool R16=false>
 __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
                                              int r, int z,
                                              unsigned char *smemRaw)
@@ -140,7 +140,7 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
     if(P.inplace) {
       // Transform in place (digit-reversed j; the row kernels do not
       // depend on row order and the backward undoes it).
-      fftDIF<T,1>(x,P.fp,tile,tile,tid,nthr);
+      fftDIF<T,1,R16>(x,P.fp,tile,tile,tid,nthr);
       for(int i=tid; i < m*tile; i += nthr) {
         int j=dTile(i), cc=i-j*tile;
         int col=col0+cc;
@@ -178,7 +178,7 @@ outerFwdKernel(const OuterPlan<T> P)
 }
 
 // Outer backward, complex data: all residues of a column tile, accumulated.
-template<typename T, bool CG>
+template<typename T, bool CG, bool R16=false>
 __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
                                              int z, unsigned char *smemRaw)
 {
@@ -232,7 +232,7 @@ __device__ __forceinline__ void outerBwdTile(const OuterPlan<T>& P, int ctile,
     }
     cplx<T> *X;
     if(inplaceFFT<T>() && P.inplace) {
-      fftDIT<T,-1>(x,P.fp,tile,tile,tid,nthr);
+      fftDIT<T,-1,R16>(x,P.fp,tile,tile,tid,nthr);
       X=x;
     } else {
       X=fftSmem<T,-1>(x,y,P.fp,tile,tile,tid,nthr);
@@ -297,6 +297,25 @@ outerBwdKernel(const OuterPlan<T> P)
 {
   extern __shared__ __align__(16) unsigned char smemRaw[];
   outerBwdTile<T,false>(P,blockIdx.x,blockIdx.z,smemRaw);
+}
+
+// FP32 in-place plans with radix-16 or radix-6 stages: their own
+// instantiations, capped at 85 registers a thread (the wider codelets need
+// more registers than the others may take).
+template<typename T>
+__global__ void __launch_bounds__(256,3)
+outerFwdKernel16(const OuterPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  outerFwdTile<T,false,true>(P,blockIdx.x,blockIdx.y,blockIdx.z,smemRaw);
+}
+
+template<typename T>
+__global__ void __launch_bounds__(256,3)
+outerBwdKernel16(const OuterPlan<T> P)
+{
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  outerBwdTile<T,false,true>(P,blockIdx.x,blockIdx.z,smemRaw);
 }
 
 // ---------------------------------------------------------------------------
@@ -643,22 +662,32 @@ template<typename T>
 cudaError_t launchOuterFwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
 {
   size_t sm=outerFwdSmem<T>(P.L,P.m,P.tile,P.inplace);
-  cudaError_t e=setSmem(outerFwdKernel<T>,sm);
-  if(e != cudaSuccess) return e;
   dim3 grid((P.C+P.tile-1)/P.tile,P.q,P.nbatch*P.count);
-  outerFwdKernel<T><<<grid,threads,sm,s>>>(P);
-  return cudaGetLastError();
+  auto go=[&](auto kernel) {
+    cudaError_t e=setSmem(kernel,sm);
+    if(e != cudaSuccess) return e;
+    kernel<<<grid,threads,sm,s>>>(P);
+    return cudaGetLastError();
+  };
+  if constexpr(std::is_same<T,float>::value)
+    if(P.inplace && hasRadix16(P.fp)) return go(outerFwdKernel16<T>);
+  return go(outerFwdKernel<T>);
 }
 
 template<typename T>
 cudaError_t launchOuterBwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
 {
   size_t sm=outerBwdSmem<T>(P.L,P.m,P.tile,P.q,P.inplace);
-  cudaError_t e=setSmem(outerBwdKernel<T>,sm);
-  if(e != cudaSuccess) return e;
   dim3 grid((P.C+P.tile-1)/P.tile,1,P.nbatch*P.count);
-  outerBwdKernel<T><<<grid,threads,sm,s>>>(P);
-  return cudaGetLastError();
+  auto go=[&](auto kernel) {
+    cudaError_t e=setSmem(kernel,sm);
+    if(e != cudaSuccess) return e;
+    kernel<<<grid,threads,sm,s>>>(P);
+    return cudaGetLastError();
+  };
+  if constexpr(std::is_same<T,float>::value)
+    if(P.inplace && hasRadix16(P.fp)) return go(outerBwdKernel16<T>);
+  return go(outerBwdKernel<T>);
 }
 
 template<typename T>
