@@ -358,22 +358,53 @@ void BatchConv::build()
   auto byCost=[](const Ord& x, const Ord& y) {return x.cost > y.cost;};
   std::sort(small.begin(),small.end(),byCost);
   std::sort(lng.begin(),lng.end(),byCost);
-  std::vector<BatchTask> tasks;
+  // The long problems pass through their staging: forward column tasks,
+  // row tasks, backward column tasks.  They go in groups of about
+  // GROUP_BYTES of staging, software-pipelined: step g queues the forward
+  // columns of group g, a share of the small problems, the rows of group
+  // g-1 and the backward columns of group g-2.  A problem's staging is then
+  // written and read back within three groups, while the L2 still holds
+  // it, and every task's producers were queued at least one group earlier,
+  // so a consumer rarely waits.  Measured on the 512-problem workload:
+  // 8 MB groups halve the FP32 launch's DRAM traffic (714 -> 364 MB) at the
+  // same speed; the FP64 launch, bound by its FP64 pipe, loses 12 % to the
+  // waits of groups that small and keeps 24 MB groups (1260 -> 1105 MB).
+  const size_t GROUP_BYTES=(prec == PREC_F64 ? 24u : 8u) << 20;
+  std::vector<std::vector<int>> groups;
+  size_t acc=0;
   for(auto& o : lng) {
-    const BatchProblem<T>& P=probs[o.i];
-    int tiles=(int) ceilquotient(P.fwd.C,P.fwd.tile);
-    for(int t=0; t < tiles; ++t)
-      for(int a=0; a < A; ++a) tasks.push_back({TASK_COLFWD,o.i,t,a});
+    const size_t bytes=e*(size_t) probs[o.i].fwd.NX*A;
+    if(groups.empty() || (acc > 0 && acc+bytes > GROUP_BYTES)) {
+      groups.emplace_back();
+      acc=0;
+    }
+    groups.back().push_back(o.i);
+    acc += bytes;
   }
-  for(auto& o : small) tasks.push_back({TASK_SMALL,o.i,0,0});
-  for(auto& o : lng)
-    for(int r=0; r < probs[o.i].nrows; ++r)
-      tasks.push_back({TASK_ROW,o.i,r,0});
-  for(auto& o : lng) {
-    const BatchProblem<T>& P=probs[o.i];
-    int tiles=(int) ceilquotient(P.bwd.C,P.bwd.tile);
-    for(int t=0; t < tiles; ++t)
-      for(int b=0; b < B; ++b) tasks.push_back({TASK_COLBWD,o.i,t,b});
+  const int ng=(int) groups.size();
+  std::vector<BatchTask> tasks;
+  size_t nextSmall=0;
+  for(int g=0; g < ng+2; ++g) {
+    if(g < ng)
+      for(int i : groups[g]) {
+        const BatchProblem<T>& P=probs[i];
+        int tiles=(int) ceilquotient(P.fwd.C,P.fwd.tile);
+        for(int t=0; t < tiles; ++t)
+          for(int a=0; a < A; ++a) tasks.push_back({TASK_COLFWD,i,t,a});
+      }
+    const size_t endSmall=small.size()*(size_t) (g+1)/(size_t) (ng+2);
+    for(; nextSmall < endSmall; ++nextSmall)
+      tasks.push_back({TASK_SMALL,small[nextSmall].i,0,0});
+    if(g >= 1 && g-1 < ng)
+      for(int i : groups[g-1])
+        for(int r=0; r < probs[i].nrows; ++r) tasks.push_back({TASK_ROW,i,r,0});
+    if(g >= 2)
+      for(int i : groups[g-2]) {
+        const BatchProblem<T>& P=probs[i];
+        int tiles=(int) ceilquotient(P.bwd.C,P.bwd.tile);
+        for(int t=0; t < tiles; ++t)
+          for(int b=0; b < B; ++b) tasks.push_back({TASK_COLBWD,i,t,b});
+      }
   }
   ntasks=(int) tasks.size();
   nfwd0.resize(n);
