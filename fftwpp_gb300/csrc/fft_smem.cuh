@@ -70,7 +70,7 @@ struct FFTPlanDev {
 
 // Whether a plan holds a radix-16 or radix-6 stage (its kernels need the
 // R16 form).
-inline bool hasRadix16(const FFTPlanDev& p)
+inline bool hasWideRadix(const FFTPlanDev& p)
 {
   for(int s=0; s < p.nst; ++s)
     if(p.radix[s] == 16 || p.radix[s] == 6) return true;

@@ -670,7 +670,7 @@ cudaError_t launchOuterFwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
     return cudaGetLastError();
   };
   if constexpr(std::is_same<T,float>::value)
-    if(P.inplace && hasRadix16(P.fp)) return go(outerFwdKernel16<T>);
+    if(P.inplace && hasWideRadix(P.fp)) return go(outerFwdKernel16<T>);
   return go(outerFwdKernel<T>);
 }
 
@@ -686,7 +686,7 @@ cudaError_t launchOuterBwd(const OuterPlan<T>& P, int threads, cudaStream_t s)
     return cudaGetLastError();
   };
   if constexpr(std::is_same<T,float>::value)
-    if(P.inplace && hasRadix16(P.fp)) return go(outerBwdKernel16<T>);
+    if(P.inplace && hasWideRadix(P.fp)) return go(outerBwdKernel16<T>);
   return go(outerBwdKernel<T>);
 }
 

@@ -874,7 +874,7 @@ cudaError_t launchRowWith(const RowPlan<T>& P, const Mul& mul, int threads,
     return cudaGetLastError();
   };
   if constexpr(std::is_same<T,float>::value)
-    if(hasRadix16(P.fp)) {
+    if(hasWideRadix(P.fp)) {
       if(P.direct) return go(rowConvKernel16<T,Mul,true>);
       return go(rowConvKernel16<T,Mul,false>);
     }
@@ -897,7 +897,7 @@ cudaError_t launchHermRowWith(const HermRowPlan<T>& P, const Mul& mul,
     return cudaGetLastError();
   };
   if constexpr(std::is_same<T,float>::value)
-    if(hasRadix16(P.fp)) return go(hermRowKernel16<T,Mul>);
+    if(hasWideRadix(P.fp)) return go(hermRowKernel16<T,Mul>);
   return go(hermRowKernel<T,Mul>);
 }
 
