@@ -24,8 +24,8 @@ The exchanges carry only the transformed x rows; no rank touches another
 GPU's memory (NCCL all-to-all through local buffers), no multicast.  The
 per-rank stages are an object with x_forward / rows / x_backward / scale;
 the GPU one (GPUStages) runs the library's kernels; the tests on CPU ranks
-pass the oracle as a stand-in.  This path is unmeasured on hardware: the
-runs of this build use one GPU.
+pass the oracle as a stand-in.  This path has not been measured on more
+than one GPU.
 """
 from __future__ import annotations
 
