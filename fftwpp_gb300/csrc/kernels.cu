@@ -126,9 +126,16 @@ __device__ __forceinline__ void outerFwdTile(const OuterPlan<T>& P, int ctile,
       int t=dTile(i), cc=i-t*tile;
       cplx<T> sum=mk((T) 0,(T) 0);
       int s0=posmod(t+c,m);
+      // The twiddle exponent advances by m r mod N from term to term.
+      int e=r != 0 ? twExp(s0,c,r,N) : 0;
+      const int de=r != 0 ? twStep(m,r,N) : 0;
       for(int s=s0; s < L; s += m) {
         cplx<T> v=y[s*tile+cc];
-        if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
+        if(r != 0) {
+          v=twmul<1>(v,tw[e]);
+          e += de;
+          if(e >= N) e -= N;
+        }
         sum=accum(sum,v);
       }
       x[sp(i)]=sum;

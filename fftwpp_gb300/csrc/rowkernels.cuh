@@ -409,12 +409,21 @@ __device__ __forceinline__ void convertStaged(cplx<T> *y, int i, int sh=0)
   }
 }
 
-// Exponent ((s-c) mod N)*r mod N of a residue twiddle.
+// Exponent ((s-c) mod N)*r mod N of a residue twiddle (r < N; 32-bit
+// arithmetic while the product fits).
 __device__ __forceinline__ int twExp(int s, int c, int r, int N)
 {
   int d=s-c;
   if(d < 0) d += N;
+  if(N <= 65536) return (int) (((unsigned) d*(unsigned) r) % (unsigned) N);
   return (int) (((unsigned long long) d*(unsigned long long) r) %
+                (unsigned long long) N);
+}
+
+// The exponent step m*r mod N between the terms s and s+m of a fold.
+__device__ __forceinline__ int twStep(int m, int r, int N)
+{
+  return (int) (((unsigned long long) m*(unsigned long long) r) %
                 (unsigned long long) N);
 }
 
@@ -623,9 +632,16 @@ __device__ __forceinline__ void rowConvRow(const RowPlan<T>& P,
         int t=dLd(i), col=i-t*ld;
         int s0=posmod(t+c,m);
         cplx<T> sum=mk((T) 0,(T) 0);
+        // The twiddle exponent advances by m r mod N from term to term.
+        int e=r != 0 ? twExp(s0,c,r,N) : 0;
+        const int de=r != 0 ? twStep(m,r,N) : 0;
         for(int s=s0; s < L; s += m) {
           cplx<T> v=fin[col*L+s];
-          if(r != 0) v=twmul<1>(v,tw[twExp(s,c,r,N)]);
+          if(r != 0) {
+            v=twmul<1>(v,tw[e]);
+            e += de;
+            if(e >= N) e -= N;
+          }
           sum=accum(sum,v);
         }
         x[sp(i)]=sum;
