@@ -136,6 +136,10 @@ def load():
     lib.fgb_parameters.argtypes = [sz, sz, sz, ctypes.c_int, P(sz), P(sz), P(sz)]
     lib.fgb_nextfftsize.restype = sz
     lib.fgb_nextfftsize.argtypes = [sz]
+    lib.fgb_fft_radices.restype = ctypes.c_int
+    lib.fgb_fft_radices.argtypes = [sz, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, P(ctypes.c_int),
+                                    ctypes.c_int]
     lib.fgb_index.restype = sz
     lib.fgb_index.argtypes = [ctypes.c_int, sz, sz, sz, sz, sz, sz, sz]
     lib.fgb_hermitian_symmetrize_x_device.restype = ctypes.c_int

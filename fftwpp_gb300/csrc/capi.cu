@@ -1047,6 +1047,19 @@ void fgb_parameters(size_t L, size_t M, size_t m, int centered,
 
 size_t fgb_nextfftsize(size_t m) {return nextfftsize(m);}
 
+int fgb_fft_radices(size_t n, int precision, int inplace, int wide,
+                    int *radix, int max)
+{
+  int r[FGB_MAXSTAGES];
+  const int nst=fftRadices((long) n,precision,inplace != 0,wide != 0,r);
+  if(nst < 0) {
+    setLastError("transform length "+std::to_string(n)+" has no radix plan");
+    return -1;
+  }
+  for(int s=0; s < nst && s < max; ++s) radix[s]=r[s];
+  return nst;
+}
+
 // Transformed index (fftBase::index, convolve.h:297-326; fftPadReal::index,
 // convolve.h:956-979).  D0 = n mod D (or D), the remainder block of the
 // residue loop (convolve.cc:701-703); overwrite is not modelled.

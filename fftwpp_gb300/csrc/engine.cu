@@ -165,19 +165,16 @@ const void *twiddles(long n, int prec)
   return d;
 }
 
-// Radices of an n-point transform.  The Stockham form wants the products of
-// earlier radices to be powers of two (odd radices last); the in-place
-// decimation forms want the spans n/(R0...Rs) to be powers of two (odd
-// radices first).  Either way the stage divisions become shifts.
-static FFTPlanDev fftPlan(long n, int prec, bool oddFirst=false,
-                          bool allow16=false)
+// Radices of an n-point transform into radix[] (at most FGB_MAXSTAGES);
+// returns their count, or -1 when n is not 2^a 3^b 5^c 7^d or needs too
+// many stages.  The Stockham form wants the products of earlier radices to
+// be powers of two (odd radices last); the in-place decimation forms want
+// the spans n/(R0...Rs) to be powers of two (odd radices first).  Either
+// way the stage divisions become shifts.
+int fftRadices(long n, int prec, bool oddFirst, bool allow16, int *radix)
 {
-  if(!smooth(n))
-    throw std::runtime_error("transform length "+std::to_string(n)+
-                             " is not a product of 2, 3, 5 and 7");
-  FFTPlanDev p;
-  p.n=(int) n;
-  p.nst=0;
+  if(n < 1 || !smooth(n)) return -1;
+  int nst=0, tmp[64];
   long r=n;
   // Largest radices first: 8, then 4 or 2, then odd primes.  FP32 in-place
   // transforms (allow16) also take radix 16 (4 x 4 in registers) where that
@@ -192,30 +189,45 @@ static FFTPlanDev fftPlan(long n, int prec, bool oddFirst=false,
     1+(k2+2)/4 < 1+(k2+3)/4;
   if(six) {k2 -= 1; r /= 2;}           // the factor 2 of the radix-6 stage
   if(wide && (k2+3)/4 < (k2+2)/3)
-    for(int i=0; i < k2-3*((k2+3)/4); ++i) {p.radix[p.nst++]=16; r /= 16;}
-  while(r % 8 == 0) {p.radix[p.nst++]=8; r /= 8;}
-  if(r % 4 == 0) {p.radix[p.nst++]=4; r /= 4;}
-  if(r % 2 == 0) {p.radix[p.nst++]=2; r /= 2;}
-  while(r % 7 == 0) {p.radix[p.nst++]=7; r /= 7;}
-  while(r % 5 == 0) {p.radix[p.nst++]=5; r /= 5;}
-  while(r % 3 == 0) {p.radix[p.nst++]=3; r /= 3;}
-  if(p.nst > FGB_MAXSTAGES)
-    throw std::runtime_error("too many FFT stages");
+    for(int i=0; i < k2-3*((k2+3)/4); ++i) {tmp[nst++]=16; r /= 16;}
+  while(r % 8 == 0) {tmp[nst++]=8; r /= 8;}
+  if(r % 4 == 0) {tmp[nst++]=4; r /= 4;}
+  if(r % 2 == 0) {tmp[nst++]=2; r /= 2;}
+  while(r % 7 == 0) {tmp[nst++]=7; r /= 7;}
+  while(r % 5 == 0) {tmp[nst++]=5; r /= 5;}
+  while(r % 3 == 0) {tmp[nst++]=3; r /= 3;}
+  if(nst > FGB_MAXSTAGES) return -1;
   if(six) {                              // one radix 3 becomes the radix 6
-    for(int s=p.nst-1; s >= 0; --s)
-      if(p.radix[s] == 3) {p.radix[s]=6; break;}
+    for(int s=nst-1; s >= 0; --s)
+      if(tmp[s] == 3) {tmp[s]=6; break;}
   }
+  int k=0;
   if(oddFirst) {
     // Odd radices first (the radix 6 with them, last), then the powers of
     // two, each group in order: every span after them is a power of two.
-    int k=0, tmp[FGB_MAXSTAGES];
-    for(int s=0; s < p.nst; ++s)
-      if(p.radix[s] % 2) tmp[k++]=p.radix[s];
-    for(int s=0; s < p.nst; ++s)
-      if(p.radix[s] == 6) tmp[k++]=p.radix[s];
-    for(int s=0; s < p.nst; ++s)
-      if(p.radix[s] % 2 == 0 && p.radix[s] != 6) tmp[k++]=p.radix[s];
-    for(int s=0; s < p.nst; ++s) p.radix[s]=tmp[s];
+    for(int s=0; s < nst; ++s)
+      if(tmp[s] % 2) radix[k++]=tmp[s];
+    for(int s=0; s < nst; ++s)
+      if(tmp[s] == 6) radix[k++]=tmp[s];
+    for(int s=0; s < nst; ++s)
+      if(tmp[s] % 2 == 0 && tmp[s] != 6) radix[k++]=tmp[s];
+  } else {
+    for(int s=0; s < nst; ++s) radix[k++]=tmp[s];
+  }
+  return nst;
+}
+
+static FFTPlanDev fftPlan(long n, int prec, bool oddFirst=false,
+                          bool allow16=false)
+{
+  FFTPlanDev p;
+  p.n=(int) n;
+  p.nst=fftRadices(n,prec,oddFirst,allow16,p.radix);
+  if(p.nst < 0) {
+    if(!smooth(n))
+      throw std::runtime_error("transform length "+std::to_string(n)+
+                               " is not a product of 2, 3, 5 and 7");
+    throw std::runtime_error("too many FFT stages");
   }
   p.tw=twiddles(n,prec);
   if(!p.tw) throw std::runtime_error("twiddle table allocation failed");

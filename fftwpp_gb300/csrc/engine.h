@@ -36,6 +36,8 @@ bool ispure(size_t m);
 void refParameters(size_t L, size_t M, size_t m, bool centered,
                    size_t& p, size_t& n, size_t& q);
 bool smooth(size_t n);   // n = 2^a 3^b 5^c 7^d
+// Radices of the shared-memory transforms of length n (engine.cu).
+int fftRadices(long n, int prec, bool oddFirst, bool allow16, int *radix);
 
 struct AxisPlan {
   int kind;

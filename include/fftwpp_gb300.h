@@ -307,6 +307,15 @@ void fgb_parameters(size_t L, size_t M, size_t m, int centered,
                     size_t *p, size_t *n, size_t *q);
 size_t fgb_nextfftsize(size_t m);
 
+/* Radices, stage by stage, of the shared-memory transforms of length n
+ * (host arithmetic, no GPU): inplace != 0 for the in-place
+ * decimation-in-frequency/time form (odd radices first), wide != 0 for the
+ * FP32 row and in-place outer transforms that may take radix 16 and 6.
+ * Writes at most max radices and returns their count, or -1 for a length
+ * that is not 2^a 3^b 5^c 7^d. */
+int fgb_fft_radices(size_t n, int precision, int inplace, int wide,
+                    int *radix, int max);
+
 /* Transformed index of entry i of residue block r (fftBase::index,
  * convolve.h:297-326, and fftPadReal::index, convolve.h:956-979) for the
  * reference's parameters (m,p,q,n,D) of a 1D transform. */

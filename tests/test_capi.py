@@ -69,6 +69,52 @@ def test_index_matches_reference(native_lib):
         assert np.array_equal(np.array(got), lay["idx"]), lay["key"]
 
 
+def _radices(lib, n, prec, inplace, wide):
+    buf = (ctypes.c_int * 32)()
+    k = lib.fgb_fft_radices(n, prec, int(inplace), int(wide), buf, 32)
+    return None if k < 0 else list(buf[:k])
+
+
+def test_fft_radix_plans(native_lib):
+    """The shared-memory transforms' radix sequences: every product equals
+    the length, the in-place form puts odd radices (and the radix 6) first
+    so every later span is a power of two, and radix 16 / 6 appear only in
+    wide FP32 plans, where they save a stage."""
+    from fftwpp_gb300._native import PRECISIONS
+    f64, f32, ff = PRECISIONS["f64"], PRECISIONS["f32"], PRECISIONS["ff"]
+    lengths = [n for n in range(1, 5000)
+               if native_lib.fgb_nextfftsize(n) == n]
+    for n in lengths:
+        for prec in (f64, f32, ff):
+            for inplace in (0, 1):
+                for wide in (0, 1):
+                    r = _radices(native_lib, n, prec, inplace, wide)
+                    assert r is not None and int(np.prod(r)) == n, (n, r)
+                    w = wide and inplace and prec == f32
+                    assert set(r) <= ({2, 3, 4, 5, 6, 7, 8, 16} if w else
+                                      {2, 3, 4, 5, 7, 8}), (n, prec, r)
+                    if inplace:
+                        span = n
+                        for k, R in enumerate(r):
+                            span //= R
+                            if R % 2 == 0 and R != 6:
+                                assert all(x % 2 == 0 and x != 6
+                                           for x in r[k:]), r
+                        assert span == 1
+                    if w:
+                        base = _radices(native_lib, n, prec, 1, 0)
+                        assert len(r) <= len(base), (n, r, base)
+                        if 16 in r or 6 in r:
+                            assert len(r) < len(base), (n, r, base)
+    assert _radices(native_lib, 768, f32, 1, 1) == [3, 16, 16]
+    assert _radices(native_lib, 1536, f32, 1, 1) == [6, 16, 16]
+    assert _radices(native_lib, 2048, f32, 1, 1) == [16, 16, 8]
+    assert _radices(native_lib, 512, f32, 1, 1) == [8, 8, 8]
+    assert _radices(native_lib, 768, f64, 0, 0) == [8, 8, 4, 3]
+    assert _radices(native_lib, 768, ff, 1, 1) == [3, 8, 8, 4]
+    assert _radices(native_lib, 11, f64, 0, 0) is None
+
+
 def test_hermitian_symmetrize_host(native_lib):
     """fftwpp_HermitianSymmetrizeX/XY agree with the oracle's restatement
     of convolve.h:1175-1258."""
