@@ -271,6 +271,37 @@ def test_zero_copy_host_path(native_lib, precision, case):
         native_lib.fgb_set_host_path(-1, -1)
 
 
+@pytest.mark.parametrize("precision", ["f64", "ff", "f32"])
+@pytest.mark.parametrize("case", [
+    ([H.PAD, H.CENTERED, H.PAD], [12, 10, 9], [23, 19, 17], "binary", 2, 1),
+    ([H.CENTERED, H.HERMITIAN], [31, 31], [46, 46], "realjacadj", 5, 4)])
+def test_host_path_column_ranges(native_lib, precision, case):
+    """Host calls with a complex outer axis copy the outputs out in column
+    ranges behind the last outer transform (and the inputs in, ahead of the
+    first): every output equals the device call's bit for bit, whichever
+    way the inputs take, in 3D and with four outputs."""
+    import torch
+    from fftwpp_gb300.gpu import HybridConvolution
+    kinds, L, M, mult, A, B = case
+    fs = _inputs(kinds, L, A, seed=29)
+    conv = HybridConvolution(kinds, L, M, A=A, B=B, mult=mult,
+                             precision=precision)
+    tdt = conv.dtype
+    dev = [torch.from_numpy(np.ascontiguousarray(f)).to(tdt).cuda()
+           for f in fs]
+    want = [o.cpu().numpy() for o in conv.convolve(*dev)]
+    try:
+        for wi in (0, 1, 2):
+            native_lib.fgb_set_host_path(wi, 0)
+            h = [torch.from_numpy(np.ascontiguousarray(f)).to(tdt)
+                 .pin_memory().numpy() for f in fs]
+            conv.convolve_host(*h)
+            for b in range(B):
+                assert np.array_equal(h[b], want[b]), (wi, b)
+    finally:
+        native_lib.fgb_set_host_path(-1, -1)
+
+
 def test_host_path_misaligned_pinned(native_lib):
     """Page-locked arrays that start off a 16-byte boundary take the copying
     path instead of failing."""
