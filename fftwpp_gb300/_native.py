@@ -136,6 +136,11 @@ def load():
     lib.fgb_parameters.argtypes = [sz, sz, sz, ctypes.c_int, P(sz), P(sz), P(sz)]
     lib.fgb_nextfftsize.restype = sz
     lib.fgb_nextfftsize.argtypes = [sz]
+    lib.fgb_batch_task_order.restype = ctypes.c_int
+    lib.fgb_batch_task_order.argtypes = [
+        ctypes.c_int, P(sz), P(ctypes.c_int), P(ctypes.c_int),
+        P(ctypes.c_int), ctypes.c_int, ctypes.c_int, ctypes.c_int, sz,
+        P(ctypes.c_int), P(ctypes.c_int), ctypes.c_int]
     lib.fgb_fft_radices.restype = ctypes.c_int
     lib.fgb_fft_radices.argtypes = [sz, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, P(ctypes.c_int),

@@ -254,6 +254,50 @@ long BatchConv::tuned(long L, long M, const std::vector<long>& cand)
   return best;
 }
 
+// Queue order of a batched launch (host logic only).  The long problems
+// pass through their staging: forward column tasks, row tasks, backward
+// column tasks.  They go in groups of about groupBytes of staging,
+// software-pipelined: step g queues the forward columns of group g, a share
+// of the small problems, the rows of group g-1 and the backward columns of
+// group g-2.  A problem's staging is then written and read back within
+// three groups, while the L2 still holds it, and every task's producers
+// were queued at least one group earlier, so a consumer rarely waits.
+std::vector<BatchTask> orderBatchTasks(const std::vector<LongTasks>& lng,
+                                       const std::vector<int>& small, int A,
+                                       int B, size_t groupBytes)
+{
+  std::vector<std::vector<const LongTasks *>> groups;
+  size_t acc=0;
+  for(const auto& o : lng) {
+    if(groups.empty() || (acc > 0 && acc+o.staging > groupBytes)) {
+      groups.emplace_back();
+      acc=0;
+    }
+    groups.back().push_back(&o);
+    acc += o.staging;
+  }
+  const int ng=(int) groups.size();
+  std::vector<BatchTask> tasks;
+  size_t nextSmall=0;
+  for(int g=0; g < ng+2; ++g) {
+    if(g < ng)
+      for(const LongTasks *p : groups[g])
+        for(int t=0; t < p->fwdTiles; ++t)
+          for(int a=0; a < A; ++a) tasks.push_back({TASK_COLFWD,p->prob,t,a});
+    const size_t endSmall=small.size()*(size_t) (g+1)/(size_t) (ng+2);
+    for(; nextSmall < endSmall; ++nextSmall)
+      tasks.push_back({TASK_SMALL,small[nextSmall],0,0});
+    if(g >= 1 && g-1 < ng)
+      for(const LongTasks *p : groups[g-1])
+        for(int r=0; r < p->rows; ++r) tasks.push_back({TASK_ROW,p->prob,r,0});
+    if(g >= 2)
+      for(const LongTasks *p : groups[g-2])
+        for(int t=0; t < p->bwdTiles; ++t)
+          for(int b=0; b < B; ++b) tasks.push_back({TASK_COLBWD,p->prob,t,b});
+  }
+  return tasks;
+}
+
 template<typename T>
 void BatchConv::build()
 {
@@ -358,54 +402,22 @@ void BatchConv::build()
   auto byCost=[](const Ord& x, const Ord& y) {return x.cost > y.cost;};
   std::sort(small.begin(),small.end(),byCost);
   std::sort(lng.begin(),lng.end(),byCost);
-  // The long problems pass through their staging: forward column tasks,
-  // row tasks, backward column tasks.  They go in groups of about
-  // GROUP_BYTES of staging, software-pipelined: step g queues the forward
-  // columns of group g, a share of the small problems, the rows of group
-  // g-1 and the backward columns of group g-2.  A problem's staging is then
-  // written and read back within three groups, while the L2 still holds
-  // it, and every task's producers were queued at least one group earlier,
-  // so a consumer rarely waits.  Measured on the 512-problem workload:
-  // 8 MB groups halve the FP32 launch's DRAM traffic (714 -> 364 MB) at the
-  // same speed; the FP64 launch, bound by its FP64 pipe, loses 12 % to the
-  // waits of groups that small and keeps 24 MB groups (1260 -> 1105 MB).
-  const size_t GROUP_BYTES=(prec == PREC_F64 ? 24u : 8u) << 20;
-  std::vector<std::vector<int>> groups;
-  size_t acc=0;
+  std::vector<LongTasks> lt;
   for(auto& o : lng) {
-    const size_t bytes=e*(size_t) probs[o.i].fwd.NX*A;
-    if(groups.empty() || (acc > 0 && acc+bytes > GROUP_BYTES)) {
-      groups.emplace_back();
-      acc=0;
-    }
-    groups.back().push_back(o.i);
-    acc += bytes;
+    const BatchProblem<T>& P=probs[o.i];
+    lt.push_back({o.i,e*(size_t) P.fwd.NX*A,
+                  (int) ceilquotient(P.fwd.C,P.fwd.tile),P.nrows,
+                  (int) ceilquotient(P.bwd.C,P.bwd.tile)});
   }
-  const int ng=(int) groups.size();
-  std::vector<BatchTask> tasks;
-  size_t nextSmall=0;
-  for(int g=0; g < ng+2; ++g) {
-    if(g < ng)
-      for(int i : groups[g]) {
-        const BatchProblem<T>& P=probs[i];
-        int tiles=(int) ceilquotient(P.fwd.C,P.fwd.tile);
-        for(int t=0; t < tiles; ++t)
-          for(int a=0; a < A; ++a) tasks.push_back({TASK_COLFWD,i,t,a});
-      }
-    const size_t endSmall=small.size()*(size_t) (g+1)/(size_t) (ng+2);
-    for(; nextSmall < endSmall; ++nextSmall)
-      tasks.push_back({TASK_SMALL,small[nextSmall].i,0,0});
-    if(g >= 1 && g-1 < ng)
-      for(int i : groups[g-1])
-        for(int r=0; r < probs[i].nrows; ++r) tasks.push_back({TASK_ROW,i,r,0});
-    if(g >= 2)
-      for(int i : groups[g-2]) {
-        const BatchProblem<T>& P=probs[i];
-        int tiles=(int) ceilquotient(P.bwd.C,P.bwd.tile);
-        for(int t=0; t < tiles; ++t)
-          for(int b=0; b < B; ++b) tasks.push_back({TASK_COLBWD,i,t,b});
-      }
-  }
+  std::vector<int> sm;
+  for(auto& o : small) sm.push_back(o.i);
+  // Measured on the 512-problem workload: 8 MB groups halve the FP32
+  // launch's DRAM traffic (714 -> 364 MB) at the same speed; the FP64
+  // launch, bound by its FP64 pipe, loses 12 % to the waits of groups that
+  // small and keeps 24 MB groups (1260 -> 1105 MB).
+  std::vector<BatchTask> tasks=orderBatchTasks(lt,sm,A,B,
+                                               (prec == PREC_F64 ? 24u : 8u)
+                                               << 20);
   ntasks=(int) tasks.size();
   nfwd0.resize(n);
   for(int i=0; i < n; ++i) nfwd0[i]=probs[i].nfwd;

@@ -4,10 +4,23 @@
 #pragma once
 
 #include "engine.h"
+#include "kernels.cuh"
 
 #include <vector>
 
 namespace fgb {
+
+// A long problem's task counts for the queue order: staging bytes, forward
+// column tiles (each once per input), row tasks, backward column tiles
+// (each once per output).
+struct LongTasks {
+  int prob;
+  size_t staging;
+  int fwdTiles, rows, bwdTiles;
+};
+std::vector<BatchTask> orderBatchTasks(const std::vector<LongTasks>& lng,
+                                       const std::vector<int>& small, int A,
+                                       int B, size_t groupBytes);
 
 class BatchConv {
 public:

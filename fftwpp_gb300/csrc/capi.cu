@@ -1047,6 +1047,26 @@ void fgb_parameters(size_t L, size_t M, size_t m, int centered,
 
 size_t fgb_nextfftsize(size_t m) {return nextfftsize(m);}
 
+int fgb_batch_task_order(int nlong, const size_t *staging,
+                         const int *fwdTiles, const int *rows,
+                         const int *bwdTiles, int nsmall, int inputs,
+                         int outputs, size_t groupBytes, int *type,
+                         int *problem, int max)
+{
+  std::vector<LongTasks> lt;
+  for(int i=0; i < nlong; ++i)
+    lt.push_back({i,staging[i],fwdTiles[i],rows[i],bwdTiles[i]});
+  std::vector<int> sm;
+  for(int i=0; i < nsmall; ++i) sm.push_back(nlong+i);
+  const std::vector<BatchTask> t=orderBatchTasks(lt,sm,inputs,outputs,
+                                                 groupBytes);
+  for(int k=0; k < (int) t.size() && k < max; ++k) {
+    type[k]=t[k].type;
+    problem[k]=t[k].prob;
+  }
+  return (int) t.size();
+}
+
 int fgb_fft_radices(size_t n, int precision, int inplace, int wide,
                     int *radix, int max)
 {

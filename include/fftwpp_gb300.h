@@ -307,6 +307,19 @@ void fgb_parameters(size_t L, size_t M, size_t m, int centered,
                     size_t *p, size_t *n, size_t *q);
 size_t fgb_nextfftsize(size_t m);
 
+/* Queue order of the batched launch's tasks (host arithmetic, no GPU), for
+ * nlong long problems with the given staging bytes, forward column tiles,
+ * row tasks and backward column tiles, and nsmall one-CTA problems
+ * (numbered after the long ones).  Writes at most max (type, problem)
+ * pairs, type 0 a small problem, 1 a forward column tile (once per input),
+ * 2 a row task, 3 a backward column tile (once per output), and returns
+ * the task count. */
+int fgb_batch_task_order(int nlong, const size_t *staging,
+                         const int *fwdTiles, const int *rows,
+                         const int *bwdTiles, int nsmall, int inputs,
+                         int outputs, size_t groupBytes, int *type,
+                         int *problem, int max);
+
 /* Radices, stage by stage, of the shared-memory transforms of length n
  * (host arithmetic, no GPU): inplace != 0 for the in-place
  * decimation-in-frequency/time form (odd radices first), wide != 0 for the
