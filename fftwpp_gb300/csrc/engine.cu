@@ -1639,7 +1639,11 @@ cudaError_t Conv::planOutputs(cudaStream_t s)
 // arrays of this plan's size (the best of three runs each, after one
 // untimed) and keeps the fastest; whole-array copies both ways if timing
 // fails.  The host writes the inputs before every timed run, as a caller
-// producing new data does, so the link reads lines the CPU holds dirty.
+// producing new data does, so the link reads lines the CPU holds dirty
+// (up to DIRTY_MAX bytes; larger plans time clean lines rather than spend
+// seconds rewriting them before every run).
+static const size_t DIRTY_MAX=(size_t) 512 << 20;
+
 void Conv::measureHostPath(cudaStream_t s)
 {
   hostWay[0]=hostWay[1]=HOST_COPY;
@@ -1677,7 +1681,7 @@ void Conv::measureHostPath(cudaStream_t s)
   double best=1e300;
   for(int rep=0; rep < 3 && ok; ++rep)
     for(const auto& w : ways) {
-      std::memset(h,0,stride*n);
+      if(stride*n <= DIRTY_MAX) std::memset(h,0,stride*n);
       ok=cudaEventRecord(e0,s) == cudaSuccess &&
         runZeroCopy(hin.data(),in.data(),hout.data(),out.data(),w.first,
                     w.second,s) ==
