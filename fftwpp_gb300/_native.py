@@ -116,6 +116,12 @@ def load():
     lib.fgb_debug_fail_allocation_after.argtypes = [ctypes.c_long]
     lib.fgb_set_autotune.restype = None
     lib.fgb_set_autotune.argtypes = [ctypes.c_int]
+    lib.fgb_wisdom_export.restype = sz
+    lib.fgb_wisdom_export.argtypes = [ctypes.c_char_p, sz]
+    lib.fgb_wisdom_import.restype = ctypes.c_int
+    lib.fgb_wisdom_import.argtypes = [ctypes.c_char_p]
+    lib.fgb_wisdom_forget.restype = None
+    lib.fgb_wisdom_forget.argtypes = []
     lib.fgb_set_residue_search.restype = None
     lib.fgb_set_residue_search.argtypes = [ctypes.c_int]
     lib.fgb_set_drop_in_precision.restype = ctypes.c_int

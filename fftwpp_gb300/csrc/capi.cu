@@ -749,6 +749,27 @@ int fgb_info(const fgb_conv *c, long *info)
 }
 
 void fgb_set_autotune(int on) {Conv::setAutotune(on != 0);}
+
+size_t fgb_wisdom_export(char *buf, size_t size)
+{
+  const std::string t=Conv::exportWisdom();
+  if(buf && size > 0) {
+    const size_t n=std::min(size-1,t.size());
+    std::memcpy(buf,t.data(),n);
+    buf[n]=0;
+  }
+  return t.size();
+}
+
+int fgb_wisdom_import(const char *text)
+{
+  if(!text) return -1;
+  const int n=Conv::importWisdom(text);
+  if(n < 0) setLastError("wisdom text does not parse");
+  return n;
+}
+
+void fgb_wisdom_forget(void) {Conv::forgetWisdom();}
 void fgb_set_residue_search(int on) {Conv::setResidueSearch(on != 0);}
 
 void fgb_debug_fail_allocation_after(long n) {failAllocationAfter(n);}

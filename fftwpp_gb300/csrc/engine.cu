@@ -10,6 +10,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <sstream>
 #include <stdexcept>
 #include <tuple>
 #include <type_traits>
@@ -626,13 +627,203 @@ static std::vector<long> residueCandidates(const AxisPlan& a, bool outer,
   return out;
 }
 
+// ---------------------------------------------------------------------------
+// Plan wisdom (engine.h).
+
+static std::mutex wisdomMutex;
+static std::map<std::string,std::string> wisdomMap;
+
+// The problem and the GPU a plan was tuned for, and whether its residue
+// blocks were searched.
+static std::string wisdomKey(int dim, const int *kinds, const long *L,
+                             const long *M, const long *mForce, int A, int B,
+                             int mult, int prec, long batch, bool searched)
+{
+  int dev=0, sms=0, major=0, minor=0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms,cudaDevAttrMultiProcessorCount,dev);
+  cudaDeviceGetAttribute(&major,cudaDevAttrComputeCapabilityMajor,dev);
+  cudaDeviceGetAttribute(&minor,cudaDevAttrComputeCapabilityMinor,dev);
+  cudaGetLastError();
+  std::string k="fgb1 sm"+std::to_string(major)+std::to_string(minor)+"x"+
+    std::to_string(sms)+" d"+std::to_string(dim);
+  for(int d=0; d < dim; ++d)
+    k += " "+std::to_string(kinds[d])+":"+std::to_string(L[d])+":"+
+      std::to_string(M[d])+":"+std::to_string(mForce ? mForce[d] : 0);
+  k += " A"+std::to_string(A)+" B"+std::to_string(B)+" u"+
+    std::to_string(mult)+" p"+std::to_string(prec)+" n"+std::to_string(batch)+
+    (searched ? " r1" : " r0");          // m searched or the cost model's
+  return k;
+}
+
+std::string Conv::exportWisdom()
+{
+  std::lock_guard<std::mutex> g(wisdomMutex);
+  std::string t;
+  for(const auto& kv : wisdomMap) t += kv.first+"\t"+kv.second+"\n";
+  return t;
+}
+
+int Conv::importWisdom(const std::string& text)
+{
+  std::vector<std::pair<std::string,std::string>> lines;
+  size_t pos=0;
+  while(pos < text.size()) {
+    size_t end=text.find('\n',pos);
+    if(end == std::string::npos) end=text.size();
+    const std::string line=text.substr(pos,end-pos);
+    pos=end+1;
+    if(line.empty()) continue;
+    const size_t tab=line.find('\t');
+    if(tab == std::string::npos || tab == 0 || line.compare(0,5,"fgb1 ") != 0)
+      return -1;
+    std::string value=line.substr(tab+1);
+    // 3 residue blocks, then per axis tile, threads, backward tile,
+    // threads, rows per CTA, then the four host-line tile numbers.
+    std::istringstream in(value);
+    long v;
+    int count=0;
+    while(in >> v) {
+      if(v < 0 || v > (1L << 40)) return -1;
+      ++count;
+    }
+    if(count != 22 || !in.eof()) return -1;
+    lines.push_back({line.substr(0,tab),value});
+  }
+  std::lock_guard<std::mutex> g(wisdomMutex);
+  for(const auto& kv : lines) wisdomMap[kv.first]=kv.second;
+  return (int) lines.size();
+}
+
+void Conv::forgetWisdom()
+{
+  std::lock_guard<std::mutex> g(wisdomMutex);
+  wisdomMap.clear();
+}
+
+std::string Conv::schedule() const
+{
+  std::string s;
+  for(int d=0; d < 3; ++d) {
+    const AxisPlan *a=d < I.dim ? &I.axis[d] : NULL;
+    for(int v : {a ? a->tile : 0,a ? a->thr : 0,a ? a->tileB : 0,
+                 a ? a->thrB : 0,a ? a->rpc : 0})
+      s += std::to_string(v)+" ";
+  }
+  for(int v : {hostTile,hostThr,hostTileB,hostThrB})
+    s += std::to_string(v)+" ";
+  s.pop_back();
+  return s;
+}
+
+// The schedule of a wisdom line, checked against what this plan's launches
+// can take (threads 128 or 256, tiles and rows per CTA the tuner would try
+// and that fit shared memory); false leaves the plan untouched.
+bool Conv::applySchedule(const std::string& text)
+{
+  std::istringstream in(text);
+  long v[19];
+  for(long& x : v)
+    if(!(in >> x)) return false;
+  const int dim=I.dim, prec=I.prec, A=I.A, B=I.B;
+  auto thrOk=[](long t) {return t == 128 || t == 256;};
+  auto p2=[](long t) {return t >= 1 && (t & (t-1)) == 0;};
+  AxisPlan ax[3];
+  for(int d=0; d < dim; ++d) ax[d]=I.axis[d];
+  for(int d=0; d < dim; ++d) {
+    const long *s=v+5*d;
+    AxisPlan& a=ax[d];
+    if(!thrOk(s[1]) || !thrOk(s[3])) return false;
+    a.thr=(int) s[1];
+    a.thrB=(int) s[3];
+    if(d < dim-1 && !I.longRow) {
+      const int tmax=wide(prec) ? 8 : 16;
+      if(!p2(s[0]) || !p2(s[2]) || s[0] > tmax || s[2] > tmax) return false;
+      size_t sf, sb;
+      if(a.kind == KIND_REAL) {
+        sf=FGB_BY_PREC(prec,outerRealSmem,a.L,a.N/2,(int) s[0]);
+        sb=FGB_BY_PREC(prec,outerRealSmem,a.L,a.N/2,(int) s[2]);
+      } else {
+        sf=FGB_BY_PREC(prec,outerFwdSmem,a.L,a.m,(int) s[0],(int) (a.p == 1));
+        sb=FGB_BY_PREC(prec,outerBwdSmem,a.L,a.m,(int) s[2],(int) a.q,
+                       (int) (a.p == 1));
+      }
+      if(sf > SMEM_MAX || sb > SMEM_MAX) return false;
+      a.tile=(int) s[0];
+      a.tileB=(int) s[2];
+    }
+    if(d == dim-1) {
+      const long r=s[4];
+      if(r != 1 && r != 2 && r != 3 && r != 4 && r != 6 && r != 8)
+        return false;
+      const size_t need=I.longRow ? rowNeed(prec,I.rowM,I.rowM,A,B,r,1) :
+        a.kind == KIND_HERMITIAN ? hermNeed(prec,a.stored,a.N/2,A,r) :
+        rowNeed(prec,a.stored,a.m,A,B,r,a.q == 1 && a.stored <= a.m);
+      if(need > SMEM_MAX) return false;
+      a.rpc=(int) r;
+    }
+  }
+  const long *h=v+15;
+  for(int k=0; k < 4; ++k)
+    if(h[k] != 0 && !(k % 2 ? thrOk(h[k]) : p2(h[k]) && h[k] <= 16))
+      return false;
+  for(int d=0; d < dim; ++d) I.axis[d]=ax[d];
+  hostTile=(int) h[0]; hostThr=(int) h[1];
+  hostTileB=(int) h[2]; hostThrB=(int) h[3];
+  return true;
+}
+
 Conv *Conv::create(int dim, const int *kinds, const long *L, const long *M,
                    const long *mForce, int A, int B, int mult, int prec,
                    long batch)
 {
+  if(!autotune)
+    return new Conv(dim,kinds,L,M,mForce,A,B,mult,prec,batch);
+  const std::string key=wisdomKey(dim,kinds,L,M,mForce,A,B,mult,prec,batch,
+                                  residueSearch);
+  std::string value;
+  {
+    std::lock_guard<std::mutex> g(wisdomMutex);
+    auto it=wisdomMap.find(key);
+    if(it != wisdomMap.end()) value=it->second;
+  }
+  if(!value.empty()) {
+    std::istringstream in(value);
+    long mw[3]={0,0,0};
+    bool ok=true;
+    for(long& m : mw) ok=ok && (bool) (in >> m);
+    std::string rest;
+    std::getline(in,rest);
+    if(ok) {
+      try {
+        std::unique_ptr<Conv> c(new Conv(dim,kinds,L,M,mw,A,B,mult,prec,batch,
+                                         false));
+        if(c->applySchedule(rest)) return c.release();
+      } catch(std::exception& x) {
+        // A record that no longer plans: plan afresh.  Failures of the
+        // device (allocations) are the caller's to see.
+        const std::string why=x.what();
+        if(why.find("allocation") != std::string::npos ||
+           why.find("memory") != std::string::npos) throw;
+      }
+    }
+  }
+  long mUsed[3]={0,0,0};
+  Conv *c=createSearched(dim,kinds,L,M,mForce,A,B,mult,prec,batch,mUsed);
+  std::lock_guard<std::mutex> g(wisdomMutex);
+  wisdomMap[key]=std::to_string(mUsed[0])+" "+std::to_string(mUsed[1])+" "+
+    std::to_string(mUsed[2])+" "+c->schedule();
+  return c;
+}
+
+Conv *Conv::createSearched(int dim, const int *kinds, const long *L,
+                           const long *M, const long *mForce, int A, int B,
+                           int mult, int prec, long batch, long *mUsed)
+{
+  for(int d=0; d < dim && d < 3; ++d) mUsed[d]=mForce ? mForce[d] : 0;
   // A caller's functor is not available at plan time: its plans keep the
   // cost model's residue blocks (the tiles are still timed).
-  if(!autotune || !residueSearch || mult == MULT_USER)
+  if(!residueSearch || mult == MULT_USER)
     return new Conv(dim,kinds,L,M,mForce,A,B,mult,prec,batch);
   long mf[3]={0,0,0};
   for(int d=0; d < dim && d < 3; ++d) mf[d]=mForce ? mForce[d] : 0;
@@ -650,6 +841,7 @@ Conv *Conv::create(int dim, const int *kinds, const long *L, const long *M,
   }
   if(!any) {
     base.reset();
+    for(int d=0; d < dim; ++d) mUsed[d]=mf[d];
     return new Conv(dim,kinds,L,M,mf,A,B,mult,prec,batch);
   }
 
@@ -703,6 +895,7 @@ Conv *Conv::create(int dim, const int *kinds, const long *L, const long *M,
   if(e0) cudaEventDestroy(e0);
   if(e1) cudaEventDestroy(e1);
   if(s) cudaStreamDestroy(s);
+  for(int d=0; d < dim; ++d) mUsed[d]=mf[d];
   return new Conv(dim,kinds,L,M,mf,A,B,mult,prec,batch);
 }
 

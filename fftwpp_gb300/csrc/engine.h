@@ -151,7 +151,26 @@ public:
   // Runs in the constructor unless disabled process-wide.
   static void setAutotune(bool on);
 
+  // Plan wisdom (the counterpart of the FFTW wisdom FFTW++ keeps in
+  // wisdom3.txt, fftw++.cc:31-72): create() records the timed choices of
+  // every plan it tunes (the residue blocks it forced and the schedule:
+  // column tiles, rows per CTA, threads, host-line tiles) under a key of
+  // the problem and the GPU, and a later create() of the same key rebuilds
+  // the plan from them without timing.  Text form: one "key<TAB>value"
+  // line per plan.  importWisdom merges (an imported line replaces one of
+  // the same key) and returns the lines taken, or -1 (nothing taken) for
+  // text that does not parse.
+  static std::string exportWisdom();
+  static int importWisdom(const std::string& text);
+  static void forgetWisdom();
+
 private:
+  std::string schedule() const;
+  bool applySchedule(const std::string& s);
+  static Conv *createSearched(int dim, const int *kinds, const long *L,
+                              const long *M, const long *mForce, int A,
+                              int B, int mult, int prec, long batch,
+                              long *mUsed);
   ConvInfo I;
   long batch;
   const RowLaunchers *user;        // row launches of a MULT_USER plan

@@ -23,12 +23,58 @@ from ._native import (CENTERED, F32, F64, FF, HERMITIAN, MULT, PAD,
 __all__ = ["HybridConvolution", "BatchedConvolution", "PaddedTransform",
            "PAD", "CENTERED", "HERMITIAN", "REAL", "default_M",
            "set_autotune", "set_residue_search", "set_host_path",
-           "set_ff_range_guard"]
+           "set_ff_range_guard", "export_wisdom", "import_wisdom",
+           "forget_wisdom", "save_wisdom", "load_wisdom"]
 
 
 def set_autotune(on: bool = True) -> None:
     """Plan-time timing of schedules and of m, process-wide (fgb_set_autotune)."""
     _native.load().fgb_set_autotune(int(bool(on)))
+
+
+def export_wisdom() -> str:
+    """The plan records of this process as text (fgb_wisdom_export)."""
+    lib = _native.load()
+    n = lib.fgb_wisdom_export(None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    lib.fgb_wisdom_export(buf, n + 1)
+    return buf.value.decode()
+
+
+def import_wisdom(text: str) -> int:
+    """Merge plan records (fgb_wisdom_import); returns the lines taken."""
+    n = _native.load().fgb_wisdom_import(text.encode())
+    if n < 0:
+        raise ValueError(_native.last_error())
+    return n
+
+
+def forget_wisdom() -> None:
+    """Drop every plan record of this process (fgb_wisdom_forget)."""
+    _native.load().fgb_wisdom_forget()
+
+
+def save_wisdom(path: str) -> None:
+    """Write the plan records to `path`, merged with those already there,
+    through a temporary file and a rename (as FFTW++ saves wisdom3.txt,
+    fftw++.cc:31-72)."""
+    import os
+    if os.path.exists(path):
+        with open(path) as f:
+            import_wisdom(f.read())
+    tmp = f"{path}.{os.getpid()}.tmp"
+    with open(tmp, "w") as f:
+        f.write(export_wisdom())
+    os.replace(tmp, path)
+
+
+def load_wisdom(path: str) -> int:
+    """Merge the plan records of `path` (none if it does not exist)."""
+    import os
+    if not os.path.exists(path):
+        return 0
+    with open(path) as f:
+        return import_wisdom(f.read())
 
 
 def set_residue_search(on: bool = True) -> None:

@@ -172,6 +172,21 @@ int fgb_info(const fgb_conv *c, long *info);
  * only: results are bit-identical either way. */
 void fgb_set_autotune(int on);
 
+/* Plan wisdom, the counterpart of the FFTW wisdom FFTW++ keeps in
+ * wisdom3.txt (fftw++.cc:31-72).  Every plan fgb_create tunes is recorded
+ * (its residue blocks and schedule, under a key of the problem and the
+ * GPU); a later fgb_create of the same key rebuilds the plan from the record
+ * without timing, so plans are deterministic across runs that share it.
+ * fgb_wisdom_export writes the records as text, one line per plan, into buf
+ * (at most size bytes, NUL-terminated when there is room) and returns the
+ * full length; fgb_wisdom_import merges such text (a line replaces the
+ * record of its key) and returns the lines taken, or -1, taking none, for
+ * text that does not parse; fgb_wisdom_forget drops every record.  A
+ * record whose schedule no longer fits the plan is ignored and replaced. */
+size_t fgb_wisdom_export(char *buf, size_t size);
+int fgb_wisdom_import(const char *text);
+void fgb_wisdom_forget(void);
+
 /* Timed residue search, process-wide (default on, effective while
  * autotuning is on): for every fftPad / fftPadCentered axis whose m is not
  * forced, fgb_create times whole convolutions with up to three residue
