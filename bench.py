@@ -1363,21 +1363,30 @@ def main():
                     help="skip the 3D real block of the default line")
     ap.add_argument("--quick", action="store_true",
                     help="skip the FP32 comparison leg")
+    ap.add_argument("--wisdom", help="plan wisdom file: loaded before the "
+                    "plans are made and saved after the run, so that a "
+                    "profiled run rebuilds the plans a plain run tuned")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.workload == "batched1d":
-        if args.impl == "reference":
-            return run_reference_batched(args)
-        return run_batched(args)
-    if args.workload == "jacobian2d_grad":
-        if args.impl == "reference":
-            return run_reference_grad(args)
-        return run_jacobian_grad(args)
-    w = override(WORKLOADS[args.workload], args)
     if args.impl == "reference":
-        return run_reference(args, w)
-    return run_ours(args, w)
+        if args.workload == "batched1d":
+            return run_reference_batched(args)
+        if args.workload == "jacobian2d_grad":
+            return run_reference_grad(args)
+        return run_reference(args, override(WORKLOADS[args.workload], args))
+    if args.wisdom:
+        from fftwpp_gb300 import gpu
+        gpu.load_wisdom(args.wisdom)
+    if args.workload == "batched1d":
+        rc = run_batched(args)
+    elif args.workload == "jacobian2d_grad":
+        rc = run_jacobian_grad(args)
+    else:
+        rc = run_ours(args, override(WORKLOADS[args.workload], args))
+    if args.wisdom:
+        gpu.save_wisdom(args.wisdom)
+    return rc
 
 
 if __name__ == "__main__":
